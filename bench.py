@@ -1,0 +1,408 @@
+#!/usr/bin/env python3
+"""Benchmark of the per-timestep simulation path on one GB300.
+
+Workload (``--workload c2``, the default): 1,000,000 Hodgkin-Huxley neurons,
+RK4 at dt = 0.01 ms, Gaussian distance-dependent connectivity (sigma = 0.1,
+100 out-edges per neuron, 1e8 synapses, int32 CSR), lognormal(-1, 1) nS
+weights, delays U{1..20} steps, 20 % inhibitory, drive U[6, 12] uA/cm^2,
+paracrine field on a 128^3 grid solved every 100 steps by Jacobi-PCG to a
+1e-6 relative residual.  All inputs are seeded synthetic data.
+
+One bench "step" is one paracrine period: 100 simulation timesteps (neuron
+update + spike delivery, replayed from a CUDA graph) plus one field solve, so
+``--steps 10`` covers the workload's 1,000 timesteps.
+
+Output: one JSON line (rank 0).  ``value`` is neuron-steps/s of the device-
+resident path; ``e2e`` is the same metric through the C-ABI entry point that
+takes host state buffers (host<->device copies inside the timed region).
+``--impl reference`` times the CPU oracle port of the same step on the host
+cores instead (the reference has no runnable CPU implementation of the path).
+Multi-GPU (torchrun): replicas only -- every rank simulates its own copy, no
+data-path collective; value = all ranks' neuron-steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "c2": dict(workload="hh_1M_gauss_k100_d20_grid128", n=1_000_000, kind="gauss", k=100, sigma=0.1,
+               w_mu=-1.0, w_sigma=1.0, dmax=20, inh=0.2, i_lo=6.0, i_hi=12.0, grid=128, timescale=100,
+               par_D=1.0, par_decay=0.0, total_steps=1000),
+    "c1": dict(workload="hh_1k_er_p0.01_grid32", n=1000, kind="er", p=0.01, w_max=0.5, dmax=1, inh=0.2,
+               i_lo=5.0, i_hi=15.0, grid=32, timescale=100, par_D=1.0, par_decay=0.0, total_steps=10000),
+}
+
+# Algorithmic bytes per unit:
+HH_BYTES_PER_NEURON_STEP = 60      # R: V,m,h,n,ge,gi,I (28 B) + ring (E,I) slot (8 B); W: 6 state floats (24 B)
+PCG_BYTES_PER_CELL_ITER = 40       # R: r,p_old (dir+apply), x,p,r,Ap (update); W: p,Ap,x,r -> 10 floats
+PUSH_BYTES_PER_EVENT = 13          # 4 B target + 4 B weight + 1 B delay + 4 B ring read-modify-write
+
+# DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
+# per unit of work; filled from the committed ncu summaries in profiles/.
+NCU_TRAFFIC_PER_UNIT = {"hh_step": None, "pcg_iteration": None}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------- distributed --
+
+def dist_env() -> tuple[int, int, int]:
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def dist_init(world: int):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist) -> None:
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def aggregate(units_per_rank: float, seconds_per_rank: float, dist) -> tuple[float, float]:
+    """Whole-job throughput: units of all ranks / the slowest rank's time."""
+    tmax = reduce_max(dist, seconds_per_rank)
+    units = reduce_sum(dist, units_per_rank)
+    return units / tmax, tmax
+
+
+# ------------------------------------------------------------------ clocks --
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.proc, self.path = device, None, None
+
+    def start(self) -> None:
+        try:
+            self.path = Path(f"/tmp/nn_clocks_{os.getpid()}.csv")
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# --------------------------------------------------------------- our arm ---
+
+def build_sim(nn, ctx, wl: dict, seed: int = 1):
+    c = nn.default_config(wl["n"])
+    c.seed = seed
+    c.max_delay = max(1, wl["dmax"])
+    c.grid = wl["grid"]
+    c.timescale = wl["timescale"]
+    c.par_D = wl["par_D"]
+    c.par_decay = wl["par_decay"]
+    c.par_rtol = 1e-6
+    c.par_max_iter = 5000
+    s = nn.Simulation(ctx, c)
+    if wl["kind"] == "gauss":
+        sp = nn.default_net_spec(nn.NN_NET_GAUSS)
+        sp.k, sp.sigma, sp.w_mu, sp.w_sigma, sp.dmax = wl["k"], wl["sigma"], wl["w_mu"], wl["w_sigma"], wl["dmax"]
+        sp.inh_fraction, sp.inh_random = wl["inh"], 1
+    else:
+        sp = nn.default_net_spec(nn.NN_NET_ER)
+        sp.p, sp.w_max, sp.inh_fraction, sp.inh_random = wl["p"], wl["w_max"], wl["inh"], 0
+    s.generate_network(sp)
+    s.init_state(-65.0, wl["i_lo"], wl["i_hi"])
+    return s
+
+
+def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
+    import neuronephys_clean_gb300 as nn
+    ctx = nn.Context(local_rank)
+    sim = build_sim(nn, ctx, wl)
+    P = wl["timescale"]
+    n = wl["n"]
+    # CUDA events bracket every neuron-update / delivery launch (event nodes in
+    # the captured period graph) and the solver iterations, inside the timed region
+    sim.set_kernel_timing(True)
+    for _ in range(args.warmup):  # warm-up also captures the period graph
+        sim.step(P)
+    ctx.synchronize()
+    launches0 = ctx.kernel_launches
+    _, spikes_a = sim.counters()
+    clocks = ClockSampler(local_rank)
+    barrier(dist)
+    clocks.start()
+    ctx.time_begin()
+    for _ in range(args.steps):
+        sim.step(P)
+    ms = ctx.time_end()
+    clock_info = clocks.stop()
+    barrier(dist)
+    launches = ctx.kernel_launches - launches0
+    _, spikes_b = sim.counters()
+    st = sim.solve_stats()
+    seconds = ms / 1e3
+    units = float(n) * P * args.steps
+    value, tmax = aggregate(units, seconds, dist)
+    spikes = spikes_b - spikes_a
+    nnz = sim.nnz
+    events = spikes * (nnz / n)
+
+    # mean launch durations of the last replayed period and the last solve
+    kt = sim.kernel_times()
+    hbm_peak, peak_kind = measured_peaks()
+    G = wl["grid"] ** 3
+    hh_ach = n * HH_BYTES_PER_NEURON_STEP / (kt.hh_step_ms * 1e-3) / 1e9 if kt.hh_step_ms > 0 else None
+    it_ms = kt.solve_ms / kt.solve_iterations if kt.solve_iterations else None
+    pcg_ach = G * PCG_BYTES_PER_CELL_ITER / (it_ms * 1e-3) / 1e9 if it_ms else None
+    per_period_hh = kt.hh_step_ms * P
+    per_period_pcg = kt.solve_ms
+    hh_roof = {"bound": "hbm", "kernel": "k_hh_step", "achieved": hh_ach, "peak": hbm_peak, "unit": "GB/s",
+               "frac": hh_ach / hbm_peak if hh_ach else None,
+               "traffic": (NCU_TRAFFIC_PER_UNIT["hh_step"] * n) if NCU_TRAFFIC_PER_UNIT["hh_step"] else None,
+               "algorithmic_bytes": n * HH_BYTES_PER_NEURON_STEP, "launch_ms": kt.hh_step_ms,
+               "peak_source": peak_kind}
+    pcg_roof = {"bound": "hbm", "kernel": "k_pcg_dir_apply+k_pcg_update (one PCG iteration)", "achieved": pcg_ach,
+                "peak": hbm_peak, "unit": "GB/s", "frac": pcg_ach / hbm_peak if pcg_ach else None,
+                "traffic": (NCU_TRAFFIC_PER_UNIT["pcg_iteration"] * G) if NCU_TRAFFIC_PER_UNIT["pcg_iteration"] else None,
+                "algorithmic_bytes": G * PCG_BYTES_PER_CELL_ITER, "launch_ms": it_ms, "peak_source": peak_kind}
+    dominant, other = (hh_roof, pcg_roof) if per_period_hh >= per_period_pcg else (pcg_roof, hh_roof)
+
+    # end to end through the host-buffer C-ABI call
+    e2e = None
+    if args.e2e_steps > 0:
+        pin_in = nn.PinnedArray((6, n), np.float32)
+        pin_out = nn.PinnedArray((6, n), np.float32)
+        for q, k in enumerate(("V", "M", "H", "N", "GE", "GI")):
+            pin_in.array[q] = sim.get_field(k)
+        sim.run_host(pin_in.array, P, pin_out.array)  # warm
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            sim.run_host(pin_in.array, P, pin_out.array)
+        e2e_s = time.perf_counter() - t0
+        e2e_val, _ = aggregate(float(n) * P * args.e2e_steps, e2e_s, dist)
+        e2e = {"value": e2e_val, "unit": "neuron-steps/s", "h2d_bytes_per_step": 6 * 4 * n,
+               "d2h_bytes_per_step": 6 * 4 * n + 8 * 2, "steps": args.e2e_steps}
+        pin_in.free()
+        pin_out.free()
+
+    if rank != 0:
+        return None
+    line = {
+        "metric": "neuron-steps/s", "value": value, "unit": "neuron-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded counter-based generators)",
+        "config": {"workload": wl["workload"], "neurons": n, "synapses": nnz, "timesteps_per_step": P,
+                   "dt_ms": 0.01, "grid": wl["grid"], "delivery": "push", "parallelism": "replicas",
+                   "l2": "inputs larger than L2 (CSR 0.9 GB, ring 168 MB, state 28 MB per step)"},
+        "synaptic_events_per_s": events / seconds if seconds else None,
+        "spikes_in_timed_region": spikes,
+        "cg": {"iterations_last_solve": st.iterations, "relres_last_solve": st.relres,
+               "time_to_tol_ms": kt.solve_ms, "grid": wl["grid"]},
+        "roofline": dominant, "roofline_other": other,
+        "kernel_ms": {"k_hh_step": kt.hh_step_ms, "k_deliver_push": kt.deliver_ms,
+                      "pcg_solve": kt.solve_ms, "samples": kt.samples},
+        "gpu_launches": int(launches),
+        "clocks": clock_info,
+        "e2e": e2e,
+    }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(sim, wl, args)
+    sim.close()
+    ctx.close()
+    return line
+
+
+# ---------------------------------------------------------- CPU baseline ---
+
+def cpu_baseline_sample(wl: dict, net_arrays, state6, i_drive, is_inh, seed: int, steps: int,
+                        solve: bool, vox=None) -> dict:
+    """Time the FP64 oracle port of the same step (OpenMP over the host cores)."""
+    import oracle
+    rp, col, w, d = net_arrays
+    n = wl["n"]
+    net = oracle.CSR(rp, col, w, d)
+    g = wl["grid"]
+    sim = oracle.Sim(net, is_inh, i_drive, seed, max(1, wl["dmax"]) + 1, state6, vox=vox,
+                     grid_cells=g ** 3 if vox is not None else 0)
+    sim.step()  # touch memory
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    t_steps = time.perf_counter() - t0
+    t_solve = 0.0
+    if solve:
+        dt_s = wl["timescale"] * 0.01 * 1e-3
+        alpha, beta = dt_s * wl["par_D"] * g * g, dt_s * wl["par_decay"]
+        b = sim.src if sim.src is not None else np.zeros(g ** 3)
+        b = b + 1e-3
+        t1 = time.perf_counter()
+        oracle.pcg7(b, np.zeros(g ** 3), (g, g, g), alpha, beta, rtol=1e-6)
+        t_solve = time.perf_counter() - t1
+    P = wl["timescale"]
+    per_step = t_steps / steps + t_solve / P
+    return {"value": n / per_step, "unit": "neuron-steps/s", "cores": int(oracle.lib().orc_num_threads()),
+            "kind": "port", "t_steps_s": t_steps, "t_solve_s": t_solve,
+            "sample": f"{steps} timesteps of all {n} neurons (FP64 oracle, OpenMP) + one {g}^3 PCG solve "
+                      f"amortised over {P} timesteps"}
+
+
+def cpu_baseline(sim, wl: dict, args) -> dict:
+    rp, col, w, d, inh = sim.get_network()
+    state6 = np.stack([sim.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")])
+    x, y, z = (sim.get_field(k) for k in ("X", "Y", "Z"))
+    g = wl["grid"]
+    ix = np.clip((x * np.float32(g)).astype(np.int32), 0, g - 1)
+    iy = np.clip((y * np.float32(g)).astype(np.int32), 0, g - 1)
+    iz = np.clip((z * np.float32(g)).astype(np.int32), 0, g - 1)
+    vox = (ix + g * (iy + g * iz)).astype(np.int32)
+    return cpu_baseline_sample(wl, (rp, col, w, d), state6, sim.get_field("IDRIVE"), inh, 1, args.cpu_steps, True,
+                               vox)
+
+
+def run_reference(args, wl: dict, rank: int) -> dict | None:
+    """The reference arm: the CPU oracle port of the same workload, all host threads."""
+    if rank != 0:
+        return None
+    import neuronephys_clean_gb300 as nn
+    # network + initial state come from the same generators (built on the GPU
+    # if one is present, else this arm is unavailable)
+    try:
+        ctx = nn.Context(0)
+    except Exception as e:  # pragma: no cover
+        return {"impl": "reference", "unavailable": f"no device to generate the seeded network: {e}"}
+    sim = build_sim(nn, ctx, wl)
+    rp, col, w, d, inh = sim.get_network()
+    state6 = np.stack([sim.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")])
+    idr = sim.get_field("IDRIVE")
+    x, y, z = (sim.get_field(k) for k in ("X", "Y", "Z"))
+    g = wl["grid"]
+    vox = (np.clip((x * np.float32(g)).astype(np.int32), 0, g - 1)
+           + g * (np.clip((y * np.float32(g)).astype(np.int32), 0, g - 1)
+                  + g * np.clip((z * np.float32(g)).astype(np.int32), 0, g - 1))).astype(np.int32)
+    sim.close()
+    ctx.close()
+    times = []
+    res = None
+    for i in range(args.warmup + args.steps):
+        res = cpu_baseline_sample(wl, (rp, col, w, d), state6, idr, inh, 1, args.cpu_steps, True, vox)
+        if i >= args.warmup:
+            times.append(wl["n"] / res["value"])
+    per_step = statistics.mean(times)
+    value = wl["n"] / per_step
+    cb = dict(res)
+    cb["value"] = value
+    return {"metric": "neuron-steps/s", "value": value, "unit": "neuron-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * wl["timescale"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded counter-based generators)", "impl": "reference",
+            "config": {"workload": wl["workload"], "neurons": wl["n"], "timesteps_per_step": wl["timescale"]},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "neuron-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    rank, world, local_rank = dist_env()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        line = run_reference(args, wl, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    from neuronephys_clean_gb300.build import build
+    if rank == 0 or world == 1:
+        build()
+    dist = dist_init(world)
+    barrier(dist)
+    if rank != 0:
+        build()  # no-op once rank 0 built it
+    args.cpu_baseline = args.cpu_baseline and rank == 0 and world == 1
+    line = run_ours(args, wl, dist, rank, local_rank)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

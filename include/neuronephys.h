@@ -1,0 +1,335 @@
+/*
+ * neuronephys.h -- C ABI of the GB300-native neuronephys simulation path.
+ *
+ * One process, one GB300 (sm_103a).  Every entry point takes plain pointers
+ * and sizes, returns an nn_status (never exits the process), and records a
+ * message retrievable with nn_ctx_last_error().  Pointers documented as
+ * "device" are CUDA device pointers (cudaMalloc'd by the caller or through
+ * nn_malloc); "host" pointers are ordinary host memory.
+ *
+ * Each block of declarations names the reference interface it replaces
+ * (file:line in NingyuanWang/neuronephys_clean).  The C++ adaptor classes in
+ * neuronephys.hpp keep the reference's class names and signatures on top of
+ * these functions, so a main.cu-style step loop compiles against them.
+ *
+ * Threading: one nn_ctx per host thread.  All work of a context is ordered on
+ * the context's CUDA stream.
+ */
+#ifndef NEURONEPHYS_H
+#define NEURONEPHYS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define NN_EXTERN extern "C"
+#else
+#define NN_EXTERN extern
+#endif
+#define NN_API NN_EXTERN __attribute__((visibility("default")))
+
+/* ------------------------------------------------------------ status ---- */
+/* Replaces gpuErrchk/cusparseErrchk's print-and-exit (src/defines.cuh:24-41). */
+typedef enum nn_status {
+    NN_OK = 0,
+    NN_ERR_INVALID_ARG = 1,
+    NN_ERR_OOM = 2,
+    NN_ERR_CUDA = 3,
+    NN_ERR_NOT_CONVERGED = 4,
+    NN_ERR_NUMERIC = 5,      /* non-finite neuron state detected on the device */
+    NN_ERR_TIMEOUT = 6,      /* a bounded device-side wait gave up */
+    NN_ERR_UNSUPPORTED = 7,
+    NN_ERR_NO_DEVICE = 8
+} nn_status;
+
+NN_API const char* nn_status_string(nn_status s);
+NN_API int nn_version(void);
+
+/* ----------------------------------------------------------- context ---- */
+typedef struct nn_ctx nn_ctx;
+NN_API nn_status nn_ctx_create(int device, nn_ctx** out);
+NN_API nn_status nn_ctx_destroy(nn_ctx* ctx);
+NN_API const char* nn_ctx_last_error(const nn_ctx* ctx);
+NN_API nn_status nn_ctx_synchronize(nn_ctx* ctx);
+/* Number of kernels this context has launched (graph replays count their nodes). */
+NN_API int64_t nn_ctx_kernel_launches(const nn_ctx* ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that interoperate. */
+NN_API void* nn_ctx_stream(nn_ctx* ctx);
+/* Wall time on the context stream: records a CUDA event now ... */
+NN_API nn_status nn_ctx_time_begin(nn_ctx* ctx);
+/* ... and here; synchronises and returns the elapsed milliseconds. */
+NN_API nn_status nn_ctx_time_end(nn_ctx* ctx, float* ms);
+/* Page-locked host memory (cudaMallocHost / cudaFreeHost). */
+NN_API nn_status nn_host_alloc(size_t bytes, void** hptr);
+NN_API nn_status nn_host_free(void* hptr);
+
+/* Device memory helpers, ordered on the context stream. */
+NN_API nn_status nn_malloc(nn_ctx* ctx, size_t bytes, void** dptr);
+NN_API nn_status nn_free(nn_ctx* ctx, void* dptr);
+NN_API nn_status nn_memcpy_h2d(nn_ctx* ctx, void* dst, const void* src, size_t bytes);
+NN_API nn_status nn_memcpy_d2h(nn_ctx* ctx, void* dst, const void* src, size_t bytes);
+NN_API nn_status nn_memset_d(nn_ctx* ctx, void* dst, int value, size_t bytes);
+
+/* ============================================================================
+ * Reference-semantics primitives (drop-in for the reference's classes)
+ * ========================================================================== */
+
+/* SoA slots of the HH sim_vars table (src/defines.cuh:57-78). */
+enum {
+    NN_HH_V = 0, NN_HH_M = 1, NN_HH_N = 2, NN_HH_H = 3,
+    NN_HH_LOCAL_Y = 4, NN_HH_IY = 5, NN_HH_EY = 6,
+    NN_HH_LOCAL_OUTPUT = 7, NN_HH_LOCAL_IN = 8, NN_HH_LOCAL_COUNT = 9,
+    NN_HH_EOUTPUT = 10, NN_HH_EIN = 11, NN_HH_ECOUNT = 12,
+    NN_HH_IOUTPUT = 13, NN_HH_IIN = 14, NN_HH_ICOUNT = 15,
+    NN_HH_APPCUR = 16, NN_HH_NUM_VARS = 17
+};
+
+/* Constants of the reference HH model: hh_params (src/defines.cuh:87-102) and
+ * the whole-brain HH namespace (src_wholebrain/ephys.cuh:45-61). */
+typedef struct nn_leapfrog_params {
+    float gna, ena, gk, ek, gl, el;
+    float Tmax, Vt, Kp, Ar, Ad;
+    float g_local, e_local, g_gaba, e_gaba, g_exc, e_exc;
+    float noise_mean, noise_intensity;
+} nn_leapfrog_params;
+/* variant 0: src/ (SCN/cortex benchmarks); 1: src_wholebrain/. */
+NN_API void nn_leapfrog_params_reference(nn_leapfrog_params* p, int variant);
+
+/* HHEphys::SimulateEphys(Float** sim_vars) (src/ephys.cu:98-103;
+ * src_wholebrain/ephys.cu:219-224): one semi-implicit Crank-Nicolson step of
+ * the reference HH model (kernel Leapfrog_HH, src/ephys.cu:28-96).
+ * vars: host array of NN_HH_NUM_VARS device pointers, each float[n].
+ * Noise: N(0,1) per neuron from the counter-based stream (seed, step); the
+ * reference's per-neuron curand XORWOW state is replaced by this stateless
+ * stream. */
+NN_API nn_status nn_hh_leapfrog_step(nn_ctx* ctx, float* const* vars, int n, float dt,
+                                     const nn_leapfrog_params* p, uint64_t seed, uint64_t step);
+
+/* AtomicCoupling (src/coupling.cuh:17-38, src_wholebrain/coupling.cuh:26-43). */
+typedef struct nn_coupling nn_coupling;
+enum { NN_SIGNAL_COUNT = 0,   /* add 1 per firing presynaptic neuron (src/coupling.cu:46) */
+       NN_SIGNAL_OUTPUT = 1   /* add the presynaptic output (src_wholebrain/coupling.cu:31) */ };
+NN_API nn_status nn_coupling_create(nn_ctx* ctx, int n, nn_coupling** out);
+NN_API nn_status nn_coupling_destroy(nn_coupling* c);
+/* AtomicCoupling::operator()(AdjacencyList const&, Float* spikes, Float const*
+ * neuron_outputs) (src/coupling.cu:111-141) / PerformCoupling
+ * (src_wholebrain/coupling.cu:43-69): inputs[] is zeroed, neurons whose output
+ * exceeds 0.1 fire (src/coupling.cu:103-109), their ascending index list is
+ * stored, and every CSR entry of a firing row adds the signal to its target.
+ * d_indices/d_offsets: device CSR (row = presynaptic).  num_firing (host) may
+ * be NULL, which keeps the call free of host synchronisation. */
+NN_API nn_status nn_coupling_run(nn_coupling* c, const int* d_indices, const int* d_offsets,
+                                 float* d_inputs, const float* d_outputs, int signal_mode,
+                                 int* num_firing);
+/* AtomicCoupling::operator()(ChunkedAdjacencyList const&, ...)
+ * (src/coupling.cu:143-178): chunk c holds target indices local to
+ * [c*n_per_chunk, (c+1)*n_per_chunk).  d_chunk_indices/d_chunk_offsets are
+ * host arrays of nchunks device pointers.  Equivalent result to
+ * nn_coupling_run on the unchunked list, for any n. */
+NN_API nn_status nn_coupling_run_chunked(nn_coupling* c, int nchunks, int n_per_chunk,
+                                         const int* const* d_chunk_indices,
+                                         const int* const* d_chunk_offsets,
+                                         float* d_inputs, const float* d_outputs, int* num_firing);
+/* GetFiringNeurons() (src/coupling.cuh:37): device pointer to the n-entry
+ * buffer whose first num_firing entries are the ascending firing indices
+ * (entries beyond keep earlier calls' values, as the reference's do). */
+NN_API const int* nn_coupling_firing_list(const nn_coupling* c);
+/* Device pointer to the int count of the last call's firing neurons. */
+NN_API const int* nn_coupling_firing_count(const nn_coupling* c);
+
+/* Network construction (src/network_factory.cuh:6-67). */
+/* UniformRandomNetwork::Generate (src/network_factory.cu:96-131): host-side,
+ * bit-identical to the reference's std::default_random_engine (minstd_rand0)
+ * + libstdc++ uniform_int_distribution draw.  engine_state is the shared
+ * engine (1 = default-constructed, the reference's UnseededRandomEngine,
+ * src/defines.cu:4-10) and is advanced in place.  h_indices: n*ncouple ints,
+ * h_offsets: n+1 ints. */
+NN_API nn_status nn_net_uniform_random(int n, int ncouple, uint32_t* engine_state,
+                                       int* h_indices, int* h_offsets);
+/* Network::ToAdjacencyList(Float*& Tcount) (src/network_factory.cu:5-27):
+ * in-degree of every neuron as float, computed on the device. */
+NN_API nn_status nn_net_tcount(nn_ctx* ctx, const int* d_indices, int64_t nnz, int n, float* d_tcount);
+/* Network::ToChunkedAdjacencyList (src/network_factory.cu:29-85) on the
+ * device.  d_chunk_indices[c] must hold nnz ints and d_chunk_offsets[c] n+1
+ * ints (host arrays of device pointers); chunk_nnz (host) receives each
+ * chunk's entry count. */
+NN_API nn_status nn_net_to_chunked(nn_ctx* ctx, const int* d_indices, const int* d_offsets, int n,
+                                   int nchunks, int n_per_chunk, int* const* d_chunk_indices,
+                                   int* const* d_chunk_offsets, int64_t* chunk_nnz);
+
+/* ParacrineModule (src/paracrine.cuh:212-267) with the reference's
+ * Crank-Nicolson / 27-point compact-Laplacian CG (src/paracrine.cu:19-134)
+ * and trilinear scatter/interpolation (src/paracrine.cu:136-296). */
+typedef struct nn_paracrine nn_paracrine;
+typedef struct nn_paracrine_ref_params {
+    int nx, ny, nz;
+    float h;              /* spatial_gridsize */
+    float D, decay;       /* diffusion_coef, decay_coef */
+    float par_dt;         /* solver time step */
+    float coup_strength;  /* source added per firing neuron */
+    int max_iter;         /* 20 in the reference (src/paracrine.cu:106) */
+    float abs_tol;        /* absolute ||r||^2 bound, 1e-6 (src/paracrine.cuh:164) */
+    int quirk_rhs;        /* 1: right-hand side uses h where dt belongs (src/paracrine.cu:105) */
+    int quirk_firing_list;/* 1: fine update keyed on the compacted list buffer (src/paracrine.cuh:250-252) */
+} nn_paracrine_ref_params;
+NN_API void nn_paracrine_ref_params_default(nn_paracrine_ref_params* p);
+/* ParacrineModule(Float*& d_g_paracrine, N, nx, ny, nz, par_dt, timescale,
+ * coup, h, D, decay, x, y, z) (src/paracrine.cuh:230-244).  d_x/d_y/d_z:
+ * centred neuron positions (device, float[n]); d_g_paracrine (device,
+ * float[n]) receives the interpolated density. */
+NN_API nn_status nn_paracrine_ref_create(nn_ctx* ctx, const nn_paracrine_ref_params* p, int n,
+                                         const float* d_x, const float* d_y, const float* d_z,
+                                         float* d_g_paracrine, nn_paracrine** out);
+NN_API nn_status nn_paracrine_destroy(nn_paracrine* pm);
+/* update_on_fine_timescale(AtomicCoupling const&) (src/paracrine.cuh:246-253). */
+NN_API nn_status nn_paracrine_ref_fine(nn_paracrine* pm, const nn_coupling* c);
+/* update_on_own_timescale() (src/paracrine.cuh:255-265): scatter, CN solve,
+ * interpolate, reset sources, copy to d_g_paracrine.  iters/final_rr (host)
+ * may be NULL. */
+NN_API nn_status nn_paracrine_ref_own(nn_paracrine* pm, int* iters, float* final_rr);
+/* get_grid().density() (src/paracrine.cuh:266, :170-172): device pointer to
+ * the nx*ny*nz density (x fastest). */
+NN_API float* nn_paracrine_density(nn_paracrine* pm);
+/* Device pointer to the per-neuron source accumulator (float[n]). */
+NN_API float* nn_paracrine_sources(nn_paracrine* pm);
+
+/* ============================================================================
+ * GB300 simulation step: RK4 Hodgkin-Huxley + weighted, delayed spike delivery
+ * + 7-point backward-Euler paracrine field with Jacobi-PCG.
+ * The step loop of the reference (_RunAndPrintSimulation, src/main.cu:112-182;
+ * MouseCortex::Simulate, src_wholebrain/mouse_cortex.cu:104-120) becomes one
+ * device-resident object whose step sequence is captured in a CUDA graph.
+ * ========================================================================== */
+
+typedef struct nn_hh_params {
+    float C, gNa, gK, gL, ENa, EK, EL;     /* uF/cm^2, mS/cm^2, mV */
+    float E_exc, E_inh, tau_exc, tau_inh;  /* synapse reversal (mV) and decay (ms) */
+    float v_thresh;                        /* upward-crossing spike threshold (mV) */
+    float noise_sigma;                     /* N(0, sigma^2) current per step, uA/cm^2 */
+    float dt;                              /* ms */
+    float g_par, E_par;                    /* paracrine conductance per unit density, reversal */
+} nn_hh_params;
+NN_API void nn_hh_params_standard(nn_hh_params* p);
+
+enum { NN_DELIVERY_PUSH = 0, NN_DELIVERY_PULL = 1 };
+
+typedef struct nn_sim_config {
+    int n;                 /* neurons */
+    int max_delay;         /* largest synaptic delay in steps (>= 1) */
+    uint64_t seed;         /* master seed of every counter-based stream */
+    nn_hh_params hp;
+    int delivery;          /* NN_DELIVERY_PUSH or NN_DELIVERY_PULL */
+    int64_t raster_capacity; /* spikes recorded as (step, neuron); 0 = off */
+    /* paracrine field: grid^3 cells over the unit cube, solved every
+     * `timescale` steps with dt_solve = timescale * dt */
+    int grid;              /* 0 = no paracrine field */
+    int timescale;
+    float par_D;           /* diffusivity, (unit cube)^2 / s */
+    float par_decay;       /* linear uptake, 1/s */
+    double par_rtol;       /* relative residual target */
+    int par_max_iter;
+    int threads_per_block; /* 0 = autotuned default */
+    int neurons_per_thread;/* 1, 2 or 4; 0 = autotuned default */
+} nn_sim_config;
+NN_API void nn_sim_config_default(nn_sim_config* c, int n);
+
+typedef struct nn_sim nn_sim;
+NN_API nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim** out);
+NN_API nn_status nn_sim_destroy(nn_sim* s);
+
+/* Network (CSR, row = presynaptic neuron): host arrays, copied to the device.
+ * Replaces Network::ToAdjacencyList + AtomicCoupling construction; the CSC
+ * transpose used by pull delivery is built on the device. */
+NN_API nn_status nn_sim_set_network(nn_sim* s, const int64_t* h_row_ptr, const int32_t* h_col,
+                                    const float* h_weight, const uint8_t* h_delay, int64_t nnz,
+                                    const uint8_t* h_is_inh);
+
+/* Counter-based network generators run on the device (replace the host-serial
+ * UniformRandomNetwork / NormalNetwork generators, src/network_factory.cu:96-131,
+ * src_wholebrain/network_factory.cu:95-138). */
+enum { NN_NET_ER = 1, NN_NET_GAUSS = 2, NN_NET_BLOCK = 3 };
+typedef struct nn_net_spec {
+    int kind;
+    double p;              /* ER: connection probability (no self-loops) */
+    float w_max;           /* ER: weights U[0, w_max] nS */
+    int k;                 /* GAUSS / BLOCK: out-degree per neuron */
+    double sigma;          /* GAUSS: kernel standard deviation (unit cube) */
+    double w_mu, w_sigma;  /* GAUSS / BLOCK: lognormal weights (nS) */
+    int dmax;              /* GAUSS: delays U{1..dmax}; ER: 0 or 1 = delay 1 */
+    double inh_fraction;   /* fraction of inhibitory neurons */
+    int inh_random;        /* 0: the last fraction of indices; 1: per-neuron draw */
+    int n_regions;         /* BLOCK: regions of lognormal size */
+    double region_size_sigma, density_sigma;
+    int block_dmax;        /* BLOCK: delays 1..block_dmax by centroid distance */
+} nn_net_spec;
+NN_API void nn_net_spec_default(nn_net_spec* sp, int kind);
+NN_API nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* spec);
+NN_API nn_status nn_sim_network_size(nn_sim* s, int64_t* nnz);
+/* Download the device network (any pointer may be NULL). */
+NN_API nn_status nn_sim_get_network(nn_sim* s, int64_t* h_row_ptr, int32_t* h_col, float* h_weight,
+                                    uint8_t* h_delay, uint8_t* h_is_inh);
+/* Download the device CSC (columns = postsynaptic; within a column, entries
+ * in ascending CSR position). */
+NN_API nn_status nn_sim_get_csc(nn_sim* s, int64_t* h_col_ptr, int32_t* h_src, float* h_weight,
+                                uint8_t* h_delay);
+
+/* Per-neuron fields. */
+enum { NN_F_V = 0, NN_F_M, NN_F_H, NN_F_N, NN_F_GE, NN_F_GI, NN_F_IDRIVE, NN_F_GNA_SCALE,
+       NN_F_X, NN_F_Y, NN_F_Z, NN_F_UPAR, NN_F_COUNT };
+NN_API nn_status nn_sim_set_field(nn_sim* s, int field, const float* h_values);
+NN_API nn_status nn_sim_get_field(nn_sim* s, int field, float* h_values);
+/* Device pointer of a field (for zero-copy callers). */
+NN_API float* nn_sim_field_ptr(nn_sim* s, int field);
+/* Default initial state: V = v0, gates at their steady state, synapses 0,
+ * drive I ~ U[i_lo, i_hi] from the seed, positions on the jittered lattice. */
+NN_API nn_status nn_sim_init_state(nn_sim* s, float v0, float i_lo, float i_hi);
+
+/* Advance nsteps on the device (no host synchronisation). */
+NN_API nn_status nn_sim_step(nn_sim* s, int nsteps);
+/* End-to-end call: copy the state (6*n floats: V,m,h,n,ge,gi planes) from
+ * host memory, advance nsteps, copy the state back and return the number of
+ * spikes emitted. */
+NN_API nn_status nn_sim_run_host(nn_sim* s, const float* h_state_in, int nsteps, float* h_state_out,
+                                 int64_t* h_spikes);
+/* Current step index and total spikes so far (synchronises). */
+NN_API nn_status nn_sim_counters(nn_sim* s, int64_t* step, int64_t* total_spikes);
+/* Recorded raster (ascending (step, neuron) after sorting on the host). */
+NN_API nn_status nn_sim_get_raster(nn_sim* s, int64_t cap, int32_t* h_step, int32_t* h_neuron,
+                                   int64_t* count);
+/* Paracrine density (grid^3 floats, x fastest) and last solve statistics. */
+NN_API nn_status nn_sim_get_density(nn_sim* s, float* h_u);
+NN_API nn_status nn_sim_set_density(nn_sim* s, const float* h_u);
+typedef struct nn_solve_stats { int iterations; double relres; int solves; int converged; } nn_solve_stats;
+NN_API nn_status nn_sim_solve_stats(nn_sim* s, nn_solve_stats* st);
+/* Kernel timing: when enabled, CUDA events bracket every neuron-update and
+ * delivery launch (also inside the captured graph) and every paracrine solve's
+ * iterations.  nn_sim_kernel_times returns the mean durations (ms) over the
+ * launches of the most recent graph replay / eager steps and the last solve. */
+NN_API nn_status nn_sim_set_kernel_timing(nn_sim* s, int enable);
+typedef struct nn_kernel_times {
+    float hh_step_ms;      /* mean k_hh_step duration */
+    float deliver_ms;      /* mean delivery-kernel duration */
+    int samples;           /* launches averaged */
+    float solve_ms;        /* last paracrine solve, all iterations */
+    int solve_iterations;
+} nn_kernel_times;
+NN_API nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out);
+
+/* ============================================================================
+ * Standalone 7-point Jacobi-PCG (backward-Euler diffusion with uptake).
+ * A = (1 + beta) I + alpha * L_D, L_D the 7-point operator with harmonic-mean
+ * face coefficients of the cell field Dcell (or 1 when Dcell is NULL), zero
+ * values outside the grid.  Vectors FP32; dot products and norms FP64.
+ * ========================================================================== */
+typedef struct nn_pcg nn_pcg;
+NN_API nn_status nn_pcg_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta,
+                               const float* d_Dcell, nn_pcg** out);
+NN_API nn_status nn_pcg_destroy(nn_pcg* pc);
+/* y = A x (device vectors). */
+NN_API nn_status nn_pcg_apply(nn_pcg* pc, const float* d_x, float* d_y);
+/* Solve A x = b to ||r|| <= rtol ||b||; d_x holds the initial guess. */
+NN_API nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter,
+                              int* iters, double* relres);
+
+#endif

@@ -1,0 +1,549 @@
+"""GB300-native neuronephys simulation path (Python host side).
+
+Mirrors the reference's C++ interfaces over the C ABI in include/neuronephys.h:
+
+* ``HHEphys``            -- Ephys/HHEphys::SimulateEphys (src/ephys.cuh:6-31)
+* ``AtomicCoupling``     -- AtomicCoupling::operator() (src/coupling.cuh:17-38)
+* ``UniformRandomNetwork`` / ``Network.to_adjacency_list`` /
+  ``Network.to_chunked_adjacency_list`` -- src/network_factory.cuh:6-67
+* ``ParacrineModule``    -- src/paracrine.cuh:212-267
+* ``Simulation``         -- the step loop (src/main.cu:112-182) as one
+  device-resident object: RK4 HH, delayed weighted delivery, 7-point PCG field
+* ``PCG``                -- standalone 7-point Jacobi-PCG
+
+Every call runs CUDA code in libneuronephys; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import HHParams, KernelTimes, LeapfrogParams, NetSpec, ParacrineRefParams, SimConfig, SolveStats
+
+__all__ = ["NNError", "Context", "DeviceArray", "HHEphys", "AtomicCoupling", "AdjacencyList",
+           "ChunkedAdjacencyList", "UniformRandomNetwork", "ParacrineModule", "Simulation", "PCG",
+           "SimConfig", "HHParams", "NetSpec", "LeapfrogParams", "ParacrineRefParams",
+           "lib", "NN_SIGNAL_COUNT", "NN_SIGNAL_OUTPUT", "FIELDS"]
+
+NN_SIGNAL_COUNT, NN_SIGNAL_OUTPUT = 0, 1
+NN_DELIVERY_PUSH, NN_DELIVERY_PULL = 0, 1
+NN_NET_ER, NN_NET_GAUSS, NN_NET_BLOCK = 1, 2, 3
+FIELDS = {name: i for i, name in enumerate(
+    ["V", "M", "H", "N", "GE", "GI", "IDRIVE", "GNA_SCALE", "X", "Y", "Z", "UPAR"])}
+# reference SoA slots (src/defines.cuh:57-78)
+SIM_PARAMS = ["V", "M", "N", "H", "LOCAL_Y", "IY", "EY", "LOCAL_OUTPUT", "LOCAL_IN", "LOCAL_COUNT",
+              "EOUTPUT", "EIN", "ECOUNT", "IOUTPUT", "IIN", "ICOUNT", "APPCUR"]
+
+
+def lib() -> C.CDLL:
+    return L.load()
+
+
+class NNError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+def _check(st: int, ctx: "Context | None" = None, what: str = "") -> None:
+    if st != 0:
+        l = lib()
+        detail = l.nn_status_string(st).decode()
+        if ctx is not None and ctx.handle:
+            le = l.nn_ctx_last_error(ctx.handle).decode()
+            if le:
+                detail += ": " + le
+        raise NNError(st, f"{what}: {detail}" if what else detail)
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    assert a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One CUDA device and stream (nn_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.handle = C.c_void_p()
+        _check(lib().nn_ctx_create(device, C.byref(self.handle)), None, "nn_ctx_create")
+
+    def close(self) -> None:
+        if self.handle:
+            lib().nn_ctx_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self) -> None:
+        _check(lib().nn_ctx_synchronize(self.handle), self, "synchronize")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().nn_ctx_kernel_launches(self.handle))
+
+    def time_begin(self) -> None:
+        """Record a CUDA event on the context stream."""
+        _check(lib().nn_ctx_time_begin(self.handle), self, "time_begin")
+
+    def time_end(self) -> float:
+        """Record a second event, synchronise, return the elapsed ms."""
+        ms = C.c_float()
+        _check(lib().nn_ctx_time_end(self.handle, C.byref(ms)), self, "time_end")
+        return float(ms.value)
+
+    def empty(self, shape, dtype) -> "DeviceArray":
+        return DeviceArray(self, shape, dtype)
+
+    def to_device(self, a: np.ndarray) -> "DeviceArray":
+        a = np.ascontiguousarray(a)
+        d = DeviceArray(self, a.shape, a.dtype)
+        d.copy_from(a)
+        return d
+
+
+class PinnedArray:
+    """Page-locked host array (nn_host_alloc), viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        self.ptr = C.c_void_p()
+        _check(lib().nn_host_alloc(max(nbytes, 1), C.byref(self.ptr)), None, "nn_host_alloc")
+        buf = (C.c_char * max(nbytes, 1)).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            lib().nn_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class DeviceArray:
+    """Device buffer owned through the C ABI (nn_malloc/nn_free)."""
+
+    def __init__(self, ctx: Context, shape, dtype):
+        self.ctx = ctx
+        self.shape = tuple(np.atleast_1d(shape).tolist()) if not isinstance(shape, tuple) else shape
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self.ptr = C.c_void_p()
+        _check(lib().nn_malloc(ctx.handle, max(self.nbytes, 1), C.byref(self.ptr)), ctx, "nn_malloc")
+
+    @property
+    def value(self) -> int:
+        return int(self.ptr.value or 0)
+
+    def copy_from(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        assert a.nbytes == self.nbytes, (a.nbytes, self.nbytes)
+        _check(lib().nn_memcpy_h2d(self.ctx.handle, self.ptr, _ptr(a), a.nbytes), self.ctx, "h2d")
+
+    def numpy(self) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype)
+        _check(lib().nn_memcpy_d2h(self.ctx.handle, _ptr(out), self.ptr, self.nbytes), self.ctx, "d2h")
+        return out
+
+    def zero(self) -> None:
+        _check(lib().nn_memset_d(self.ctx.handle, self.ptr, 0, self.nbytes), self.ctx, "memset")
+
+    def free(self) -> None:
+        if self.ptr and self.ctx.handle:
+            lib().nn_free(self.ctx.handle, self.ptr)
+        self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------- reference mirrors --
+
+class HHEphys:
+    """HHEphys with the struct-of-arrays it owns (src_wholebrain/ephys.cuh:6-43).
+
+    ``simulate_ephys()`` is HHEphys::SimulateEphys: one Leapfrog_HH step
+    (src/ephys.cu:28-103) of all neurons at dt = leapfrog_dt = 0.4 ms.
+    """
+
+    def __init__(self, ctx: Context, n: int, variant: int = 0, seed: int = 0, dt: float = 0.4):
+        self.ctx, self.n, self.seed, self.dt, self.step = ctx, n, seed, dt, 0
+        self.params = LeapfrogParams()
+        lib().nn_leapfrog_params_reference(C.byref(self.params), variant)
+        self.vars = [ctx.empty((n,), np.float32) for _ in SIM_PARAMS]
+        for v in self.vars:
+            v.zero()
+
+    def sim_vars_cpu(self) -> list[int]:
+        return [v.value for v in self.vars]
+
+    def set(self, name: str, values) -> None:
+        self.vars[SIM_PARAMS.index(name)].copy_from(np.broadcast_to(np.asarray(values, np.float32), (self.n,)))
+
+    def get(self, name: str) -> np.ndarray:
+        return self.vars[SIM_PARAMS.index(name)].numpy()
+
+    def simulate_ephys(self) -> None:
+        table = (C.c_void_p * len(self.vars))(*[v.value for v in self.vars])
+        _check(lib().nn_hh_leapfrog_step(self.ctx.handle, table, self.n, self.dt, C.byref(self.params),
+                                         self.seed, self.step), self.ctx, "SimulateEphys")
+        self.step += 1
+
+
+@dataclass
+class AdjacencyList:
+    """Device CSR, row = presynaptic (src/coupling.cuh:4-8)."""
+    indices: DeviceArray
+    offset_in_indices: DeviceArray
+
+
+@dataclass
+class ChunkedAdjacencyList:
+    """Per-chunk device CSR with chunk-local targets (src/coupling.cuh:10-14)."""
+    indices_chunks: list
+    offset_in_indices_chunks: list
+    n_per_chunk: int
+    chunk_nnz: list
+
+
+class AtomicCoupling:
+    """AtomicCoupling (src/coupling.cuh:17-38)."""
+
+    def __init__(self, ctx: Context, n: int):
+        self.ctx, self.n = ctx, n
+        self.handle = C.c_void_p()
+        _check(lib().nn_coupling_create(ctx.handle, n, C.byref(self.handle)), ctx, "AtomicCoupling")
+
+    def __call__(self, connectivity, spikes: DeviceArray, neuron_outputs: DeviceArray,
+                 signal_mode: int = NN_SIGNAL_COUNT, read_count: bool = True) -> int | None:
+        nf = C.c_int(-1)
+        pnf = C.byref(nf) if read_count else None
+        if isinstance(connectivity, ChunkedAdjacencyList):
+            k = len(connectivity.indices_chunks)
+            ci = (C.c_void_p * k)(*[a.value for a in connectivity.indices_chunks])
+            co = (C.c_void_p * k)(*[a.value for a in connectivity.offset_in_indices_chunks])
+            st = lib().nn_coupling_run_chunked(self.handle, k, connectivity.n_per_chunk, ci, co, spikes.ptr,
+                                               neuron_outputs.ptr, pnf)
+        else:
+            st = lib().nn_coupling_run(self.handle, connectivity.indices.ptr, connectivity.offset_in_indices.ptr,
+                                       spikes.ptr, neuron_outputs.ptr, signal_mode, pnf)
+        _check(st, self.ctx, "AtomicCoupling()")
+        return nf.value if read_count else None
+
+    def get_firing_neurons(self) -> np.ndarray:
+        """GetFiringNeurons(): the full n-entry buffer (src/coupling.cuh:37)."""
+        out = np.empty(self.n, np.int32)
+        p = lib().nn_coupling_firing_list(self.handle)
+        _check(lib().nn_memcpy_d2h(self.ctx.handle, _ptr(out), C.c_void_p(p), out.nbytes), self.ctx)
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().nn_coupling_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Network:
+    """Host-side CSR (src/network_factory.cuh:6-53)."""
+
+    def __init__(self):
+        self.indices = np.zeros(0, np.int32)
+        self.offset_in_indices = np.zeros(1, np.int32)
+
+    @property
+    def n(self) -> int:
+        return len(self.offset_in_indices) - 1
+
+    def to_adjacency_list(self, ctx: Context, tcount: DeviceArray) -> AdjacencyList:
+        """ToAdjacencyList(Float*& Tcount) (src/network_factory.cu:5-27)."""
+        lst = AdjacencyList(ctx.to_device(self.indices), ctx.to_device(self.offset_in_indices))
+        _check(lib().nn_net_tcount(ctx.handle, lst.indices.ptr, len(self.indices), self.n, tcount.ptr), ctx,
+               "ToAdjacencyList")
+        return lst
+
+    def to_chunked_adjacency_list(self, ctx: Context, tcount: DeviceArray, nchunks: int = 2,
+                                  n_per_chunk: int = 7319) -> ChunkedAdjacencyList:
+        """ToChunkedAdjacencyList(Float*& Tcount) (src/network_factory.cu:29-85)."""
+        d_idx = ctx.to_device(self.indices)
+        d_off = ctx.to_device(self.offset_in_indices)
+        _check(lib().nn_net_tcount(ctx.handle, d_idx.ptr, len(self.indices), self.n, tcount.ptr), ctx, "Tcount")
+        nnz = max(len(self.indices), 1)
+        ci = [ctx.empty((nnz,), np.int32) for _ in range(nchunks)]
+        co = [ctx.empty((self.n + 1,), np.int32) for _ in range(nchunks)]
+        cnt = (C.c_int64 * nchunks)()
+        _check(lib().nn_net_to_chunked(ctx.handle, d_idx.ptr, d_off.ptr, self.n, nchunks, n_per_chunk,
+                                       (C.c_void_p * nchunks)(*[a.value for a in ci]),
+                                       (C.c_void_p * nchunks)(*[a.value for a in co]), cnt), ctx,
+               "ToChunkedAdjacencyList")
+        return ChunkedAdjacencyList(ci, co, n_per_chunk, list(cnt))
+
+
+class UniformRandomNetwork(Network):
+    """UniformRandomNetwork (src/network_factory.cuh:56-67); the engine is the
+    reference's shared default-constructed minstd_rand0 (state 1)."""
+
+    engine = C.c_uint32(1)
+
+    def __init__(self, ncouple: int):
+        super().__init__()
+        self.ncouple = ncouple
+
+    @classmethod
+    def reset_engine(cls, state: int = 1) -> None:
+        cls.engine = C.c_uint32(state)
+
+    def generate(self, n: int) -> bool:
+        self.indices = np.zeros(n * self.ncouple, np.int32)
+        self.offset_in_indices = np.zeros(n + 1, np.int32)
+        st = lib().nn_net_uniform_random(n, self.ncouple, C.byref(UniformRandomNetwork.engine),
+                                         _ptr(self.indices), _ptr(self.offset_in_indices))
+        return st == 0
+
+
+class ParacrineModule:
+    """ParacrineModule (src/paracrine.cuh:212-267)."""
+
+    def __init__(self, ctx: Context, d_g_paracrine: DeviceArray, n: int, params: ParacrineRefParams,
+                 x: DeviceArray, y: DeviceArray, z: DeviceArray):
+        self.ctx, self.n, self.params = ctx, n, params
+        self.handle = C.c_void_p()
+        _check(lib().nn_paracrine_ref_create(ctx.handle, C.byref(params), n, x.ptr, y.ptr, z.ptr,
+                                             d_g_paracrine.ptr, C.byref(self.handle)), ctx, "ParacrineModule")
+        self.G = params.nx * params.ny * params.nz
+
+    @staticmethod
+    def default_params() -> ParacrineRefParams:
+        p = ParacrineRefParams()
+        lib().nn_paracrine_ref_params_default(C.byref(p))
+        return p
+
+    def update_on_fine_timescale(self, coupling: AtomicCoupling) -> None:
+        _check(lib().nn_paracrine_ref_fine(self.handle, coupling.handle), self.ctx, "update_on_fine_timescale")
+
+    def update_on_own_timescale(self) -> tuple[int, float]:
+        it, rr = C.c_int(0), C.c_float(0)
+        _check(lib().nn_paracrine_ref_own(self.handle, C.byref(it), C.byref(rr)), self.ctx,
+               "update_on_own_timescale")
+        return it.value, rr.value
+
+    def _read(self, p: int, count: int) -> np.ndarray:
+        out = np.empty(count, np.float32)
+        _check(lib().nn_memcpy_d2h(self.ctx.handle, _ptr(out), C.c_void_p(p), out.nbytes), self.ctx)
+        return out
+
+    def density(self) -> np.ndarray:
+        return self._read(lib().nn_paracrine_density(self.handle), self.G)
+
+    def set_density(self, u: np.ndarray) -> None:
+        u = np.ascontiguousarray(u, np.float32).ravel()
+        _check(lib().nn_memcpy_h2d(self.ctx.handle, C.c_void_p(lib().nn_paracrine_density(self.handle)), _ptr(u),
+                                   u.nbytes), self.ctx)
+
+    def sources(self) -> np.ndarray:
+        return self._read(lib().nn_paracrine_sources(self.handle), self.n)
+
+    def set_sources(self, s: np.ndarray) -> None:
+        s = np.ascontiguousarray(s, np.float32)
+        _check(lib().nn_memcpy_h2d(self.ctx.handle, C.c_void_p(lib().nn_paracrine_sources(self.handle)), _ptr(s),
+                                   s.nbytes), self.ctx)
+
+    def close(self):
+        if self.handle:
+            lib().nn_paracrine_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------- GB300 sim --
+
+def default_config(n: int) -> SimConfig:
+    c = SimConfig()
+    lib().nn_sim_config_default(C.byref(c), n)
+    return c
+
+
+def default_net_spec(kind: int) -> NetSpec:
+    s = NetSpec()
+    lib().nn_net_spec_default(C.byref(s), kind)
+    return s
+
+
+class Simulation:
+    """Device-resident network simulation (RK4 HH + delayed delivery + field)."""
+
+    def __init__(self, ctx: Context, config: SimConfig):
+        self.ctx, self.config, self.n = ctx, config, config.n
+        self.handle = C.c_void_p()
+        _check(lib().nn_sim_create(ctx.handle, C.byref(config), C.byref(self.handle)), ctx, "nn_sim_create")
+
+    def close(self):
+        if self.handle:
+            lib().nn_sim_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_network(self, row_ptr, col, weight, delay, is_inh=None) -> None:
+        row_ptr = np.ascontiguousarray(row_ptr, np.int64)
+        col = np.ascontiguousarray(col, np.int32)
+        weight = np.ascontiguousarray(weight, np.float32)
+        delay = np.ascontiguousarray(delay, np.uint8)
+        inh = None if is_inh is None else np.ascontiguousarray(is_inh, np.uint8)
+        _check(lib().nn_sim_set_network(self.handle, _ptr(row_ptr), _ptr(col), _ptr(weight), _ptr(delay), len(col),
+                                        None if inh is None else _ptr(inh)), self.ctx, "set_network")
+
+    def generate_network(self, spec: NetSpec) -> int:
+        _check(lib().nn_sim_generate_network(self.handle, C.byref(spec)), self.ctx, "generate_network")
+        return self.nnz
+
+    @property
+    def nnz(self) -> int:
+        v = C.c_int64()
+        _check(lib().nn_sim_network_size(self.handle, C.byref(v)), self.ctx)
+        return v.value
+
+    def get_network(self):
+        nnz = self.nnz
+        rp = np.empty(self.n + 1, np.int64)
+        col = np.empty(nnz, np.int32)
+        w = np.empty(nnz, np.float32)
+        d = np.empty(nnz, np.uint8)
+        inh = np.empty(self.n, np.uint8)
+        _check(lib().nn_sim_get_network(self.handle, _ptr(rp), _ptr(col), _ptr(w), _ptr(d), _ptr(inh)), self.ctx)
+        return rp, col, w, d, inh
+
+    def get_csc(self):
+        nnz = self.nnz
+        cp = np.empty(self.n + 1, np.int64)
+        src = np.empty(nnz, np.int32)
+        w = np.empty(nnz, np.float32)
+        d = np.empty(nnz, np.uint8)
+        _check(lib().nn_sim_get_csc(self.handle, _ptr(cp), _ptr(src), _ptr(w), _ptr(d)), self.ctx, "get_csc")
+        return cp, src, w, d
+
+    def init_state(self, v0: float = -65.0, i_lo: float = 5.0, i_hi: float = 15.0) -> None:
+        _check(lib().nn_sim_init_state(self.handle, v0, i_lo, i_hi), self.ctx, "init_state")
+
+    def set_field(self, name: str, values) -> None:
+        v = np.ascontiguousarray(np.broadcast_to(np.asarray(values, np.float32), (self.n,)))
+        _check(lib().nn_sim_set_field(self.handle, FIELDS[name], _ptr(v)), self.ctx, "set_field")
+
+    def get_field(self, name: str) -> np.ndarray:
+        out = np.empty(self.n, np.float32)
+        _check(lib().nn_sim_get_field(self.handle, FIELDS[name], _ptr(out)), self.ctx, "get_field")
+        return out
+
+    def step(self, nsteps: int = 1) -> None:
+        _check(lib().nn_sim_step(self.handle, nsteps), self.ctx, "step")
+
+    def run_host(self, state_in: np.ndarray, nsteps: int, state_out: np.ndarray) -> int:
+        sp = C.c_int64()
+        _check(lib().nn_sim_run_host(self.handle, _ptr(state_in), nsteps, _ptr(state_out), C.byref(sp)), self.ctx,
+               "run_host")
+        return sp.value
+
+    def counters(self) -> tuple[int, int]:
+        s, t = C.c_int64(), C.c_int64()
+        _check(lib().nn_sim_counters(self.handle, C.byref(s), C.byref(t)), self.ctx, "counters")
+        return s.value, t.value
+
+    def raster(self, cap: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+        cap = int(self.config.raster_capacity if cap is None else cap)
+        st = np.empty(max(cap, 1), np.int32)
+        ne = np.empty(max(cap, 1), np.int32)
+        cnt = C.c_int64()
+        _check(lib().nn_sim_get_raster(self.handle, cap, _ptr(st), _ptr(ne), C.byref(cnt)), self.ctx, "raster")
+        m = min(cap, cnt.value)
+        return st[:m].copy(), ne[:m].copy()
+
+    def density(self) -> np.ndarray:
+        g = self.config.grid
+        out = np.empty(g * g * g, np.float32)
+        _check(lib().nn_sim_get_density(self.handle, _ptr(out)), self.ctx, "density")
+        return out
+
+    def set_density(self, u: np.ndarray) -> None:
+        u = np.ascontiguousarray(u, np.float32).ravel()
+        _check(lib().nn_sim_set_density(self.handle, _ptr(u)), self.ctx, "set_density")
+
+    def set_kernel_timing(self, on: bool = True) -> None:
+        _check(lib().nn_sim_set_kernel_timing(self.handle, int(on)), self.ctx, "set_kernel_timing")
+
+    def kernel_times(self) -> KernelTimes:
+        k = KernelTimes()
+        _check(lib().nn_sim_kernel_times(self.handle, C.byref(k)), self.ctx, "kernel_times")
+        return k
+
+    def solve_stats(self) -> SolveStats:
+        s = SolveStats()
+        _check(lib().nn_sim_solve_stats(self.handle, C.byref(s)), self.ctx)
+        return s
+
+
+class PCG:
+    """Standalone 7-point Jacobi-PCG (nn_pcg_*)."""
+
+    def __init__(self, ctx: Context, nx: int, ny: int, nz: int, alpha: float, beta: float,
+                 Dcell: DeviceArray | None = None):
+        self.ctx, self.shape = ctx, (nz, ny, nx)
+        self.handle = C.c_void_p()
+        _check(lib().nn_pcg_create(ctx.handle, nx, ny, nz, alpha, beta, None if Dcell is None else Dcell.ptr,
+                                   C.byref(self.handle)), ctx, "nn_pcg_create")
+        self._D = Dcell
+
+    def apply(self, x: DeviceArray, y: DeviceArray) -> None:
+        _check(lib().nn_pcg_apply(self.handle, x.ptr, y.ptr), self.ctx, "pcg_apply")
+
+    def solve(self, b: DeviceArray, x: DeviceArray, rtol: float = 1e-6, max_iter: int = 10000) -> tuple[int, float]:
+        it, rel = C.c_int(0), C.c_double(0)
+        _check(lib().nn_pcg_solve(self.handle, b.ptr, x.ptr, rtol, max_iter, C.byref(it), C.byref(rel)), self.ctx,
+               "pcg_solve")
+        return it.value, rel.value
+
+    def close(self):
+        if self.handle:
+            lib().nn_pcg_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

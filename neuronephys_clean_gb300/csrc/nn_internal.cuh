@@ -1,0 +1,150 @@
+// Internal declarations shared by the translation units of libneuronephys.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "neuronephys.h"
+
+// ----------------------------------------------------------------- context --
+struct nn_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    int64_t launches = 0;  // kernels launched on behalf of the caller
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // nn_ctx_time_begin/end
+};
+
+nn_status nn_fail(nn_ctx* ctx, nn_status st, const char* fmt, ...);
+nn_status nn_cuda_check(nn_ctx* ctx, cudaError_t e, const char* what);
+
+#define NN_CUDA(ctx, expr)                                                   \
+    do {                                                                     \
+        cudaError_t e_ = (expr);                                             \
+        if (e_ != cudaSuccess) return nn_cuda_check((ctx), e_, #expr);       \
+    } while (0)
+
+#define NN_CHECK_LAUNCH(ctx, what)                                           \
+    do {                                                                     \
+        cudaError_t e_ = cudaGetLastError();                                 \
+        if (e_ != cudaSuccess) return nn_cuda_check((ctx), e_, what);        \
+        (ctx)->launches++;                                                   \
+    } while (0)
+
+#define NN_TRY(expr)                                                         \
+    do {                                                                     \
+        nn_status s_ = (expr);                                               \
+        if (s_ != NN_OK) return s_;                                          \
+    } while (0)
+
+template <class T>
+nn_status nn_alloc(nn_ctx* ctx, T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) return NN_OK;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return nn_fail(ctx, e == cudaErrorMemoryAllocation ? NN_ERR_OOM : NN_ERR_CUDA,
+                       "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    }
+    return NN_OK;
+}
+
+template <class T>
+void nn_release(T*& p)
+{
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+inline int nn_grid_for(const nn_ctx* ctx, int64_t work, int threads, int per_sm = 8)
+{
+    int64_t b = (work + threads - 1) / threads;
+    int64_t cap = (int64_t)ctx->num_sms * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// ---------------------------------------------------------- counter RNG --
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11).  Streams are addressed by (seed; a, b, c, purpose).
+enum nn_rng_purpose : uint32_t {
+    NN_P_NOISE = 1, NN_P_DRIVE = 2, NN_P_POS = 3, NN_P_ER = 4, NN_P_GAUSS = 5,
+    NN_P_WEIGHT = 6, NN_P_TYPE = 7, NN_P_BLOCK = 8, NN_P_REGION = 9
+};
+
+struct nn_u4 { uint32_t x, y, z, w; };
+
+__host__ __device__ __forceinline__ void nn_mulhilo(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo)
+{
+#ifdef __CUDA_ARCH__
+    hi = __umulhi(a, b);
+    lo = a * b;
+#else
+    uint64_t p = (uint64_t)a * (uint64_t)b;
+    hi = (uint32_t)(p >> 32);
+    lo = (uint32_t)p;
+#endif
+}
+
+__host__ __device__ __forceinline__ nn_u4 nn_philox(uint64_t seed, uint32_t a, uint32_t b, uint32_t c, uint32_t purpose)
+{
+    uint32_t c0 = a, c1 = b, c2 = c, c3 = purpose;
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, lo0, hi1, lo1;
+        nn_mulhilo(0xD2511F53u, c0, hi0, lo0);
+        nn_mulhilo(0xCD9E8D57u, c2, hi1, lo1);
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return nn_u4{c0, c1, c2, c3};
+}
+
+// uniform in [0,1) and (0,1] with 24 random bits (exact in float)
+__host__ __device__ __forceinline__ float nn_u01f(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+__host__ __device__ __forceinline__ float nn_u01f_open(uint32_t x) { return (float)((x >> 8) + 1u) * (1.0f / 16777216.0f); }
+__host__ __device__ __forceinline__ double nn_u01d(uint32_t x) { return (double)(x >> 8) * (1.0 / 16777216.0); }
+__host__ __device__ __forceinline__ double nn_u01d_open(uint32_t x) { return (double)((x >> 8) + 1u) * (1.0 / 16777216.0); }
+
+// Lattice side of the jittered-lattice layout: smallest L with L^3 >= n.
+__host__ __device__ inline int nn_lattice_side(int n)
+{
+    int L = 1;
+    while ((int64_t)L * L * L < n) ++L;
+    return L;
+}
+
+// ------------------------------------------------------ shared host helpers --
+nn_status nn_scan_exclusive_i64(nn_ctx* ctx, const int64_t* d_in, int64_t* d_out, int64_t n);
+nn_status nn_build_csc(nn_ctx* ctx, int n, int64_t nnz, const int64_t* d_row_ptr, const int32_t* d_col,
+                       int64_t* d_col_ptr, uint32_t* d_edge_of);
+double nn_host_inv_phi(double p);
+void nn_host_gauss_table(double sigma_sites, int16_t* table4096);
+
+// Device warp helpers
+__device__ __forceinline__ double nn_warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float nn_warp_sumf(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}

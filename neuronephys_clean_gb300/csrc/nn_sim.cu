@@ -1,0 +1,1368 @@
+// GB300 simulation step: RK4 Hodgkin-Huxley over SoA state, spike compaction
+// fused into the neuron update, delayed weighted spike delivery (push scatter
+// with red.global or deterministic pull gather over the CSC transpose) into an
+// integer-delay ring buffer, and the paracrine field (spike deposit, 7-point
+// backward-Euler Jacobi-PCG every `timescale` steps, gather to neurons).
+//
+// The step loop this replaces is _RunAndPrintSimulation's body
+// (src/main.cu:166-181): coupling -> paracrine -> ephys, with a host
+// synchronisation after every launch and the firing count read back every step.
+// Here one step is two kernels with no host interaction:
+//   k_hh_step      : ring slot t%D -> (ge, gi), RK4 with noise, spike test,
+//                    warp-aggregated compaction, spike bitmap, voxel deposit
+//   k_deliver_*    : spikes of step t -> ring slots (t+d)%D (push) or the
+//                    whole input of step t+1 (pull); the last block to finish
+//                    advances the device step counter.
+// Periods of steps are captured once into a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "nn_hh.cuh"
+#include "nn_internal.cuh"
+
+struct nn_pcg;
+nn_status nn_pcg_run(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int* iters, double* relres,
+                     int* converged);
+
+struct nn_sim {
+    nn_ctx* ctx = nullptr;
+    nn_sim_config cfg{};
+    int n = 0, n_pad = 0, D = 0, words = 0;
+    int npt = 2, tpb = 256;
+    // neuron state (n_pad floats each)
+    float* f[NN_F_COUNT] = {};
+    float2* ring = nullptr;        // D * n_pad
+    uint32_t* bitmap = nullptr;    // D * words (pull delivery)
+    int* list = nullptr;           // 2 * n_pad
+    int* counts = nullptr;         // [0], [1]: spikes of the step with that parity
+    unsigned long long* step = nullptr;     // device step counter
+    unsigned long long* total = nullptr;    // spikes so far
+    unsigned long long* rcount = nullptr;   // raster entries written
+    int2* raster = nullptr;        // (step, neuron)
+    unsigned int* ticket = nullptr;
+    int* err = nullptr;
+    uint8_t* is_inh = nullptr;
+    // network
+    int64_t nnz = 0;
+    int64_t* row_ptr = nullptr;
+    int32_t* col = nullptr;
+    float* weight = nullptr;
+    uint8_t* delay = nullptr;
+    int64_t* col_ptr = nullptr;    // CSC
+    uint32_t* csc_src = nullptr;   // source | inhibitory << 31
+    float* csc_w = nullptr;
+    uint8_t* csc_d = nullptr;
+    // paracrine
+    int grid = 0;
+    int64_t G = 0;
+    int32_t* vox = nullptr;
+    float* src = nullptr;
+    float* u = nullptr;
+    float* b = nullptr;
+    nn_pcg* pcg = nullptr;
+    nn_solve_stats stats{};
+    // host mirrors
+    int64_t host_step = 0;
+    bool gna_set = false;  // per-neuron gNa scale given (else the kernel skips the load)
+    // graph of one period
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    // kernel timing: events before the neuron update, between it and the
+    // delivery, and after the delivery, one triple per step of a period
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_a, ev_b, ev_c;
+    std::vector<char> ev_valid;
+};
+
+void nn_pcg_set_timing(nn_pcg* pc, bool on);
+void nn_pcg_last_timing(const nn_pcg* pc, float* ms, int* iters);
+
+
+namespace {
+
+constexpr int DELIV_THREADS = 256;
+
+struct StepArgs {
+    float *V, *m, *h, *nn, *ge, *gi;
+    const float* idrive;
+    const float* gna_scale;
+    const float* upar;
+    float* ring;            // float2 interleaved
+    uint32_t* bitmap;
+    int* list;
+    int* counts;
+    const unsigned long long* step;
+    const int32_t* vox;
+    float* src;
+    int* err;
+    int n, n_pad, D, words;
+    int zero_ring;
+    uint64_t seed;
+    nn_hh_dev p;
+};
+
+template <int NPT> struct VecT;
+template <> struct VecT<1> { using type = float; };
+template <> struct VecT<2> { using type = float2; };
+template <> struct VecT<4> { using type = float4; };
+
+template <int NPT>
+__device__ __forceinline__ void vload(const float* base, int i0, float (&out)[NPT])
+{
+    using V = typename VecT<NPT>::type;
+    const V v = *reinterpret_cast<const V*>(base + i0);
+    const float* pv = reinterpret_cast<const float*>(&v);
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) out[q] = pv[q];
+}
+
+template <int NPT>
+__device__ __forceinline__ void vstore(float* base, int i0, const float (&in)[NPT])
+{
+    using V = typename VecT<NPT>::type;
+    V v;
+    float* pv = reinterpret_cast<float*>(&v);
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) pv[q] = in[q];
+    *reinterpret_cast<V*>(base + i0) = v;
+}
+
+// One simulation step of NPT consecutive neurons per lane.  Loop trip counts
+// are warp-uniform so the warp-collective compaction stays converged.
+template <int NPT>
+__global__ void __launch_bounds__(256) k_hh_step(StepArgs a)
+{
+    const uint64_t t = *a.step;
+    const int slot = (int)(t % (uint64_t)a.D);
+    float* ring_slot = a.ring + (size_t)slot * a.n_pad * 2;
+    int* list = a.list + (size_t)(t & 1) * a.n_pad;
+    int* cnt = a.counts + (t & 1);
+    uint32_t* bm = a.bitmap ? a.bitmap + (size_t)slot * a.words : nullptr;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int chunk = 32 * NPT;
+    const int nchunks = a.n_pad / chunk;
+    for (int ch = warp; ch < nchunks; ch += nwarps) {
+        const int i0 = ch * chunk + lane * NPT;
+        float V[NPT], M[NPT], H[NPT], N[NPT], GE[NPT], GI[NPT], ID[NPT];
+        vload<NPT>(a.V, i0, V);
+        vload<NPT>(a.m, i0, M);
+        vload<NPT>(a.h, i0, H);
+        vload<NPT>(a.nn, i0, N);
+        vload<NPT>(a.ge, i0, GE);
+        vload<NPT>(a.gi, i0, GI);
+        vload<NPT>(a.idrive, i0, ID);
+        float RG[2 * NPT];
+        if (NPT == 1) {
+            const float2 v = *reinterpret_cast<const float2*>(ring_slot + 2 * i0);
+            RG[0] = v.x; RG[1] = v.y;
+        } else {
+#pragma unroll
+            for (int q = 0; q < NPT / 2; ++q) {
+                const float4 v = *reinterpret_cast<const float4*>(ring_slot + 2 * i0 + 4 * q);
+                RG[4 * q] = v.x; RG[4 * q + 1] = v.y; RG[4 * q + 2] = v.z; RG[4 * q + 3] = v.w;
+            }
+        }
+        float GS[NPT], UP[NPT];
+        if (a.gna_scale) vload<NPT>(a.gna_scale, i0, GS);
+        else {
+#pragma unroll
+            for (int q = 0; q < NPT; ++q) GS[q] = 1.0f;
+        }
+        if (a.upar) vload<NPT>(a.upar, i0, UP);
+        else {
+#pragma unroll
+            for (int q = 0; q < NPT; ++q) UP[q] = 0.0f;
+        }
+        uint32_t mask = 0;
+        bool bad = false;
+        bool any_in = false;
+#pragma unroll
+        for (int q = 0; q < NPT; ++q) {
+            const int i = i0 + q;
+            nn_hh_state y{V[q], M[q], H[q], N[q], GE[q] + RG[2 * q], GI[q] + RG[2 * q + 1]};
+            any_in |= (RG[2 * q] != 0.0f) | (RG[2 * q + 1] != 0.0f);
+            const float iext = ID[q] + a.p.noise_sigma * nn_normal(a.seed, (uint32_t)i, t);
+            const float v_old = y.V;
+            nn_hh_rk4(a.p, a.p.gNa * GS[q], iext, a.p.g_par * UP[q], y);
+            const bool valid = i < a.n;
+            if (valid && v_old < a.p.v_thresh && y.V >= a.p.v_thresh) mask |= 1u << q;
+            if (valid && !isfinite(y.V)) bad = true;
+            V[q] = y.V; M[q] = y.m; H[q] = y.h; N[q] = y.n; GE[q] = y.ge; GI[q] = y.gi;
+        }
+        vstore<NPT>(a.V, i0, V);
+        vstore<NPT>(a.m, i0, M);
+        vstore<NPT>(a.h, i0, H);
+        vstore<NPT>(a.nn, i0, N);
+        vstore<NPT>(a.ge, i0, GE);
+        vstore<NPT>(a.gi, i0, GI);
+        if (a.zero_ring && any_in) {
+            if (NPT == 1) {
+                *reinterpret_cast<float2*>(ring_slot + 2 * i0) = make_float2(0.0f, 0.0f);
+            } else {
+#pragma unroll
+                for (int q = 0; q < NPT / 2; ++q)
+                    *reinterpret_cast<float4*>(ring_slot + 2 * i0 + 4 * q) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        }
+        if (bad) atomicOr(a.err, 1);
+        // spike bitmap word of 32 consecutive neurons (pull delivery)
+        if (bm) {
+            uint32_t bits = mask << ((lane * NPT) & 31);
+#pragma unroll
+            for (int o = 1; o < 32 / NPT; o <<= 1) bits |= __shfl_xor_sync(0xffffffffu, bits, o);
+            if ((lane % (32 / NPT)) == 0) bm[(ch * chunk + lane * NPT) >> 5] = bits;
+        }
+        // warp-aggregated compaction: one atomic per warp with spikes
+        const int c = __popc(mask);
+        if (__any_sync(0xffffffffu, c != 0)) {
+            int inc = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int tv = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += tv;
+            }
+            const int tot = __shfl_sync(0xffffffffu, inc, 31);
+            int base = 0;
+            if (lane == 31) base = atomicAdd(cnt, tot);
+            base = __shfl_sync(0xffffffffu, base, 31);
+            int pos = base + inc - c;
+#pragma unroll
+            for (int q = 0; q < NPT; ++q)
+                if (mask & (1u << q)) {
+                    list[pos++] = i0 + q;
+                    if (a.src) atomicAdd(a.src + a.vox[i0 + q], 1.0f);
+                }
+        }
+    }
+}
+
+struct DelivArgs {
+    const int64_t* row_ptr;
+    const int32_t* col;
+    const float* weight;
+    const uint8_t* delay;
+    const int64_t* col_ptr;
+    const uint32_t* csc_src;
+    const float* csc_w;
+    const uint8_t* csc_d;
+    const uint8_t* is_inh;
+    const uint32_t* bitmap;
+    float* ring;
+    int* list;
+    int* counts;
+    unsigned long long* step;
+    unsigned long long* total;
+    unsigned long long* rcount;
+    int2* raster;
+    long long rcap;
+    unsigned int* ticket;
+    int n, n_pad, D, words;
+};
+
+// Bookkeeping once every block of the delivery kernel has read the step
+// counter: advance it, clear the next step's spike count, accumulate totals.
+__device__ __forceinline__ void deliver_finish(const DelivArgs& a, uint64_t t, int cnt, unsigned long long rbase)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(a.ticket, 1u) == gridDim.x - 1) {
+            __threadfence();
+            *a.step = t + 1;
+            a.counts[(t + 1) & 1] = 0;
+            *a.total += (unsigned long long)cnt;
+            if (a.raster) {
+                unsigned long long r = rbase + (unsigned long long)cnt;
+                *a.rcount = r > (unsigned long long)a.rcap ? (unsigned long long)a.rcap : r;
+            }
+            *a.ticket = 0;
+        }
+    }
+}
+
+__device__ __forceinline__ void record_raster(const DelivArgs& a, uint64_t t, unsigned long long rbase, int f, int j)
+{
+    const unsigned long long r = rbase + (unsigned long long)f;
+    if (a.raster && r < (unsigned long long)a.rcap) a.raster[r] = make_int2((int)t, j);
+}
+
+// Push: a warp per spiking neuron, lanes over its out-edges; red.global.add
+// into ring slot (t + delay) % D, channel = the source's type.
+__global__ void __launch_bounds__(DELIV_THREADS) k_deliver_push(DelivArgs a)
+{
+    const uint64_t t = *a.step;
+    const int cnt = a.counts[t & 1];
+    const int* list = a.list + (size_t)(t & 1) * a.n_pad;
+    const int s0 = (int)(t % (uint64_t)a.D);
+    const unsigned long long rbase = a.raster ? *a.rcount : 0ull;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (DELIV_THREADS / 32);
+    for (int f = blockIdx.x * (DELIV_THREADS / 32) + (threadIdx.x >> 5); f < cnt; f += nwarps) {
+        const int j = list[f];
+        const int ch = a.is_inh[j] ? 1 : 0;
+        const int64_t beg = a.row_ptr[j], end = a.row_ptr[j + 1];
+        for (int64_t e = beg + lane; e < end; e += 32) {
+            const int k = a.col[e];
+            int sl = s0 + (int)a.delay[e];
+            if (sl >= a.D) sl -= a.D;
+            atomicAdd(a.ring + 2 * ((size_t)sl * a.n_pad + k) + ch, a.weight[e]);
+        }
+        if (lane == 0) record_raster(a, t, rbase, f, j);
+    }
+    deliver_finish(a, t, cnt, rbase);
+}
+
+// Pull: a warp per postsynaptic neuron sums its CSC column against the spike
+// bitmap of step t + 1 - delay and writes the complete input of step t + 1.
+// Deterministic: the column order and the warp reduction order are fixed.
+__global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(DelivArgs a)
+{
+    const uint64_t t = *a.step;
+    const int cnt = a.counts[t & 1];
+    const int* list = a.list + (size_t)(t & 1) * a.n_pad;
+    const int s1 = (int)((t + 1) % (uint64_t)a.D);
+    const unsigned long long rbase = a.raster ? *a.rcount : 0ull;
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (DELIV_THREADS / 32) + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * (DELIV_THREADS / 32);
+    float* out = a.ring + (size_t)s1 * a.n_pad * 2;
+    for (int k = gw; k < a.n; k += nwarps) {
+        const int64_t beg = a.col_ptr[k], end = a.col_ptr[k + 1];
+        float acc_e = 0.0f, acc_i = 0.0f;
+        for (int64_t e = beg + lane; e < end; e += 32) {
+            const int d = a.csc_d[e];
+            if ((uint64_t)d > t + 1) continue;
+            const uint64_t tau = t + 1 - (uint64_t)d;
+            const uint32_t s = a.csc_src[e];
+            const uint32_t sid = s & 0x7fffffffu;
+            const int hs = (int)(tau % (uint64_t)a.D);
+            const uint32_t word = a.bitmap[(size_t)hs * a.words + (sid >> 5)];
+            if ((word >> (sid & 31)) & 1u) {
+                if (s >> 31) acc_i += a.csc_w[e];
+                else acc_e += a.csc_w[e];
+            }
+        }
+        acc_e = nn_warp_sumf(acc_e);
+        acc_i = nn_warp_sumf(acc_i);
+        if (lane == 0) reinterpret_cast<float2*>(out)[k] = make_float2(acc_e, acc_i);
+    }
+    for (int f = gw; f < cnt; f += nwarps)
+        if (lane == 0) record_raster(a, t, rbase, f, list[f]);
+    deliver_finish(a, t, cnt, rbase);
+}
+
+// paracrine: b = u + src ; src = 0
+__global__ void k_par_rhs(const float* u, float* src, float* b, int64_t G)
+{
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < G; q += (int64_t)gridDim.x * blockDim.x) {
+        b[q] = u[q] + src[q];
+        src[q] = 0.0f;
+    }
+}
+
+__global__ void k_par_gather(const float* u, const int32_t* vox, float* upar, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) upar[i] = u[vox[i]];
+}
+
+// ------------------------------------------------------------ generators --
+
+__global__ void k_fill_f(float* p, int64_t n, float v)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// ER: edge i -> j (j != i) iff philox word < thr; counts per row.
+__global__ void k_er_count(int n, uint32_t thr, uint64_t seed, int64_t* cnt)
+{
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int nb = (n + 3) >> 2;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+        int c = 0;
+        for (int jb = lane; jb < nb; jb += 32) {
+            const nn_u4 r = nn_philox(seed, (uint32_t)i, (uint32_t)jb, 0u, NN_P_ER);
+            const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = 4 * jb + q;
+                c += (j < n && j != i && w[q] < thr) ? 1 : 0;
+            }
+        }
+        c = __reduce_add_sync(0xffffffffu, c);
+        if (lane == 0) cnt[i] = c;
+    }
+}
+
+__global__ void k_er_fill(int n, uint32_t thr, uint64_t seed, float wmax, const int64_t* row_ptr, int32_t* col,
+                          float* weight, uint8_t* delay)
+{
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int nb = (n + 3) >> 2;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+        int64_t pos = row_ptr[i];
+        int e_run = 0;
+        for (int jb0 = 0; jb0 < nb; jb0 += 32) {
+            const int jb = jb0 + lane;
+            uint32_t m = 0;
+            if (jb < nb) {
+                const nn_u4 r = nn_philox(seed, (uint32_t)i, (uint32_t)jb, 0u, NN_P_ER);
+                const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int j = 4 * jb + q;
+                    if (j < n && j != i && w[q] < thr) m |= 1u << q;
+                }
+            }
+            const int c = __popc(m);
+            int inc = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int tv = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += tv;
+            }
+            int e = e_run + inc - c;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (m & (1u << q)) {
+                    const nn_u4 rw = nn_philox(seed, (uint32_t)i, (uint32_t)e, 0u, NN_P_WEIGHT);
+                    col[pos + e] = 4 * jb + q;
+                    weight[pos + e] = __fmul_rn(wmax, nn_u01f(rw.x));
+                    delay[pos + e] = 1;
+                    ++e;
+                }
+            e_run += __shfl_sync(0xffffffffu, inc, 31);
+        }
+    }
+}
+
+__device__ __forceinline__ float lognormal_w(uint64_t seed, uint32_t i, uint32_t e, double mu, double sg, uint32_t* r2)
+{
+    const nn_u4 rw = nn_philox(seed, i, e, 0u, NN_P_WEIGHT);
+    const double u1 = nn_u01d_open(rw.x), u2 = nn_u01d(rw.y);
+    const double z = sqrt(-2.0 * log(u1)) * cos(6.283185307179586476925 * u2);
+    *r2 = rw.z;
+    return (float)exp(mu + sg * z);
+}
+
+// Gaussian distance-dependent: fixed out-degree k, lattice offsets drawn from
+// the discretised Gaussian table, redrawn while outside the lattice, empty or
+// the source itself (64 attempts, then the next neuron).
+__global__ void k_gauss_fill(int n, int k, int L, const int16_t* table, uint64_t seed, double mu, double sg, int dmax,
+                             int32_t* col, float* weight, uint8_t* delay)
+{
+    const int64_t total = (int64_t)n * k;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q / k), e = (int)(q % k);
+        const int cx = i % L, cy = (i / L) % L, cz = i / (L * L);
+        int tgt = (i + 1) % n;
+        for (int at = 0; at < 64; ++at) {
+            const nn_u4 r = nn_philox(seed, (uint32_t)i, (uint32_t)e, (uint32_t)at, NN_P_GAUSS);
+            const int tx = cx + table[r.x >> 20], ty = cy + table[r.y >> 20], tz = cz + table[r.z >> 20];
+            if (tx < 0 || ty < 0 || tz < 0 || tx >= L || ty >= L || tz >= L) continue;
+            const int64_t s = (int64_t)tx + (int64_t)L * ((int64_t)ty + (int64_t)L * tz);
+            if (s >= n || s == i) continue;
+            tgt = (int)s;
+            break;
+        }
+        uint32_t r2;
+        weight[q] = lognormal_w(seed, (uint32_t)i, (uint32_t)e, mu, sg, &r2);
+        col[q] = tgt;
+        delay[q] = (uint8_t)(1u + (uint32_t)(((uint64_t)r2 * (uint64_t)dmax) >> 32));
+    }
+}
+
+// Region-block model: source region r, target region drawn from the row's
+// cumulative 32-bit thresholds, target neuron uniform in the region, delay from
+// the region-pair table.
+__global__ void k_block_fill(int n, int k, int R, const int* region_of, const int* region_start,
+                             const int* region_size, const uint32_t* cum, const uint8_t* pair_delay, uint64_t seed,
+                             double mu, double sg, int32_t* col, float* weight, uint8_t* delay)
+{
+    const int64_t total = (int64_t)n * k;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q / k), e = (int)(q % k);
+        const int r = region_of[i];
+        int tgt = (i + 1) % n, s = r;
+        for (int at = 0; at < 64; ++at) {
+            const nn_u4 u = nn_philox(seed, (uint32_t)i, (uint32_t)e, (uint32_t)at, NN_P_BLOCK);
+            // first region whose cumulative threshold exceeds u.x
+            int lo = 0, hi = R - 1;
+            const uint32_t* row = cum + (size_t)r * R;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (row[mid] > u.x) hi = mid; else lo = mid + 1;
+            }
+            s = lo;
+            const int off = (int)(((uint64_t)u.y * (uint64_t)region_size[s]) >> 32);
+            const int cand = region_start[s] + off;
+            if (cand == i) continue;
+            tgt = cand;
+            break;
+        }
+        uint32_t r2;
+        weight[q] = lognormal_w(seed, (uint32_t)i, (uint32_t)e, mu, sg, &r2);
+        col[q] = tgt;
+        delay[q] = pair_delay[(size_t)r * R + s];
+    }
+}
+
+__global__ void k_inh(int n, int random, double frac, uint64_t seed, uint8_t* is_inh)
+{
+    const int n_inh = (int)llround(frac * n);
+    const double tf = floor(frac * 4294967296.0);
+    const uint32_t thr = tf >= 4294967295.0 ? 0xffffffffu : (uint32_t)tf;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (random) is_inh[i] = nn_philox(seed, (uint32_t)i, 0u, 0u, NN_P_TYPE).x < thr ? 1 : 0;
+        else is_inh[i] = i >= n - n_inh ? 1 : 0;
+    }
+}
+
+// Initial state: V = v0, gates at their steady state, synapses 0, drive
+// lo + (hi - lo) u, jittered-lattice positions and their voxels.
+__global__ void k_init_state(StepArgs a, float v0, float m0, float h0, float n0, float lo, float hi, float* x, float* y,
+                             float* z, float* gs, int L, int grid, int32_t* vox)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n_pad; i += gridDim.x * blockDim.x) {
+        a.V[i] = v0; a.m[i] = m0; a.h[i] = h0; a.nn[i] = n0; a.ge[i] = 0.0f; a.gi[i] = 0.0f;
+        gs[i] = 1.0f;
+        if (i >= a.n) {
+            const_cast<float*>(a.idrive)[i] = 0.0f;
+            x[i] = y[i] = z[i] = 0.0f;
+            continue;
+        }
+        const nn_u4 r = nn_philox(a.seed, (uint32_t)i, 0u, 0u, NN_P_DRIVE);
+        const_cast<float*>(a.idrive)[i] = __fadd_rn(lo, __fmul_rn(__fsub_rn(hi, lo), nn_u01f(r.x)));
+        const nn_u4 rp = nn_philox(a.seed, (uint32_t)i, 0u, 0u, NN_P_POS);
+        const int cx = i % L, cy = (i / L) % L, cz = i / (L * L);
+        x[i] = __fdiv_rn(__fadd_rn((float)cx, nn_u01f(rp.x)), (float)L);
+        y[i] = __fdiv_rn(__fadd_rn((float)cy, nn_u01f(rp.y)), (float)L);
+        z[i] = __fdiv_rn(__fadd_rn((float)cz, nn_u01f(rp.z)), (float)L);
+        if (vox) {
+            int ix = (int)__fmul_rn(x[i], (float)grid), iy = (int)__fmul_rn(y[i], (float)grid),
+                iz = (int)__fmul_rn(z[i], (float)grid);
+            ix = min(max(ix, 0), grid - 1); iy = min(max(iy, 0), grid - 1); iz = min(max(iz, 0), grid - 1);
+            vox[i] = ix + grid * (iy + grid * iz);
+        }
+    }
+}
+
+__global__ void k_vox(const float* x, const float* y, const float* z, int n, int grid, int32_t* vox)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int ix = (int)__fmul_rn(x[i], (float)grid), iy = (int)__fmul_rn(y[i], (float)grid),
+            iz = (int)__fmul_rn(z[i], (float)grid);
+        ix = min(max(ix, 0), grid - 1); iy = min(max(iy, 0), grid - 1); iz = min(max(iz, 0), grid - 1);
+        vox[i] = ix + grid * (iy + grid * iz);
+    }
+}
+
+// CSC payload gather after the edge ids are ordered
+__global__ void k_csc_gather(const uint32_t* edge_of, int64_t nnz, const int64_t* row_ptr, int n, const float* w,
+                             const uint8_t* d, const uint8_t* is_inh, uint32_t* src, float* cw, uint8_t* cd)
+{
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = edge_of[q];
+        int lo = 0, hi = n - 1;  // row containing e: last lo with row_ptr[lo] <= e
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (row_ptr[mid] <= e) lo = mid; else hi = mid - 1;
+        }
+        src[q] = (uint32_t)lo | (is_inh[lo] ? 0x80000000u : 0u);
+        cw[q] = w[e];
+        cd[q] = d[e];
+    }
+}
+
+}  // namespace
+
+// ================================================================== API ====
+
+extern "C" void nn_hh_params_standard(nn_hh_params* p)
+{
+    if (!p) return;
+    p->C = 1.0f; p->gNa = 120.0f; p->gK = 36.0f; p->gL = 0.3f;
+    p->ENa = 50.0f; p->EK = -77.0f; p->EL = -54.4f;
+    p->E_exc = 0.0f; p->E_inh = -80.0f; p->tau_exc = 5.0f; p->tau_inh = 5.0f;
+    p->v_thresh = -20.0f; p->noise_sigma = 1.0f; p->dt = 0.01f;
+    p->g_par = 0.0f; p->E_par = 0.0f;
+}
+
+extern "C" void nn_sim_config_default(nn_sim_config* c, int n)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof *c);
+    c->n = n;
+    c->max_delay = 1;
+    c->seed = 1;
+    nn_hh_params_standard(&c->hp);
+    c->delivery = NN_DELIVERY_PUSH;
+    c->grid = 0;
+    c->timescale = 100;
+    c->par_D = 1.0f;
+    c->par_decay = 0.0f;
+    c->par_rtol = 1e-6;
+    c->par_max_iter = 2000;
+}
+
+extern "C" void nn_net_spec_default(nn_net_spec* sp, int kind)
+{
+    if (!sp) return;
+    std::memset(sp, 0, sizeof *sp);
+    sp->kind = kind;
+    sp->p = 0.01;
+    sp->w_max = 0.5f;
+    sp->k = 100;
+    sp->sigma = 0.1;
+    sp->w_mu = -1.0;
+    sp->w_sigma = 1.0;
+    sp->dmax = kind == NN_NET_ER ? 1 : 20;
+    sp->inh_fraction = 0.2;
+    sp->inh_random = kind == NN_NET_ER ? 0 : 1;
+    sp->n_regions = 200;
+    sp->region_size_sigma = 1.0;
+    sp->density_sigma = 1.0;
+    sp->block_dmax = 40;
+}
+
+static StepArgs step_args(nn_sim* s)
+{
+    StepArgs a;
+    a.V = s->f[NN_F_V]; a.m = s->f[NN_F_M]; a.h = s->f[NN_F_H]; a.nn = s->f[NN_F_N];
+    a.ge = s->f[NN_F_GE]; a.gi = s->f[NN_F_GI];
+    a.idrive = s->f[NN_F_IDRIVE];
+    a.gna_scale = s->gna_set ? s->f[NN_F_GNA_SCALE] : nullptr;  // all ones unless set
+    a.upar = (s->cfg.hp.g_par != 0.0f && s->grid > 0) ? s->f[NN_F_UPAR] : nullptr;
+    a.ring = reinterpret_cast<float*>(s->ring);
+    a.bitmap = s->bitmap;
+    a.list = s->list;
+    a.counts = s->counts;
+    a.step = s->step;
+    a.vox = s->vox;
+    a.src = s->grid > 0 ? s->src : nullptr;
+    a.err = s->err;
+    a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
+    a.zero_ring = s->cfg.delivery == NN_DELIVERY_PUSH;
+    a.seed = s->cfg.seed;
+    a.p = nn_hh_to_dev(s->cfg.hp);
+    return a;
+}
+
+static DelivArgs deliv_args(nn_sim* s)
+{
+    DelivArgs a;
+    a.row_ptr = s->row_ptr; a.col = s->col; a.weight = s->weight; a.delay = s->delay;
+    a.col_ptr = s->col_ptr; a.csc_src = s->csc_src; a.csc_w = s->csc_w; a.csc_d = s->csc_d;
+    a.is_inh = s->is_inh;
+    a.bitmap = s->bitmap;
+    a.ring = reinterpret_cast<float*>(s->ring);
+    a.list = s->list;
+    a.counts = s->counts;
+    a.step = s->step;
+    a.total = s->total;
+    a.rcount = s->rcount;
+    a.raster = s->raster;
+    a.rcap = s->cfg.raster_capacity;
+    a.ticket = s->ticket;
+    a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
+    return a;
+}
+
+static void drop_graph(nn_sim* s)
+{
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+    s->graph_steps = 0;
+}
+
+extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim** out)
+{
+    if (!ctx || !cfg || !out) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: NULL argument");
+    if (cfg->n <= 0 || cfg->max_delay < 1 || cfg->max_delay > 254 ||
+        (cfg->delivery != NN_DELIVERY_PUSH && cfg->delivery != NN_DELIVERY_PULL) || cfg->grid < 0 ||
+        (cfg->grid > 0 && cfg->timescale < 1) || !(cfg->hp.dt > 0.0f) || cfg->raster_capacity < 0)
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: invalid configuration");
+    if (cfg->neurons_per_thread != 0 && cfg->neurons_per_thread != 1 && cfg->neurons_per_thread != 2 &&
+        cfg->neurons_per_thread != 4)
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: neurons_per_thread must be 1, 2 or 4");
+    nn_sim* s = new nn_sim();
+    s->ctx = ctx;
+    s->cfg = *cfg;
+    s->n = cfg->n;
+    s->n_pad = (cfg->n + 127) / 128 * 128;
+    s->D = cfg->max_delay + 1;
+    s->words = s->n_pad / 32;
+    s->npt = cfg->neurons_per_thread ? cfg->neurons_per_thread : 2;
+    s->tpb = cfg->threads_per_block ? cfg->threads_per_block : 256;
+    if (s->tpb % 32 || s->tpb > 256 || s->tpb < 32) {
+        delete s;
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: threads_per_block must be a multiple of 32 <= 256");
+    }
+    s->grid = cfg->grid;
+    s->G = (int64_t)cfg->grid * cfg->grid * cfg->grid;
+    const size_t NP = (size_t)s->n_pad;
+    nn_status st = NN_OK;
+    for (int q = 0; q < NN_F_COUNT && st == NN_OK; ++q) st = nn_alloc(ctx, &s->f[q], NP);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->ring, (size_t)s->D * NP);
+    if (st == NN_OK && cfg->delivery == NN_DELIVERY_PULL) st = nn_alloc(ctx, &s->bitmap, (size_t)s->D * s->words);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->list, 2 * NP);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->counts, 2);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->step, 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->total, 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->rcount, 1);
+    if (st == NN_OK && cfg->raster_capacity > 0) st = nn_alloc(ctx, &s->raster, (size_t)cfg->raster_capacity);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->ticket, 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->err, 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->is_inh, NP);
+    if (st == NN_OK && s->grid > 0) {
+        st = nn_alloc(ctx, &s->vox, NP);
+        if (st == NN_OK) st = nn_alloc(ctx, &s->src, (size_t)s->G);
+        if (st == NN_OK) st = nn_alloc(ctx, &s->u, (size_t)s->G);
+        if (st == NN_OK) st = nn_alloc(ctx, &s->b, (size_t)s->G);
+        if (st == NN_OK) {
+            const double dt_s = (double)cfg->timescale * cfg->hp.dt * 1e-3;
+            const double alpha = dt_s * cfg->par_D * (double)cfg->grid * cfg->grid;
+            const double beta = dt_s * cfg->par_decay;
+            st = nn_pcg_create(ctx, cfg->grid, cfg->grid, cfg->grid, alpha, beta, nullptr, &s->pcg);
+        }
+    }
+    if (st != NN_OK) {
+        nn_sim_destroy(s);
+        return st;
+    }
+    cudaStream_t cs = ctx->stream;
+    for (int q = 0; q < NN_F_COUNT; ++q) cudaMemsetAsync(s->f[q], 0, NP * sizeof(float), cs);
+    k_fill_f<<<nn_grid_for(ctx, (int64_t)NP, 256), 256, 0, cs>>>(s->f[NN_F_GNA_SCALE], (int64_t)NP, 1.0f);
+    ctx->launches++;
+    cudaMemsetAsync(s->ring, 0, (size_t)s->D * NP * sizeof(float2), cs);
+    if (s->bitmap) cudaMemsetAsync(s->bitmap, 0, (size_t)s->D * s->words * sizeof(uint32_t), cs);
+    cudaMemsetAsync(s->list, 0, 2 * NP * sizeof(int), cs);
+    cudaMemsetAsync(s->counts, 0, 2 * sizeof(int), cs);
+    cudaMemsetAsync(s->step, 0, sizeof(unsigned long long), cs);
+    cudaMemsetAsync(s->total, 0, sizeof(unsigned long long), cs);
+    cudaMemsetAsync(s->rcount, 0, sizeof(unsigned long long), cs);
+    cudaMemsetAsync(s->ticket, 0, sizeof(unsigned int), cs);
+    cudaMemsetAsync(s->err, 0, sizeof(int), cs);
+    cudaMemsetAsync(s->is_inh, 0, NP, cs);
+    if (s->grid > 0) {
+        cudaMemsetAsync(s->vox, 0, NP * sizeof(int32_t), cs);
+        cudaMemsetAsync(s->src, 0, (size_t)s->G * sizeof(float), cs);
+        cudaMemsetAsync(s->u, 0, (size_t)s->G * sizeof(float), cs);
+    }
+    st = nn_cuda_check(ctx, cudaStreamSynchronize(cs), "nn_sim_create");
+    if (st != NN_OK) {
+        nn_sim_destroy(s);
+        return st;
+    }
+    *out = s;
+    return NN_OK;
+}
+
+static void free_network(nn_sim* s)
+{
+    nn_release(s->row_ptr); nn_release(s->col); nn_release(s->weight); nn_release(s->delay);
+    nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
+    s->nnz = 0;
+}
+
+extern "C" nn_status nn_sim_destroy(nn_sim* s)
+{
+    if (!s) return NN_OK;
+    if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
+    drop_graph(s);
+    for (int q = 0; q < NN_F_COUNT; ++q) nn_release(s->f[q]);
+    nn_release(s->ring); nn_release(s->bitmap); nn_release(s->list); nn_release(s->counts); nn_release(s->step);
+    nn_release(s->total); nn_release(s->rcount); nn_release(s->raster); nn_release(s->ticket); nn_release(s->err);
+    nn_release(s->is_inh); nn_release(s->vox); nn_release(s->src); nn_release(s->u); nn_release(s->b);
+    free_network(s);
+    if (s->pcg) nn_pcg_destroy(s->pcg);
+    for (auto e : s->ev_a) cudaEventDestroy(e);
+    for (auto e : s->ev_b) cudaEventDestroy(e);
+    for (auto e : s->ev_c) cudaEventDestroy(e);
+    delete s;
+    return NN_OK;
+}
+
+static nn_status build_csc(nn_sim* s)
+{
+    nn_ctx* ctx = s->ctx;
+    if (s->col_ptr) return NN_OK;
+    NN_TRY(nn_alloc(ctx, &s->col_ptr, (size_t)s->n + 1));
+    uint32_t* edge_of = nullptr;
+    NN_TRY(nn_alloc(ctx, &edge_of, (size_t)std::max<int64_t>(s->nnz, 1)));
+    NN_TRY(nn_build_csc(ctx, s->n, s->nnz, s->row_ptr, s->col, s->col_ptr, edge_of));
+    const size_t E = (size_t)std::max<int64_t>(s->nnz, 1);
+    NN_TRY(nn_alloc(ctx, &s->csc_src, E));
+    NN_TRY(nn_alloc(ctx, &s->csc_w, E));
+    NN_TRY(nn_alloc(ctx, &s->csc_d, E));
+    if (s->nnz > 0) {
+        k_csc_gather<<<nn_grid_for(ctx, s->nnz, 256, 16), 256, 0, ctx->stream>>>(
+            edge_of, s->nnz, s->row_ptr, s->n, s->weight, s->delay, s->is_inh, s->csc_src, s->csc_w, s->csc_d);
+        NN_CHECK_LAUNCH(ctx, "k_csc_gather");
+    }
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(edge_of);
+    return NN_OK;
+}
+
+static nn_status after_network(nn_sim* s)
+{
+    drop_graph(s);
+    nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
+    if (s->cfg.delivery == NN_DELIVERY_PULL) NN_TRY(build_csc(s));
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_set_network(nn_sim* s, const int64_t* h_row_ptr, const int32_t* h_col,
+                                        const float* h_weight, const uint8_t* h_delay, int64_t nnz,
+                                        const uint8_t* h_is_inh)
+{
+    if (!s || !h_row_ptr || nnz < 0 || (nnz && (!h_col || !h_weight || !h_delay)))
+        return nn_fail(s ? s->ctx : nullptr, NN_ERR_INVALID_ARG, "nn_sim_set_network: bad argument");
+    nn_ctx* ctx = s->ctx;
+    const int n = s->n;
+    if (h_row_ptr[0] != 0 || h_row_ptr[n] != nnz) return nn_fail(ctx, NN_ERR_INVALID_ARG, "row_ptr must span [0, nnz]");
+    for (int i = 0; i < n; ++i)
+        if (h_row_ptr[i + 1] < h_row_ptr[i]) return nn_fail(ctx, NN_ERR_INVALID_ARG, "row_ptr is not monotone at %d", i);
+    for (int64_t e = 0; e < nnz; ++e) {
+        if (h_col[e] < 0 || h_col[e] >= n) return nn_fail(ctx, NN_ERR_INVALID_ARG, "col[%lld] = %d out of range", (long long)e, h_col[e]);
+        if (h_delay[e] < 1 || h_delay[e] > s->cfg.max_delay)
+            return nn_fail(ctx, NN_ERR_INVALID_ARG, "delay[%lld] = %d outside [1, %d]", (long long)e, h_delay[e], s->cfg.max_delay);
+        if (!std::isfinite(h_weight[e])) return nn_fail(ctx, NN_ERR_INVALID_ARG, "weight[%lld] is not finite", (long long)e);
+    }
+    free_network(s);
+    s->nnz = nnz;
+    const size_t E = (size_t)std::max<int64_t>(nnz, 1);
+    NN_TRY(nn_alloc(ctx, &s->row_ptr, (size_t)n + 1));
+    NN_TRY(nn_alloc(ctx, &s->col, E));
+    NN_TRY(nn_alloc(ctx, &s->weight, E));
+    NN_TRY(nn_alloc(ctx, &s->delay, E));
+    cudaStream_t cs = ctx->stream;
+    NN_CUDA(ctx, cudaMemcpyAsync(s->row_ptr, h_row_ptr, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, cs));
+    if (nnz) {
+        NN_CUDA(ctx, cudaMemcpyAsync(s->col, h_col, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, cs));
+        NN_CUDA(ctx, cudaMemcpyAsync(s->weight, h_weight, sizeof(float) * (size_t)nnz, cudaMemcpyHostToDevice, cs));
+        NN_CUDA(ctx, cudaMemcpyAsync(s->delay, h_delay, (size_t)nnz, cudaMemcpyHostToDevice, cs));
+    }
+    NN_CUDA(ctx, cudaMemsetAsync(s->is_inh, 0, (size_t)s->n_pad, cs));
+    if (h_is_inh) NN_CUDA(ctx, cudaMemcpyAsync(s->is_inh, h_is_inh, (size_t)n, cudaMemcpyHostToDevice, cs));
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    return after_network(s);
+}
+
+// Host-side tables of the region-block model (shared by the oracle's
+// restatement): lognormal region sizes (largest-remainder rounding), uniform
+// centroids, lognormal block densities turned into per-row cumulative 32-bit
+// thresholds weighted by target size, delays 1..dmax by centroid distance.
+static void block_tables(int n, const nn_net_spec* sp, uint64_t seed, std::vector<int>& start, std::vector<int>& size,
+                         std::vector<uint32_t>& cum, std::vector<uint8_t>& pdelay)
+{
+    const int R = sp->n_regions;
+    std::vector<double> w(R), cx(R), cy(R), cz(R);
+    double sw = 0.0;
+    for (int r = 0; r < R; ++r) {
+        const nn_u4 u = nn_philox(seed, (uint32_t)r, 0u, 0u, NN_P_REGION);
+        const double u1 = nn_u01d_open(u.x), u2 = nn_u01d(u.y);
+        const double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586476925 * u2);
+        w[r] = std::exp(sp->region_size_sigma * z);
+        sw += w[r];
+        cx[r] = nn_u01d(u.z);
+        const nn_u4 v = nn_philox(seed, (uint32_t)r, 1u, 0u, NN_P_REGION);
+        cy[r] = nn_u01d(v.x);
+        cz[r] = nn_u01d(v.y);
+    }
+    // every region gets at least one neuron, the rest by largest remainder
+    size.assign(R, 1);
+    int left = n - R;
+    std::vector<double> fr(R);
+    std::vector<int> order(R);
+    int assigned = 0;
+    for (int r = 0; r < R; ++r) {
+        const double want = left * w[r] / sw;
+        const int fl = (int)std::floor(want);
+        size[r] += fl;
+        assigned += fl;
+        fr[r] = want - fl;
+        order[r] = r;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return fr[a] > fr[b]; });
+    for (int q = 0; q < left - assigned; ++q) size[order[q]] += 1;
+    start.assign(R, 0);
+    for (int r = 1; r < R; ++r) start[r] = start[r - 1] + size[r - 1];
+    // block densities
+    cum.assign((size_t)R * R, 0);
+    pdelay.assign((size_t)R * R, 1);
+    double dmax_dist = 0.0;
+    for (int r = 0; r < R; ++r)
+        for (int t = 0; t < R; ++t)
+            dmax_dist = std::max(dmax_dist, std::sqrt((cx[r] - cx[t]) * (cx[r] - cx[t]) + (cy[r] - cy[t]) * (cy[r] - cy[t]) +
+                                                      (cz[r] - cz[t]) * (cz[r] - cz[t])));
+    std::vector<double> row(R);
+    for (int r = 0; r < R; ++r) {
+        double s = 0.0;
+        for (int t = 0; t < R; ++t) {
+            const nn_u4 u = nn_philox(seed, (uint32_t)r, (uint32_t)t, 0u, NN_P_BLOCK + 16u);
+            const double u1 = nn_u01d_open(u.x), u2 = nn_u01d(u.y);
+            const double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586476925 * u2);
+            row[t] = std::exp(sp->density_sigma * z) * (double)size[t];
+            s += row[t];
+            const double dist = std::sqrt((cx[r] - cx[t]) * (cx[r] - cx[t]) + (cy[r] - cy[t]) * (cy[r] - cy[t]) +
+                                          (cz[r] - cz[t]) * (cz[r] - cz[t]));
+            const double dd = dmax_dist > 0 ? 1.0 + (sp->block_dmax - 1) * dist / dmax_dist : 1.0;
+            pdelay[(size_t)r * R + t] = (uint8_t)std::min<long>(sp->block_dmax, std::max<long>(1, std::lround(dd)));
+        }
+        double acc = 0.0;
+        for (int t = 0; t < R; ++t) {
+            acc += row[t];
+            const double th = std::floor(acc / s * 4294967296.0);
+            cum[(size_t)r * R + t] = t == R - 1 ? 0xffffffffu : (uint32_t)std::min(th, 4294967295.0);
+        }
+    }
+}
+
+extern "C" nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* sp)
+{
+    if (!s || !sp) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    const int n = s->n;
+    const uint64_t seed = s->cfg.seed;
+    free_network(s);
+    NN_TRY(nn_alloc(ctx, &s->row_ptr, (size_t)n + 1));
+    if (sp->kind == NN_NET_ER) {
+        if (!(sp->p >= 0.0 && sp->p <= 1.0)) return nn_fail(ctx, NN_ERR_INVALID_ARG, "ER p outside [0,1]");
+        const double tf = std::floor(sp->p * 4294967296.0);
+        const uint32_t thr = tf >= 4294967295.0 ? 0xffffffffu : (uint32_t)tf;
+        int64_t* cnt = nullptr;
+        NN_TRY(nn_alloc(ctx, &cnt, (size_t)n + 1));
+        NN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * ((size_t)n + 1), cs));
+        k_er_count<<<nn_grid_for(ctx, (int64_t)n * 32, 256, 16), 256, 0, cs>>>(n, thr, seed, cnt);
+        NN_CHECK_LAUNCH(ctx, "k_er_count");
+        NN_TRY(nn_scan_exclusive_i64(ctx, cnt, s->row_ptr, (int64_t)n + 1));
+        cudaFree(cnt);
+        NN_CUDA(ctx, cudaMemcpyAsync(&s->nnz, s->row_ptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, cs));
+        NN_CUDA(ctx, cudaStreamSynchronize(cs));
+        const size_t E = (size_t)std::max<int64_t>(s->nnz, 1);
+        NN_TRY(nn_alloc(ctx, &s->col, E));
+        NN_TRY(nn_alloc(ctx, &s->weight, E));
+        NN_TRY(nn_alloc(ctx, &s->delay, E));
+        k_er_fill<<<nn_grid_for(ctx, (int64_t)n * 32, 256, 16), 256, 0, cs>>>(n, thr, seed, sp->w_max, s->row_ptr, s->col,
+                                                                               s->weight, s->delay);
+        NN_CHECK_LAUNCH(ctx, "k_er_fill");
+    } else if (sp->kind == NN_NET_GAUSS || sp->kind == NN_NET_BLOCK) {
+        if (sp->k < 0 || (int64_t)n * sp->k >= ((int64_t)1 << 32))
+            return nn_fail(ctx, NN_ERR_INVALID_ARG, "out-degree k out of range");
+        s->nnz = (int64_t)n * sp->k;
+        std::vector<int64_t> rp((size_t)n + 1);
+        for (int i = 0; i <= n; ++i) rp[(size_t)i] = (int64_t)i * sp->k;
+        NN_CUDA(ctx, cudaMemcpyAsync(s->row_ptr, rp.data(), sizeof(int64_t) * rp.size(), cudaMemcpyHostToDevice, cs));
+        const size_t E = (size_t)std::max<int64_t>(s->nnz, 1);
+        NN_TRY(nn_alloc(ctx, &s->col, E));
+        NN_TRY(nn_alloc(ctx, &s->weight, E));
+        NN_TRY(nn_alloc(ctx, &s->delay, E));
+        if (sp->kind == NN_NET_GAUSS) {
+            if (sp->dmax < 1 || sp->dmax > s->cfg.max_delay)
+                return nn_fail(ctx, NN_ERR_INVALID_ARG, "dmax %d outside [1, max_delay=%d]", sp->dmax, s->cfg.max_delay);
+            const int L = nn_lattice_side(n);
+            int16_t table[4096];
+            nn_host_gauss_table(sp->sigma * (double)L, table);
+            int16_t* d_table = nullptr;
+            NN_TRY(nn_alloc(ctx, &d_table, 4096));
+            NN_CUDA(ctx, cudaMemcpyAsync(d_table, table, sizeof table, cudaMemcpyHostToDevice, cs));
+            if (s->nnz)
+                k_gauss_fill<<<nn_grid_for(ctx, s->nnz, 256, 16), 256, 0, cs>>>(n, sp->k, L, d_table, seed, sp->w_mu,
+                                                                                 sp->w_sigma, sp->dmax, s->col,
+                                                                                 s->weight, s->delay);
+            NN_CHECK_LAUNCH(ctx, "k_gauss_fill");
+            NN_CUDA(ctx, cudaStreamSynchronize(cs));
+            cudaFree(d_table);
+        } else {
+            const int R = sp->n_regions;
+            if (R < 1 || R > n || sp->block_dmax < 1 || sp->block_dmax > s->cfg.max_delay)
+                return nn_fail(ctx, NN_ERR_INVALID_ARG, "block model: bad region count or delay range");
+            std::vector<int> start, size;
+            std::vector<uint32_t> cum;
+            std::vector<uint8_t> pdel;
+            block_tables(n, sp, seed, start, size, cum, pdel);
+            std::vector<int> region_of((size_t)n);
+            for (int r = 0; r < R; ++r)
+                for (int q = 0; q < size[(size_t)r]; ++q) region_of[(size_t)(start[(size_t)r] + q)] = r;
+            int *d_rof = nullptr, *d_start = nullptr, *d_size = nullptr;
+            uint32_t* d_cum = nullptr;
+            uint8_t* d_pd = nullptr;
+            NN_TRY(nn_alloc(ctx, &d_rof, (size_t)n));
+            NN_TRY(nn_alloc(ctx, &d_start, (size_t)R));
+            NN_TRY(nn_alloc(ctx, &d_size, (size_t)R));
+            NN_TRY(nn_alloc(ctx, &d_cum, (size_t)R * R));
+            NN_TRY(nn_alloc(ctx, &d_pd, (size_t)R * R));
+            NN_CUDA(ctx, cudaMemcpyAsync(d_rof, region_of.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, cs));
+            NN_CUDA(ctx, cudaMemcpyAsync(d_start, start.data(), sizeof(int) * (size_t)R, cudaMemcpyHostToDevice, cs));
+            NN_CUDA(ctx, cudaMemcpyAsync(d_size, size.data(), sizeof(int) * (size_t)R, cudaMemcpyHostToDevice, cs));
+            NN_CUDA(ctx, cudaMemcpyAsync(d_cum, cum.data(), sizeof(uint32_t) * cum.size(), cudaMemcpyHostToDevice, cs));
+            NN_CUDA(ctx, cudaMemcpyAsync(d_pd, pdel.data(), pdel.size(), cudaMemcpyHostToDevice, cs));
+            if (s->nnz)
+                k_block_fill<<<nn_grid_for(ctx, s->nnz, 256, 16), 256, 0, cs>>>(n, sp->k, R, d_rof, d_start, d_size,
+                                                                                 d_cum, d_pd, seed, sp->w_mu,
+                                                                                 sp->w_sigma, s->col, s->weight,
+                                                                                 s->delay);
+            NN_CHECK_LAUNCH(ctx, "k_block_fill");
+            NN_CUDA(ctx, cudaStreamSynchronize(cs));
+            cudaFree(d_rof); cudaFree(d_start); cudaFree(d_size); cudaFree(d_cum); cudaFree(d_pd);
+        }
+    } else {
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "unknown network kind %d", sp->kind);
+    }
+    NN_CUDA(ctx, cudaMemsetAsync(s->is_inh, 0, (size_t)s->n_pad, cs));
+    k_inh<<<nn_grid_for(ctx, n, 256, 16), 256, 0, cs>>>(n, sp->inh_random, sp->inh_fraction, seed, s->is_inh);
+    NN_CHECK_LAUNCH(ctx, "k_inh");
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    return after_network(s);
+}
+
+extern "C" nn_status nn_sim_network_size(nn_sim* s, int64_t* nnz)
+{
+    if (!s || !nnz) return NN_ERR_INVALID_ARG;
+    *nnz = s->nnz;
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_get_network(nn_sim* s, int64_t* h_row_ptr, int32_t* h_col, float* h_weight,
+                                        uint8_t* h_delay, uint8_t* h_is_inh)
+{
+    if (!s) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    if (!s->row_ptr) return nn_fail(ctx, NN_ERR_INVALID_ARG, "no network set");
+    if (h_row_ptr) NN_CUDA(ctx, cudaMemcpyAsync(h_row_ptr, s->row_ptr, sizeof(int64_t) * ((size_t)s->n + 1), cudaMemcpyDeviceToHost, cs));
+    if (s->nnz) {
+        if (h_col) NN_CUDA(ctx, cudaMemcpyAsync(h_col, s->col, sizeof(int32_t) * (size_t)s->nnz, cudaMemcpyDeviceToHost, cs));
+        if (h_weight) NN_CUDA(ctx, cudaMemcpyAsync(h_weight, s->weight, sizeof(float) * (size_t)s->nnz, cudaMemcpyDeviceToHost, cs));
+        if (h_delay) NN_CUDA(ctx, cudaMemcpyAsync(h_delay, s->delay, (size_t)s->nnz, cudaMemcpyDeviceToHost, cs));
+    }
+    if (h_is_inh) NN_CUDA(ctx, cudaMemcpyAsync(h_is_inh, s->is_inh, (size_t)s->n, cudaMemcpyDeviceToHost, cs));
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_get_csc(nn_sim* s, int64_t* h_col_ptr, int32_t* h_src, float* h_weight, uint8_t* h_delay)
+{
+    if (!s) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    if (!s->row_ptr) return nn_fail(ctx, NN_ERR_INVALID_ARG, "no network set");
+    NN_TRY(build_csc(s));
+    cudaStream_t cs = ctx->stream;
+    if (h_col_ptr) NN_CUDA(ctx, cudaMemcpyAsync(h_col_ptr, s->col_ptr, sizeof(int64_t) * ((size_t)s->n + 1), cudaMemcpyDeviceToHost, cs));
+    if (s->nnz) {
+        if (h_src) NN_CUDA(ctx, cudaMemcpyAsync(h_src, s->csc_src, sizeof(uint32_t) * (size_t)s->nnz, cudaMemcpyDeviceToHost, cs));
+        if (h_weight) NN_CUDA(ctx, cudaMemcpyAsync(h_weight, s->csc_w, sizeof(float) * (size_t)s->nnz, cudaMemcpyDeviceToHost, cs));
+        if (h_delay) NN_CUDA(ctx, cudaMemcpyAsync(h_delay, s->csc_d, (size_t)s->nnz, cudaMemcpyDeviceToHost, cs));
+    }
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    if (h_src)
+        for (int64_t e = 0; e < s->nnz; ++e) h_src[e] &= 0x7fffffff;
+    return NN_OK;
+}
+
+extern "C" float* nn_sim_field_ptr(nn_sim* s, int field)
+{
+    if (!s || field < 0 || field >= NN_F_COUNT) return nullptr;
+    return s->f[field];
+}
+
+extern "C" nn_status nn_sim_set_field(nn_sim* s, int field, const float* h)
+{
+    if (!s || !h || field < 0 || field >= NN_F_COUNT) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    NN_CUDA(ctx, cudaMemcpyAsync(s->f[field], h, sizeof(float) * (size_t)s->n, cudaMemcpyHostToDevice, ctx->stream));
+    if (field == NN_F_GNA_SCALE && !s->gna_set) {
+        s->gna_set = true;
+        drop_graph(s);  // the captured kernels' arguments change
+    }
+    if ((field == NN_F_X || field == NN_F_Y || field == NN_F_Z) && s->grid > 0) {
+        k_vox<<<nn_grid_for(ctx, s->n, 256, 16), 256, 0, ctx->stream>>>(s->f[NN_F_X], s->f[NN_F_Y], s->f[NN_F_Z], s->n,
+                                                                         s->grid, s->vox);
+        NN_CHECK_LAUNCH(ctx, "k_vox");
+    }
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return NN_OK;
+}
+
+static nn_status check_err(nn_sim* s)
+{
+    int e = 0;
+    NN_CUDA(s->ctx, cudaMemcpyAsync(&e, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->ctx->stream));
+    NN_CUDA(s->ctx, cudaStreamSynchronize(s->ctx->stream));
+    if (e) return nn_fail(s->ctx, NN_ERR_NUMERIC, "non-finite membrane potential detected");
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_get_field(nn_sim* s, int field, float* h)
+{
+    if (!s || !h || field < 0 || field >= NN_F_COUNT) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    NN_CUDA(ctx, cudaMemcpyAsync(h, s->f[field], sizeof(float) * (size_t)s->n, cudaMemcpyDeviceToHost, ctx->stream));
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_err(s);
+}
+
+extern "C" nn_status nn_sim_init_state(nn_sim* s, float v0, float i_lo, float i_hi)
+{
+    if (!s) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    // steady-state gates at v0 (double precision on the host)
+    auto xr = [](double u) { return std::fabs(u) < 1e-4 ? 1.0 + 0.5 * u + u * u / 12.0 : u / (-std::expm1(-u)); };
+    const double V = v0;
+    const double am = xr((V + 40.0) / 10.0), bm = 4.0 * std::exp(-(V + 65.0) / 18.0);
+    const double ah = 0.07 * std::exp(-(V + 65.0) / 20.0), bh = 1.0 / (1.0 + std::exp(-(V + 35.0) / 10.0));
+    const double an = 0.1 * xr((V + 55.0) / 10.0), bn = 0.125 * std::exp(-(V + 65.0) / 80.0);
+    StepArgs a = step_args(s);
+    const int L = nn_lattice_side(s->n);
+    k_init_state<<<nn_grid_for(ctx, s->n_pad, 256, 16), 256, 0, ctx->stream>>>(
+        a, v0, (float)(am / (am + bm)), (float)(ah / (ah + bh)), (float)(an / (an + bn)), i_lo, i_hi, s->f[NN_F_X],
+        s->f[NN_F_Y], s->f[NN_F_Z], s->f[NN_F_GNA_SCALE], L, s->grid, s->grid > 0 ? s->vox : nullptr);
+    NN_CHECK_LAUNCH(ctx, "k_init_state");
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return NN_OK;
+}
+
+// Enqueue one step (two kernels).
+static nn_status enqueue_step(nn_sim* s, int q)
+{
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    const bool tm = s->timing && q >= 0 && q < (int)s->ev_a.size();
+    if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_a[q], cs, cudaEventRecordExternal));
+    StepArgs a = step_args(s);
+    const int warps_needed = s->n_pad / (32 * s->npt);
+    const int blocks = std::max(1, std::min((warps_needed * 32 + s->tpb - 1) / s->tpb, ctx->num_sms * 16));
+    switch (s->npt) {
+        case 1: k_hh_step<1><<<blocks, s->tpb, 0, cs>>>(a); break;
+        case 2: k_hh_step<2><<<blocks, s->tpb, 0, cs>>>(a); break;
+        default: k_hh_step<4><<<blocks, s->tpb, 0, cs>>>(a); break;
+    }
+    NN_CHECK_LAUNCH(ctx, "k_hh_step");
+    if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_b[q], cs, cudaEventRecordExternal));
+    DelivArgs d = deliv_args(s);
+    if (s->cfg.delivery == NN_DELIVERY_PULL) {
+        k_deliver_pull<<<nn_grid_for(ctx, (int64_t)s->n * 32, DELIV_THREADS, 8), DELIV_THREADS, 0, cs>>>(d);
+        NN_CHECK_LAUNCH(ctx, "k_deliver_pull");
+    } else {
+        k_deliver_push<<<ctx->num_sms * 2, DELIV_THREADS, 0, cs>>>(d);
+        NN_CHECK_LAUNCH(ctx, "k_deliver_push");
+    }
+    if (tm) {
+        NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_c[q], cs, cudaEventRecordExternal));
+        s->ev_valid[q] = 1;
+    }
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_set_kernel_timing(nn_sim* s, int enable)
+{
+    if (!s) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    const int P = s->grid > 0 ? s->cfg.timescale : 50;
+    drop_graph(s);
+    s->timing = enable != 0;
+    if (s->timing && (int)s->ev_a.size() < P) {
+        while ((int)s->ev_a.size() < P) {
+            cudaEvent_t a, b, c;
+            NN_CUDA(ctx, cudaEventCreate(&a));
+            NN_CUDA(ctx, cudaEventCreate(&b));
+            NN_CUDA(ctx, cudaEventCreate(&c));
+            s->ev_a.push_back(a);
+            s->ev_b.push_back(b);
+            s->ev_c.push_back(c);
+        }
+    }
+    s->ev_valid.assign(s->ev_a.size(), 0);
+    if (s->pcg) nn_pcg_set_timing(s->pcg, s->timing);
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out)
+{
+    if (!s || !out) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double hh = 0.0, dl = 0.0;
+    int cnt = 0;
+    for (size_t q = 0; q < s->ev_valid.size(); ++q) {
+        if (!s->ev_valid[q]) continue;
+        float a = 0.0f, b = 0.0f;
+        NN_CUDA(ctx, cudaEventElapsedTime(&a, s->ev_a[q], s->ev_b[q]));
+        NN_CUDA(ctx, cudaEventElapsedTime(&b, s->ev_b[q], s->ev_c[q]));
+        hh += a;
+        dl += b;
+        ++cnt;
+    }
+    out->hh_step_ms = cnt ? (float)(hh / cnt) : 0.0f;
+    out->deliver_ms = cnt ? (float)(dl / cnt) : 0.0f;
+    out->samples = cnt;
+    out->solve_ms = 0.0f;
+    out->solve_iterations = 0;
+    if (s->pcg) nn_pcg_last_timing(s->pcg, &out->solve_ms, &out->solve_iterations);
+    return NN_OK;
+}
+
+static nn_status paracrine_solve(nn_sim* s)
+{
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    k_par_rhs<<<nn_grid_for(ctx, s->G, 256, 8), 256, 0, cs>>>(s->u, s->src, s->b, s->G);
+    NN_CHECK_LAUNCH(ctx, "k_par_rhs");
+    int it = 0, conv = 0;
+    double rel = 0.0;
+    NN_TRY(nn_pcg_run(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, &it, &rel, &conv));
+    s->stats.iterations = it;
+    s->stats.relres = rel;
+    s->stats.converged = conv;
+    s->stats.solves += 1;
+    if (s->cfg.hp.g_par != 0.0f) {
+        k_par_gather<<<nn_grid_for(ctx, s->n, 256, 16), 256, 0, cs>>>(s->u, s->vox, s->f[NN_F_UPAR], s->n);
+        NN_CHECK_LAUNCH(ctx, "k_par_gather");
+    }
+    return NN_OK;
+}
+
+// Steps per captured graph: one paracrine period, or 50 steps without a field.
+static int period_steps(const nn_sim* s) { return s->grid > 0 ? s->cfg.timescale : 50; }
+
+static nn_status ensure_graph(nn_sim* s)
+{
+    if (s->graph) return NN_OK;
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    const int P = period_steps(s);
+    const int64_t launches0 = ctx->launches;
+    NN_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    nn_status st = NN_OK;
+    for (int q = 0; q < P && st == NN_OK; ++q) st = enqueue_step(s, q);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cs, &g);
+    ctx->launches = launches0;
+    if (st != NN_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return nn_cuda_check(ctx, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        s->graph = nullptr;
+        return nn_cuda_check(ctx, e, "cudaGraphInstantiate");
+    }
+    s->graph_steps = P;
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
+{
+    if (!s || nsteps < 0) return NN_ERR_INVALID_ARG;
+    if (!s->row_ptr) return nn_fail(s->ctx, NN_ERR_INVALID_ARG, "nn_sim_step: no network set");
+    nn_ctx* ctx = s->ctx;
+    const int P = period_steps(s);
+    int left = nsteps;
+    while (left > 0) {
+        const bool aligned = (s->host_step % P) == 0;
+        if (aligned && left >= P) {
+            NN_TRY(ensure_graph(s));
+            NN_CUDA(ctx, cudaGraphLaunch(s->graph, ctx->stream));
+            ctx->launches += 2 * (int64_t)P;
+            s->host_step += P;
+            left -= P;
+        } else {
+            NN_TRY(enqueue_step(s, (int)(s->host_step % P)));
+            s->host_step += 1;
+            left -= 1;
+        }
+        if (s->grid > 0 && (s->host_step % s->cfg.timescale) == 0) NN_TRY(paracrine_solve(s));
+    }
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_run_host(nn_sim* s, const float* h_in, int nsteps, float* h_out, int64_t* h_spikes)
+{
+    if (!s || !h_in || !h_out || nsteps < 0) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    const size_t bytes = sizeof(float) * (size_t)s->n;
+    const int planes[6] = {NN_F_V, NN_F_M, NN_F_H, NN_F_N, NN_F_GE, NN_F_GI};
+    unsigned long long t0 = 0;
+    NN_CUDA(ctx, cudaMemcpyAsync(&t0, s->total, sizeof t0, cudaMemcpyDeviceToHost, cs));
+    for (int q = 0; q < 6; ++q)
+        NN_CUDA(ctx, cudaMemcpyAsync(s->f[planes[q]], h_in + (size_t)q * s->n, bytes, cudaMemcpyHostToDevice, cs));
+    NN_TRY(nn_sim_step(s, nsteps));
+    for (int q = 0; q < 6; ++q)
+        NN_CUDA(ctx, cudaMemcpyAsync(h_out + (size_t)q * s->n, s->f[planes[q]], bytes, cudaMemcpyDeviceToHost, cs));
+    unsigned long long t1 = 0;
+    NN_CUDA(ctx, cudaMemcpyAsync(&t1, s->total, sizeof t1, cudaMemcpyDeviceToHost, cs));
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    if (h_spikes) *h_spikes = (int64_t)(t1 - t0);
+    return check_err(s);
+}
+
+extern "C" nn_status nn_sim_counters(nn_sim* s, int64_t* step, int64_t* total_spikes)
+{
+    if (!s) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    unsigned long long v[2];
+    NN_CUDA(ctx, cudaMemcpyAsync(&v[0], s->step, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    NN_CUDA(ctx, cudaMemcpyAsync(&v[1], s->total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (step) *step = (int64_t)v[0];
+    if (total_spikes) *total_spikes = (int64_t)v[1];
+    return check_err(s);
+}
+
+extern "C" nn_status nn_sim_get_raster(nn_sim* s, int64_t cap, int32_t* h_step, int32_t* h_neuron, int64_t* count)
+{
+    if (!s || !count || cap < 0) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    unsigned long long rc = 0;
+    NN_CUDA(ctx, cudaMemcpyAsync(&rc, s->rcount, sizeof rc, cudaMemcpyDeviceToHost, ctx->stream));
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *count = (int64_t)rc;
+    const int64_t m = std::min<int64_t>(cap, (int64_t)rc);
+    if (m > 0 && s->raster) {
+        std::vector<int2> tmp((size_t)m);
+        NN_CUDA(ctx, cudaMemcpyAsync(tmp.data(), s->raster, sizeof(int2) * (size_t)m, cudaMemcpyDeviceToHost, ctx->stream));
+        NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        std::sort(tmp.begin(), tmp.end(), [](const int2& a, const int2& b) { return a.x != b.x ? a.x < b.x : a.y < b.y; });
+        for (int64_t q = 0; q < m; ++q) {
+            if (h_step) h_step[q] = tmp[(size_t)q].x;
+            if (h_neuron) h_neuron[q] = tmp[(size_t)q].y;
+        }
+    }
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_get_density(nn_sim* s, float* h_u)
+{
+    if (!s || !h_u || s->grid <= 0) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    NN_CUDA(ctx, cudaMemcpyAsync(h_u, s->u, sizeof(float) * (size_t)s->G, cudaMemcpyDeviceToHost, ctx->stream));
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_set_density(nn_sim* s, const float* h_u)
+{
+    if (!s || !h_u || s->grid <= 0) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    NN_CUDA(ctx, cudaMemcpyAsync(s->u, h_u, sizeof(float) * (size_t)s->G, cudaMemcpyHostToDevice, ctx->stream));
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_solve_stats(nn_sim* s, nn_solve_stats* st)
+{
+    if (!s || !st) return NN_ERR_INVALID_ARG;
+    *st = s->stats;
+    return NN_OK;
+}

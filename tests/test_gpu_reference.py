@@ -1,0 +1,181 @@
+"""Reference-semantics primitives on the GPU against the oracle (and, for the
+network factory, the reference's own golden vectors)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import neuronephys_clean_gb300 as nn
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _init_leapfrog(eph, rng):
+    n = eph.n
+    host = {name: np.zeros(n, np.float32) for name in nn.SIM_PARAMS}
+    host["V"] = rng.normal(-55, 25, n).astype(np.float32)          # src/main.cu:333-336
+    host["M"] = rng.uniform(0, 0.2, n).astype(np.float32)
+    host["N"] = rng.uniform(0.2, 0.5, n).astype(np.float32)
+    host["H"] = rng.uniform(0.3, 0.7, n).astype(np.float32)
+    for ch in ("LOCAL", "E", "I"):
+        cnt = rng.integers(0, 12, n).astype(np.float32)
+        host[f"{ch}_COUNT" if ch == "LOCAL" else f"{ch}COUNT"] = cnt
+        host[f"{ch}_IN" if ch == "LOCAL" else f"{ch}IN"] = (cnt * rng.uniform(0, 1, n)).astype(np.float32)
+    host["APPCUR"] = rng.uniform(0, 2, n).astype(np.float32)
+    for k, v in host.items():
+        eph.set(k, v)
+    return [host[k].copy() for k in nn.SIM_PARAMS]
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_leapfrog_matches_oracle(ctx, orc, variant):
+    """Leapfrog_HH (src/ephys.cu:28-96): 25 steps of 0.4 ms (10 ms)."""
+    n, seed = 4096, 11
+    rng = np.random.default_rng(variant)
+    eph = nn.HHEphys(ctx, n, variant=variant, seed=seed)
+    host = _init_leapfrog(eph, rng)
+    params = orc.leapfrog_params(variant)
+    for step in range(25):
+        eph.simulate_ephys()
+        orc.hh_leapfrog(host, 0.4, params, orc.normals(seed, n, step))
+    got = {k: eph.get(k) for k in nn.SIM_PARAMS}
+    ref = dict(zip(nn.SIM_PARAMS, host))
+    # tolerance: 1e-4 relative with a 1 mV floor for V, absolute 1e-4 for gates/synapses/outputs
+    dv = np.abs(got["V"] - ref["V"]) / (np.abs(ref["V"]) + 1.0)
+    assert dv.max() < 1e-4, dv.max()
+    for k in ("M", "N", "H", "LOCAL_Y", "IY", "EY", "EOUTPUT", "IOUTPUT", "LOCAL_OUTPUT"):
+        assert np.abs(got[k] - ref[k]).max() < 1e-4, k
+    assert np.all(np.isfinite(got["V"]))
+
+
+def _outputs(rng, n, frac=0.1):
+    out = rng.uniform(0, 0.1, n).astype(np.float32)
+    fire = rng.random(n) < frac
+    out[fire] = rng.uniform(0.1001, 1.0, fire.sum()).astype(np.float32)
+    out[:3] = [0.1, 0.1000001, 0.0999999]   # boundary of CheckFiringOperator (> 0.1)
+    return out
+
+
+def test_coupling_push_count_and_signal(ctx, orc):
+    n = 3000
+    rng = np.random.default_rng(3)
+    nn.UniformRandomNetwork.reset_engine()
+    net = nn.UniformRandomNetwork(20)
+    assert net.generate(n)
+    tc = ctx.empty((n,), np.float32)
+    lst = net.to_adjacency_list(ctx, tc)
+    assert np.array_equal(tc.numpy(), orc.tcount(net.indices, n))
+    cp = nn.AtomicCoupling(ctx, n)
+    outs = ctx.empty((n,), np.float32)
+    ins = ctx.empty((n,), np.float32)
+    buf_emul = np.zeros(n, np.int32)
+    for trial, frac in enumerate([0.15, 0.02, 0.0, 0.3]):
+        o = _outputs(rng, n, frac)
+        outs.copy_from(o)
+        for mode in (nn.NN_SIGNAL_COUNT, nn.NN_SIGNAL_OUTPUT):
+            nf = cp(lst, ins, outs, signal_mode=mode)
+            rnf, rin, rfire = orc.coupling_push(net.indices, net.offset_in_indices, o, mode)
+            assert nf == rnf
+            if mode == nn.NN_SIGNAL_COUNT:
+                assert np.array_equal(ins.numpy(), rin)          # integer counts: bit-exact
+            else:
+                np.testing.assert_allclose(ins.numpy(), rin, rtol=2e-6, atol=1e-6)
+            buf_emul[:rnf] = rfire
+            assert np.array_equal(cp.get_firing_neurons(), buf_emul)  # ascending + stale tail
+
+
+def test_chunked_list_and_coupling(ctx, orc):
+    n = 2 * 7319
+    rng = np.random.default_rng(5)
+    nn.UniformRandomNetwork.reset_engine()
+    net = nn.UniformRandomNetwork(3)
+    net.generate(n)
+    tc = ctx.empty((n,), np.float32)
+    ch = net.to_chunked_adjacency_list(ctx, tc, 2, 7319)
+    ci, co = orc.chunked(net.indices, net.offset_in_indices, n, 2, 7319)
+    for c in range(2):
+        assert ch.chunk_nnz[c] == len(ci[c])
+        assert np.array_equal(ch.indices_chunks[c].numpy()[:len(ci[c])], ci[c])
+        assert np.array_equal(ch.offset_in_indices_chunks[c].numpy(), co[c])
+    lst = net.to_adjacency_list(ctx, tc)
+    cp = nn.AtomicCoupling(ctx, n)
+    o = _outputs(rng, n, 0.2)
+    outs = ctx.to_device(o)
+    a, b = ctx.empty((n,), np.float32), ctx.empty((n,), np.float32)
+    assert cp(lst, a, outs) == cp(ch, b, outs)
+    assert np.array_equal(a.numpy(), b.numpy())
+
+
+def test_device_tcount_matches_reference_golden(ctx):
+    g = np.load(GOLDEN / "ref_netgen_A.npz")
+    net = nn.Network()
+    net.indices, net.offset_in_indices = g["e_indices"], g["e_offsets"]
+    tc = ctx.empty((1000,), np.float32)
+    net.to_adjacency_list(ctx, tc)
+    assert np.array_equal(tc.numpy(), g["e_tcount"])
+
+
+STENCIL = np.array([1, 3, 1, 3, 14, 3, 1, 3, 1, 3, 14, 3, 14, -128, 14, 3, 14, 3,
+                    1, 3, 1, 3, 14, 3, 1, 3, 1], np.float64)
+
+
+@pytest.mark.parametrize("quirk", [1, 0])
+def test_paracrine_module_matches_oracle(ctx, orc, quirk):
+    """scatter -> CN/27-point CG -> interpolate (src/paracrine.cu:63-296)."""
+    n, g, h = 2000, 16, 1.0
+    rng = np.random.default_rng(7)
+    L = (g - 1) * h
+    xyz = [rng.uniform(-L / 2, L / 2 * 0.999, n).astype(np.float32) for _ in range(3)]
+    p = nn.ParacrineModule.default_params()
+    p.nx = p.ny = p.nz = g
+    p.h, p.D, p.decay, p.par_dt = h, 0.05, 3e-4, 1.0
+    p.quirk_rhs = quirk
+    gpar = ctx.empty((n,), np.float32)
+    pm = nn.ParacrineModule(ctx, gpar, n, p, *[ctx.to_device(a) for a in xyz])
+    idx, w = orc.trilinear(*xyz, g, g, g, h)
+    u = np.zeros(g ** 3)
+    for rnd in range(3):
+        s = (rng.random(n) < 0.3).astype(np.float32) * 0.5
+        pm.set_sources(s)
+        it, rr = pm.update_on_own_timescale()
+        orc.lib().orc_scatter(n, orc.ptr(idx), orc.ptr(w), orc.ptr(s.astype(np.float64)), orc.ptr(u))
+        u, rit, rrr = orc.paracrine_cn_solve(u, (g, g, g), h, p.D, p.decay, p.par_dt, 1e-6, 20, quirk)
+        assert it == rit
+        dens = pm.density().astype(np.float64)
+        assert np.abs(dens - u).max() <= 1e-5 * max(1.0, np.abs(u).max())
+        interp = np.zeros(n)
+        orc.lib().orc_interp(n, orc.ptr(idx), orc.ptr(w), orc.ptr(u), orc.ptr(interp))
+        np.testing.assert_allclose(gpar.numpy(), interp, rtol=1e-5, atol=1e-6)
+        assert np.all(pm.sources() == 0)
+
+
+def test_paracrine_fine_update_quirk(ctx, orc):
+    """update_on_fine_timescale keys on the compacted index buffer
+    (src/paracrine.cuh:250-252); quirk_firing_list=0 keys on the firing set."""
+    n = 500
+    rng = np.random.default_rng(9)
+    xyz = [ctx.to_device(rng.uniform(-7, 7, n).astype(np.float32)) for _ in range(3)]
+    nn.UniformRandomNetwork.reset_engine()
+    net = nn.UniformRandomNetwork(4)
+    net.generate(n)
+    tc = ctx.empty((n,), np.float32)
+    lst = net.to_adjacency_list(ctx, tc)
+    cp = nn.AtomicCoupling(ctx, n)
+    for quirk in (1, 0):
+        p = nn.ParacrineModule.default_params()
+        p.nx = p.ny = p.nz = 16
+        p.quirk_firing_list = quirk
+        pm = nn.ParacrineModule(ctx, ctx.empty((n,), np.float32), n, p, *xyz)
+        o = _outputs(rng, n, 0.1)
+        ins = ctx.empty((n,), np.float32)
+        cp(lst, ins, ctx.to_device(o))
+        pm.update_on_fine_timescale(cp)
+        buf = cp.get_firing_neurons()
+        fired = np.flatnonzero(o > np.float32(0.1))
+        want = np.zeros(n, np.float32)
+        if quirk:
+            want[buf != 0] += p.coup_strength
+        else:
+            want[fired] += p.coup_strength
+        assert np.array_equal(pm.sources(), want)

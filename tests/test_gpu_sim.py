@@ -1,0 +1,175 @@
+"""The GB300 simulation step against the FP64 oracle of the same model.
+
+Tolerances (stated per result):
+* V, m, h, n over the first 10 ms: |gpu - oracle| <= 1e-4 * (|oracle| + s), with
+  the floor s = 1 mV for V and 1e-3 for gating variables (relative error
+  with a floor, since V crosses 0 and gates approach 0);
+* spike rasters over the first 10 ms: identical (step, neuron) sets;
+* population spike count over 50 ms: within 1 %.
+"""
+import numpy as np
+import pytest
+
+import neuronephys_clean_gb300 as nn
+
+pytestmark = pytest.mark.gpu
+
+
+def make_sim(ctx, n=1000, delivery=0, seed=2024, raster=200000, grid=0, **kw):
+    c = nn.default_config(n)
+    c.seed = seed
+    c.delivery = delivery
+    c.raster_capacity = raster
+    c.grid = grid
+    for k, v in kw.items():
+        setattr(c, k, v)
+    s = nn.Simulation(ctx, c)
+    spec = nn.default_net_spec(nn.NN_NET_ER)
+    spec.p, spec.w_max = 0.01, 0.5
+    s.generate_network(spec)
+    s.init_state(-65.0, 5.0, 15.0)
+    return s
+
+
+def oracle_for(orc, s, seed, grid=0, vox=None):
+    rp, col, w, d, inh = s.get_network()
+    state = np.stack([s.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")])
+    net = orc.CSR(rp, col, w, d)
+    return orc.Sim(net, inh, s.get_field("IDRIVE"), seed, s.config.max_delay + 1, state,
+                   vox=vox, grid_cells=grid ** 3 if grid else 0)
+
+
+def gpu_state(s):
+    return np.stack([s.get_field(k) for k in ("V", "M", "H", "N")])
+
+
+def check_state(got, ref):
+    V, gates = got[0], got[1:4]
+    rV, rg = ref[0], ref[1:4]
+    assert (np.abs(V - rV) / (np.abs(rV) + 1.0)).max() < 1e-4
+    assert (np.abs(gates - rg) / (np.abs(rg) + 1e-3)).max() < 1e-4
+
+
+def raster_set(steps, neurons):
+    return set(zip(steps.tolist(), neurons.tolist()))
+
+
+@pytest.mark.parametrize("delivery", [0, 1])
+def test_first_10ms_parity(ctx, orc, delivery):
+    seed = 2024
+    s = make_sim(ctx, delivery=delivery, seed=seed)
+    o = oracle_for(orc, s, seed)
+    ref_spikes = set()
+    for t in range(1000):
+        for j in o.step():
+            ref_spikes.add((t, int(j)))
+    s.step(1000)
+    check_state(gpu_state(s), o.state()[:4])
+    st, ne = s.raster()
+    assert len(ref_spikes) > 50
+    assert raster_set(st, ne) == ref_spikes
+    step, total = s.counters()
+    assert step == 1000 and total == len(ref_spikes)
+
+
+def test_population_rate_50ms(ctx, orc):
+    seed = 7
+    s = make_sim(ctx, seed=seed, raster=0)
+    o = oracle_for(orc, s, seed)
+    nref = sum(len(o.step()) for _ in range(5000))
+    s.step(5000)
+    _, total = s.counters()
+    assert nref > 500
+    assert abs(total - nref) / nref < 0.01
+
+
+def test_push_pull_agree_and_pull_is_deterministic(ctx):
+    a = make_sim(ctx, delivery=0, seed=5)
+    b = make_sim(ctx, delivery=1, seed=5)
+    c = make_sim(ctx, delivery=1, seed=5)
+    for s in (a, b, c):
+        s.step(1000)
+    assert raster_set(*a.raster()) == raster_set(*b.raster())
+    np.testing.assert_allclose(gpu_state(a), gpu_state(b), rtol=1e-4, atol=1e-4)
+    assert np.array_equal(gpu_state(b), gpu_state(c))
+
+
+def test_delays_parity(ctx, orc):
+    """Gaussian network with delays U{1..20}: raster and state vs the oracle."""
+    n, seed = 2744, 31
+    c = nn.default_config(n)
+    c.seed, c.max_delay, c.raster_capacity = seed, 20, 100000
+    for delivery in (0, 1):
+        c.delivery = delivery
+        s = nn.Simulation(ctx, c)
+        spec = nn.default_net_spec(nn.NN_NET_GAUSS)
+        spec.k, spec.dmax, spec.w_mu = 30, 20, 0.0
+        s.generate_network(spec)
+        s.init_state(-65.0, 6.0, 12.0)
+        o = oracle_for(orc, s, seed)
+        ref = set()
+        for t in range(600):
+            ref |= {(t, int(j)) for j in o.step()}
+        s.step(600)
+        assert len(ref) > 50
+        assert raster_set(*s.raster()) == ref
+        check_state(gpu_state(s), o.state()[:4])
+
+
+def test_paracrine_field(ctx, orc):
+    """Deposits of 100 steps, then one 7-point backward-Euler PCG solve."""
+    seed, g, ts = 17, 16, 100
+    s = make_sim(ctx, seed=seed, grid=g, timescale=ts, par_D=1.0, par_decay=0.5)
+    x, y, z = (s.get_field(k) for k in ("X", "Y", "Z"))
+    ix = np.clip((x * np.float32(g)).astype(np.int32), 0, g - 1)
+    iy = np.clip((y * np.float32(g)).astype(np.int32), 0, g - 1)
+    iz = np.clip((z * np.float32(g)).astype(np.int32), 0, g - 1)
+    vox = (ix + g * (iy + g * iz)).astype(np.int32)
+    o = oracle_for(orc, s, seed, grid=g, vox=vox)
+    for _ in range(ts):
+        o.step()
+    s.step(ts)
+    src = o.src.copy()
+    dt_s = ts * 0.01 * 1e-3
+    alpha, beta = dt_s * 1.0 * g * g, dt_s * 0.5
+    ref, it, _ = orc.pcg7(src, np.zeros(g ** 3), (g, g, g), alpha, beta, rtol=1e-12)
+    got = s.density()
+    st = s.solve_stats()
+    assert st.converged and st.relres <= 1e-6 and st.solves == 1
+    assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref)
+    assert src.sum() > 0 and abs(src.sum() - s.counters()[1]) < 1e-6
+
+
+def test_run_host_matches_device_path(ctx):
+    a = make_sim(ctx, seed=9, raster=0)
+    b = make_sim(ctx, seed=9, raster=0)
+    state = np.stack([a.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")]).astype(np.float32)
+    out = np.empty_like(state)
+    spikes = a.run_host(np.ascontiguousarray(state), 300, out)
+    b.step(300)
+    ref = np.stack([b.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")])
+    assert np.array_equal(out, ref)
+    assert spikes == b.counters()[1]
+
+
+def test_non_finite_state_is_reported(ctx):
+    s = make_sim(ctx, seed=1, raster=0)
+    v = s.get_field("V")
+    v[17] = np.nan
+    s.set_field("V", v)
+    s.step(2)
+    with pytest.raises(nn.NNError) as e:
+        s.get_field("V")
+    assert e.value.status == 5
+
+
+def test_invalid_network_rejected(ctx):
+    c = nn.default_config(10)
+    s = nn.Simulation(ctx, c)
+    with pytest.raises(nn.NNError) as e:
+        s.set_network(np.array([0, 1] + [1] * 9, np.int64), np.array([10], np.int32),
+                      np.array([0.1], np.float32), np.array([1], np.uint8))
+    assert e.value.status == 1
+    with pytest.raises(nn.NNError):
+        s.set_network(np.array([0, 1] + [1] * 9, np.int64), np.array([3], np.int32),
+                      np.array([0.1], np.float32), np.array([2], np.uint8))  # delay > max_delay
