@@ -125,7 +125,7 @@ class ClockSampler:
             self.path = Path(f"/tmp/nn_clocks_{os.getpid()}.csv")
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -187,8 +187,10 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     import neuronephys_clean_gb300 as nn
     ctx = nn.Context(local_rank)
     sim = build_sim(nn, ctx, wl)
-    P = wl["timescale"]
+    P = wl["total_steps"]  # timesteps per bench step: one full run of the workload
     n = wl["n"]
+    # settle: start the timed region in steady tonic firing, not at rest
+    sim.step(args.settle)
     # CUDA events bracket every neuron-update / delivery launch (event nodes in
     # the captured period graph) and the solver iterations, inside the timed region
     sim.set_kernel_timing(True)
@@ -363,10 +365,10 @@ def run_reference(args, wl: dict, rank: int) -> dict | None:
     cb = dict(res)
     cb["value"] = value
     return {"metric": "neuron-steps/s", "value": value, "unit": "neuron-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * wl["timescale"] * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * wl["total_steps"] * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded counter-based generators)", "impl": "reference",
-            "config": {"workload": wl["workload"], "neurons": wl["n"], "timesteps_per_step": wl["timescale"]},
+            "config": {"workload": wl["workload"], "neurons": wl["n"], "timesteps_per_step": wl["total_steps"]},
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "neuron-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -379,6 +381,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--settle", type=int, default=2000, help="untimed timesteps before the warm-up")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()

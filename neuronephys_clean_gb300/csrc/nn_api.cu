@@ -70,15 +70,30 @@ extern "C" nn_status nn_ctx_create(int device, nn_ctx** out)
     return NN_OK;
 }
 
-extern "C" nn_status nn_ctx_destroy(nn_ctx* ctx)
+void nn_ctx_retain(nn_ctx* ctx)
 {
-    if (!ctx) return NN_OK;
+    if (ctx) ++ctx->refs;
+}
+
+void nn_ctx_release(nn_ctx* ctx)
+{
+    if (!ctx || --ctx->refs > 0) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+// Drops the caller's reference; objects still alive on the context keep it
+// (and its stream) until they are destroyed.
+extern "C" nn_status nn_ctx_destroy(nn_ctx* ctx)
+{
+    if (!ctx) return NN_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    nn_ctx_release(ctx);
     return NN_OK;
 }
 

@@ -116,6 +116,6 @@ __device__ __forceinline__ float nn_normal(uint64_t seed, uint32_t i, uint64_t s
     const float u1 = nn_u01f_open(r.x), u2 = nn_u01f(r.y);
     const float rad = sqrtf(-2.0f * logf(u1));
     float s, c;
-    __sincosf(6.28318530717958647692f * u2, &s, &c);
+    sincospif(2.0f * u2, &s, &c);
     return (step & 1u) ? rad * s : rad * c;
 }

@@ -19,7 +19,14 @@ struct nn_ctx {
     std::string last_error;
     int64_t launches = 0;  // kernels launched on behalf of the caller
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // nn_ctx_time_begin/end
+    // Objects created on a context hold a reference, so destroying the context
+    // before them (in any order) never leaves them with a dangling pointer.
+    int refs = 1;
 };
+
+// Take / drop a reference; the last release frees the context.
+void nn_ctx_retain(nn_ctx* ctx);
+void nn_ctx_release(nn_ctx* ctx);
 
 nn_status nn_fail(nn_ctx* ctx, nn_status st, const char* fmt, ...);
 nn_status nn_cuda_check(nn_ctx* ctx, cudaError_t e, const char* what);

@@ -109,16 +109,23 @@ __device__ bool last_block_sum(int nsum, const double* v, double* partials, unsi
     }
     __syncthreads();
     if (!last) return false;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        for (int q = 0; q < nsum; ++q) {
-            double s = 0.0;
-            const volatile double* pp = partials + (size_t)q * gridDim.x;
-            for (unsigned b = 0; b < gridDim.x; ++b) s += pp[b];
-            out[q] = s;
+    // the last block sums the partials with all its threads (fixed order)
+    __threadfence();
+    for (int q = 0; q < nsum; ++q) {
+        const volatile double* pp = partials + (size_t)q * gridDim.x;
+        double s = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += PCG_THREADS) s += pp[b];
+        s = nn_warp_sum(s);
+        __syncthreads();
+        if (lane == 0) ws[q][w] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int u = 0; u < PCG_THREADS / 32; ++u) t += ws[q][u];
+            out[q] = t;
         }
-        *ticket = 0;
     }
+    if (threadIdx.x == 0) *ticket = 0;
     __syncthreads();
     return true;
 }
@@ -281,6 +288,7 @@ extern "C" nn_status nn_pcg_create(nn_ctx* ctx, int nx, int ny, int nz, double a
         return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_pcg_create: bad argument");
     nn_pcg* pc = new nn_pcg();
     pc->ctx = ctx;
+    nn_ctx_retain(ctx);
     pc->nx = nx; pc->ny = ny; pc->nz = nz;
     pc->G = (int64_t)nx * ny * nz;
     pc->alpha = alpha;
@@ -327,7 +335,9 @@ extern "C" nn_status nn_pcg_destroy(nn_pcg* pc)
     nn_release(pc->partials); nn_release(pc->ticket); nn_release(pc->flags); nn_release(pc->invd);
     for (auto e : pc->ev_a) cudaEventDestroy(e);
     for (auto e : pc->ev_b) cudaEventDestroy(e);
+    nn_ctx* ctx = pc->ctx;
     delete pc;
+    nn_ctx_release(ctx);
     return NN_OK;
 }
 

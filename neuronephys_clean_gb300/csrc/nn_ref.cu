@@ -232,6 +232,7 @@ extern "C" nn_status nn_coupling_create(nn_ctx* ctx, int n, nn_coupling** out)
     if (!ctx || !out || n < 0) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_coupling_create: bad argument");
     nn_coupling* c = new nn_coupling();
     c->ctx = ctx;
+    nn_ctx_retain(ctx);
     c->n = n;
     c->nblocks = (n + CMP_TILE - 1) / CMP_TILE;
     if (c->nblocks < 1) c->nblocks = 1;
@@ -256,7 +257,9 @@ extern "C" nn_status nn_coupling_destroy(nn_coupling* c)
     nn_release(c->firing);
     nn_release(c->count);
     nn_release(c->block_counts);
+    nn_ctx* ctx = c->ctx;
     delete c;
+    nn_ctx_release(ctx);
     return NN_OK;
 }
 
@@ -635,11 +638,18 @@ __device__ bool last_block_reduce(double v, double* partials, unsigned int* tick
     }
     __syncthreads();
     if (!is_last) return false;
+    // the last block sums the partials with all its threads (fixed order)
+    __threadfence();
+    double s = 0.0;
+    for (unsigned q = threadIdx.x; q < gridDim.x; q += blockDim.x) s += ((volatile double*)partials)[q];
+    s = nn_warp_sum(s);
+    __syncthreads();
+    if (lane == 0) ws[w] = s;
+    __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        double s = 0.0;
-        for (unsigned q = 0; q < gridDim.x; ++q) s += ((volatile double*)partials)[q];
-        *result = s;
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += ws[q];
+        *result = t;
         *ticket = 0;
     }
     __syncthreads();
@@ -721,6 +731,7 @@ extern "C" nn_status nn_paracrine_ref_create(nn_ctx* ctx, const nn_paracrine_ref
         return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_paracrine_ref_create: bad argument");
     nn_paracrine* pm = new nn_paracrine();
     pm->ctx = ctx;
+    nn_ctx_retain(ctx);
     pm->p = *p;
     pm->n = n;
     pm->G = (int64_t)p->nx * p->ny * p->nz;
@@ -770,7 +781,9 @@ extern "C" nn_status nn_paracrine_destroy(nn_paracrine* pm)
     nn_release(pm->x); nn_release(pm->b); nn_release(pm->r); nn_release(pm->pv); nn_release(pm->Ap);
     nn_release(pm->at_neurons); nn_release(pm->generated); nn_release(pm->scal); nn_release(pm->partials);
     nn_release(pm->ticket); nn_release(pm->done);
+    nn_ctx* ctx = pm->ctx;
     delete pm;
+    nn_ctx_release(ctx);
     return NN_OK;
 }
 
@@ -848,6 +861,21 @@ extern "C" nn_status nn_paracrine_ref_own(nn_paracrine* pm, int* iters, float* f
         k_interp<<<nb, 256, 0, s>>>(pm->n, pm->idx8, pm->w8, pm->u, G, pm->at_neurons, pm->g_out);
         NN_CHECK_LAUNCH(ctx, "k_interp");
         NN_CUDA(ctx, cudaMemsetAsync(pm->generated, 0, sizeof(float) * (size_t)pm->n, s));
+    }
+    if (std::getenv("NN_DEBUG_PARACRINE")) {
+        int h_done[2];
+        double h_scal[3];
+        std::vector<float> hu((size_t)G), hx((size_t)G), hax((size_t)G);
+        cudaMemcpyAsync(h_done, pm->done, sizeof h_done, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(h_scal, pm->scal, sizeof h_scal, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hu.data(), pm->u, sizeof(float) * (size_t)G, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hx.data(), pm->x, sizeof(float) * (size_t)G, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hax.data(), pm->Ax, sizeof(float) * (size_t)G, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        double su = 0, sx = 0, sa = 0;
+        for (int64_t q = 0; q < G; ++q) { su += hu[(size_t)q]; sx += hx[(size_t)q]; sa += hax[(size_t)q]; }
+        fprintf(stderr, "[paracrine] done=%d iters=%d rr0=%g pAp=%g rr=%g sum(u)=%.9g sum(x)=%.9g sum(Ax)=%.9g\n",
+                h_done[0], h_done[1], h_scal[0], h_scal[1], h_scal[2], su, sx, sa);
     }
     if (iters || final_rr) {
         int h_done[2];

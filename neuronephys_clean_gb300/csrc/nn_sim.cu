@@ -692,6 +692,7 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
         return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: neurons_per_thread must be 1, 2 or 4");
     nn_sim* s = new nn_sim();
     s->ctx = ctx;
+    nn_ctx_retain(ctx);
     s->cfg = *cfg;
     s->n = cfg->n;
     s->n_pad = (cfg->n + 127) / 128 * 128;
@@ -700,7 +701,7 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
     s->npt = cfg->neurons_per_thread ? cfg->neurons_per_thread : 2;
     s->tpb = cfg->threads_per_block ? cfg->threads_per_block : 256;
     if (s->tpb % 32 || s->tpb > 256 || s->tpb < 32) {
-        delete s;
+        nn_sim_destroy(s);
         return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: threads_per_block must be a multiple of 32 <= 256");
     }
     s->grid = cfg->grid;
@@ -784,7 +785,9 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     for (auto e : s->ev_a) cudaEventDestroy(e);
     for (auto e : s->ev_b) cudaEventDestroy(e);
     for (auto e : s->ev_c) cudaEventDestroy(e);
+    nn_ctx* ctx = s->ctx;
     delete s;
+    nn_ctx_release(ctx);
     return NN_OK;
 }
 

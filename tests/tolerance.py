@@ -1,0 +1,52 @@
+"""Trajectory tolerance shared by the parity tests.
+
+FP32 device state against the FP64 oracle: rounding differences of ~1e-7 are
+amplified only at spike initiation, where the upstroke is unstable; a neuron
+caught mid-spike at the checkpoint can differ by ~1e-3 relative although its
+spike time agrees to well under a microsecond.  The criterion is therefore
+stated per neuron:
+
+* |dV/dt| < 20 mV/ms at the checkpoint (not in a spike): every variable within
+  ``rtol`` = 1e-4 relative, with floors of 1 mV for V and 1e-3 for gates;
+* steep neurons (in a spike): each variable's difference below its rate of
+  change times a spike-time shift of 1 us (|dx/dt| * 1e-3 ms), plus the
+  1e-4-relative allowance;
+
+and spike rasters must be identical (checked by the callers).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+STEEP_MV_PER_MS = 20.0
+SHIFT_MS = 1e-3
+
+
+def trajectory_errors(got: np.ndarray, ref: np.ndarray, ref_prev: np.ndarray, dt_ms: float,
+                      rtol: float = 1e-4) -> dict:
+    """got/ref/ref_prev: (4, n) arrays of V, m, h, n.  Returns violation counts
+    and the error statistics used in reports."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    rate = np.abs(ref - np.asarray(ref_prev, np.float64)) / dt_ms
+    steep = rate[0] >= STEEP_MV_PER_MS
+    floors = np.array([1.0, 1e-3, 1e-3, 1e-3])[:, None]
+    err = np.abs(got - ref)
+    rel = err / (np.abs(ref) + floors)
+    allow = rtol * (np.abs(ref) + floors)
+    allow_steep = allow + rate * SHIFT_MS
+    bad_flat = (err > allow) & ~steep[None, :]
+    bad_steep = (err > allow_steep) & steep[None, :]
+    return {
+        "violations": int(bad_flat.sum() + bad_steep.sum()),
+        "steep_neurons": int(steep.sum()),
+        "max_rel_flat": float(rel[:, ~steep].max()) if (~steep).any() else 0.0,
+        "max_rel_all": float(rel.max()),
+        "median_rel": float(np.median(rel)),
+    }
+
+
+def assert_trajectory(got, ref, ref_prev, dt_ms, rtol=1e-4):
+    e = trajectory_errors(got, ref, ref_prev, dt_ms, rtol)
+    assert e["violations"] == 0, e
+    return e
