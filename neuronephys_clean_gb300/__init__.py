@@ -60,8 +60,9 @@ def _check(st: int, ctx: "Context | None" = None, what: str = "") -> None:
 
 
 def _ptr(a: np.ndarray) -> C.c_void_p:
+    """Pointer to a contiguous array; the returned object keeps the array alive."""
     assert a.flags["C_CONTIGUOUS"]
-    return C.c_void_p(a.ctypes.data)
+    return a.ctypes.data_as(C.c_void_p)
 
 
 class Context:

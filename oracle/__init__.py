@@ -88,10 +88,12 @@ def lib() -> C.CDLL:
 
 
 def ptr(a: np.ndarray | None) -> C.c_void_p | None:
+    """Pointer to a contiguous array; the returned object keeps the array alive
+    (so temporaries passed as ptr(np.ascontiguousarray(...)) stay valid)."""
     if a is None:
         return None
     assert a.flags["C_CONTIGUOUS"]
-    return C.c_void_p(a.ctypes.data)
+    return a.ctypes.data_as(C.c_void_p)
 
 
 # ------------------------------------------------------------ helpers ------
