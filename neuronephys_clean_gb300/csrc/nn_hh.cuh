@@ -47,9 +47,10 @@ __device__ __forceinline__ nn_rates nn_hh_rates(float V)
 {
     nn_rates r;
     const float um = (V + 40.0f) * 0.1f;
-    const float un = (V + 55.0f) * 0.1f;
-    r.am = nn_xexprel(um, __expf(-um));
-    r.an = 0.1f * nn_xexprel(un, __expf(-un));
+    const float un = (V + 55.0f) * 0.1f;  // = um + 1.5
+    const float em = __expf(-um);
+    r.am = nn_xexprel(um, em);
+    r.an = 0.1f * nn_xexprel(un, em * 0.22313016014842982f);  // e^{-un} = e^{-um} e^{-1.5}
     const float q = __expf((V + 65.0f) * (-1.0f / 80.0f));  // e^{-(V+65)/80}
     r.bn = 0.125f * q;
     const float q2 = q * q;
@@ -108,14 +109,23 @@ __device__ __forceinline__ void nn_hh_rk4(const nn_hh_dev& p, float gna, float i
     y.gi += s6 * (k1.gi + 2.0f * (k2.gi + k3.gi) + k4.gi);
 }
 
-// Standard normal for (neuron i, step) from the counter-based stream: one
-// Philox call serves two consecutive steps (Box-Muller cos / sin branches).
-__device__ __forceinline__ float nn_normal(uint64_t seed, uint32_t i, uint64_t step)
+// Standard normals for the neuron pair (2k, 2k+1) at one step from the
+// counter-based stream: one Philox call and one Box-Muller transform per pair
+// (cos branch for the even neuron, sin branch for the odd one).
+__device__ __forceinline__ void nn_normal_pair(uint64_t seed, uint32_t k, uint64_t step, float& z0, float& z1)
 {
-    const nn_u4 r = nn_philox(seed, i, (uint32_t)(step >> 1), (uint32_t)(step >> 33), NN_P_NOISE);
+    const nn_u4 r = nn_philox(seed, k, (uint32_t)step, (uint32_t)(step >> 32), NN_P_NOISE);
     const float u1 = nn_u01f_open(r.x), u2 = nn_u01f(r.y);
     const float rad = sqrtf(-2.0f * logf(u1));
     float s, c;
     sincospif(2.0f * u2, &s, &c);
-    return (step & 1u) ? rad * s : rad * c;
+    z0 = rad * c;
+    z1 = rad * s;
+}
+
+__device__ __forceinline__ float nn_normal(uint64_t seed, uint32_t i, uint64_t step)
+{
+    float z0, z1;
+    nn_normal_pair(seed, i >> 1, step, z0, z1);
+    return (i & 1u) ? z1 : z0;
 }

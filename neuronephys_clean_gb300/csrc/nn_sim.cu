@@ -41,7 +41,6 @@ struct nn_sim {
     unsigned long long* total = nullptr;    // spikes so far
     unsigned long long* rcount = nullptr;   // raster entries written
     int2* raster = nullptr;        // (step, neuron)
-    unsigned int* ticket = nullptr;
     int* err = nullptr;
     uint8_t* is_inh = nullptr;
     // network
@@ -89,11 +88,22 @@ struct StepArgs {
     const float* idrive;
     const float* gna_scale;
     const float* upar;
-    float* ring;            // float2 interleaved
-    uint32_t* bitmap;
-    int* list;
+    float* ring;            // float2 (E, I) per neuron, D slots
+    uint32_t* bitmap;       // pull delivery: spike bitmap of the last D steps
+    int* list;              // spikes of the step (by step parity)
     int* counts;
-    const unsigned long long* step;
+    const unsigned long long* base;  // first step of the current period
+    int q;                  // this launch's step within the period
+    // push delivery (row_ptr == nullptr: pull delivery runs as its own kernel)
+    const int64_t* row_ptr;
+    const int32_t* col;
+    const float* weight;
+    const uint8_t* delay;
+    const uint8_t* is_inh;
+    unsigned long long* total;
+    unsigned long long* rcount;
+    int2* raster;
+    long long rcap;
     const int32_t* vox;
     float* src;
     int* err;
@@ -129,12 +139,18 @@ __device__ __forceinline__ void vstore(float* base, int i0, const float (&in)[NP
     *reinterpret_cast<V*>(base + i0) = v;
 }
 
-// One simulation step of NPT consecutive neurons per lane.  Loop trip counts
-// are warp-uniform so the warp-collective compaction stays converged.
+// One simulation step, NPT consecutive neurons per lane:
+//   ring slot t%D -> (ge, gi) jump, RK4 with noise, upward threshold crossing,
+//   warp-aggregated compaction (one atomic per warp with spikes), spike bitmap
+//   (pull), voxel deposit, raster, and -- in push mode -- the delivery itself:
+//   the warp that found the spikes scatters their out-edges into ring slots
+//   (t+d)%D with red.global.add (d >= 1, so never the slot this launch reads).
+// Loop trip counts are warp-uniform so the warp collectives stay converged.
 template <int NPT>
 __global__ void __launch_bounds__(256) k_hh_step(StepArgs a)
 {
-    const uint64_t t = *a.step;
+    const uint64_t t = *a.base + (uint64_t)a.q;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.counts[(t + 1) & 1] = 0;  // next step's count
     const int slot = (int)(t % (uint64_t)a.D);
     float* ring_slot = a.ring + (size_t)slot * a.n_pad * 2;
     int* list = a.list + (size_t)(t & 1) * a.n_pad;
@@ -177,6 +193,14 @@ __global__ void __launch_bounds__(256) k_hh_step(StepArgs a)
 #pragma unroll
             for (int q = 0; q < NPT; ++q) UP[q] = 0.0f;
         }
+        // noise: one Philox draw and one Box-Muller per neuron pair
+        float Z[NPT];
+        if (NPT == 1) {
+            Z[0] = nn_normal(a.seed, (uint32_t)i0, t);
+        } else {
+#pragma unroll
+            for (int q = 0; q < NPT; q += 2) nn_normal_pair(a.seed, (uint32_t)(i0 + q) >> 1, t, Z[q], Z[q + 1]);
+        }
         uint32_t mask = 0;
         bool bad = false;
         bool any_in = false;
@@ -185,7 +209,7 @@ __global__ void __launch_bounds__(256) k_hh_step(StepArgs a)
             const int i = i0 + q;
             nn_hh_state y{V[q], M[q], H[q], N[q], GE[q] + RG[2 * q], GI[q] + RG[2 * q + 1]};
             any_in |= (RG[2 * q] != 0.0f) | (RG[2 * q + 1] != 0.0f);
-            const float iext = ID[q] + a.p.noise_sigma * nn_normal(a.seed, (uint32_t)i, t);
+            const float iext = ID[q] + a.p.noise_sigma * Z[q];
             const float v_old = y.V;
             nn_hh_rk4(a.p, a.p.gNa * GS[q], iext, a.p.g_par * UP[q], y);
             const bool valid = i < a.n;
@@ -216,116 +240,81 @@ __global__ void __launch_bounds__(256) k_hh_step(StepArgs a)
             for (int o = 1; o < 32 / NPT; o <<= 1) bits |= __shfl_xor_sync(0xffffffffu, bits, o);
             if ((lane % (32 / NPT)) == 0) bm[(ch * chunk + lane * NPT) >> 5] = bits;
         }
-        // warp-aggregated compaction: one atomic per warp with spikes
         const int c = __popc(mask);
-        if (__any_sync(0xffffffffu, c != 0)) {
-            int inc = c;
+        if (!__any_sync(0xffffffffu, c != 0)) continue;
+        // warp-aggregated compaction, totals and raster: one atomic each per warp
+        int inc = c;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int tv = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += tv;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int tv = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += tv;
+        }
+        const int tot = __shfl_sync(0xffffffffu, inc, 31);
+        int base = 0;
+        unsigned long long rbase = 0;
+        if (lane == 31) {
+            base = atomicAdd(cnt, tot);
+            atomicAdd(a.total, (unsigned long long)tot);
+            if (a.raster) rbase = atomicAdd(a.rcount, (unsigned long long)tot);
+        }
+        base = __shfl_sync(0xffffffffu, base, 31);
+        rbase = __shfl_sync(0xffffffffu, rbase, 31);
+        int pos = base + inc - c;
+        unsigned long long rpos = rbase + (unsigned long long)(inc - c);
+#pragma unroll
+        for (int q = 0; q < NPT; ++q)
+            if (mask & (1u << q)) {
+                list[pos++] = i0 + q;
+                if (a.src) atomicAdd(a.src + a.vox[i0 + q], 1.0f);
+                if (a.raster && rpos < (unsigned long long)a.rcap) a.raster[rpos] = make_int2((int)t, i0 + q);
+                ++rpos;
             }
-            const int tot = __shfl_sync(0xffffffffu, inc, 31);
-            int base = 0;
-            if (lane == 31) base = atomicAdd(cnt, tot);
-            base = __shfl_sync(0xffffffffu, base, 31);
-            int pos = base + inc - c;
+        // push delivery of this warp's spikes, all lanes over each out-edge list
+        if (a.row_ptr) {
+            unsigned who = __ballot_sync(0xffffffffu, mask != 0);
+            while (who) {
+                const int sl_lane = __ffs(who) - 1;
+                who &= who - 1;
+                const uint32_t m = __shfl_sync(0xffffffffu, mask, sl_lane);
 #pragma unroll
-            for (int q = 0; q < NPT; ++q)
-                if (mask & (1u << q)) {
-                    list[pos++] = i0 + q;
-                    if (a.src) atomicAdd(a.src + a.vox[i0 + q], 1.0f);
+                for (int q = 0; q < NPT; ++q) {
+                    if (!(m & (1u << q))) continue;
+                    const int j = ch * chunk + sl_lane * NPT + q;
+                    const int chn = a.is_inh[j] ? 1 : 0;
+                    const int64_t beg = a.row_ptr[j], end = a.row_ptr[j + 1];
+                    for (int64_t e = beg + lane; e < end; e += 32) {
+                        int sl = slot + (int)a.delay[e];
+                        if (sl >= a.D) sl -= a.D;
+                        atomicAdd(a.ring + 2 * ((size_t)sl * a.n_pad + a.col[e]) + chn, a.weight[e]);
+                    }
                 }
+            }
         }
     }
 }
 
-struct DelivArgs {
-    const int64_t* row_ptr;
-    const int32_t* col;
-    const float* weight;
-    const uint8_t* delay;
+// Advance the period's first step once all its launches are enqueued before it.
+__global__ void k_advance(unsigned long long* base, int steps) { *base += (unsigned long long)steps; }
+
+struct PullArgs {
     const int64_t* col_ptr;
     const uint32_t* csc_src;
     const float* csc_w;
     const uint8_t* csc_d;
-    const uint8_t* is_inh;
     const uint32_t* bitmap;
     float* ring;
-    int* list;
-    int* counts;
-    unsigned long long* step;
-    unsigned long long* total;
-    unsigned long long* rcount;
-    int2* raster;
-    long long rcap;
-    unsigned int* ticket;
+    const unsigned long long* base;
+    int q;
     int n, n_pad, D, words;
 };
-
-// Bookkeeping once every block of the delivery kernel has read the step
-// counter: advance it, clear the next step's spike count, accumulate totals.
-__device__ __forceinline__ void deliver_finish(const DelivArgs& a, uint64_t t, int cnt, unsigned long long rbase)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(a.ticket, 1u) == gridDim.x - 1) {
-            __threadfence();
-            *a.step = t + 1;
-            a.counts[(t + 1) & 1] = 0;
-            *a.total += (unsigned long long)cnt;
-            if (a.raster) {
-                unsigned long long r = rbase + (unsigned long long)cnt;
-                *a.rcount = r > (unsigned long long)a.rcap ? (unsigned long long)a.rcap : r;
-            }
-            *a.ticket = 0;
-        }
-    }
-}
-
-__device__ __forceinline__ void record_raster(const DelivArgs& a, uint64_t t, unsigned long long rbase, int f, int j)
-{
-    const unsigned long long r = rbase + (unsigned long long)f;
-    if (a.raster && r < (unsigned long long)a.rcap) a.raster[r] = make_int2((int)t, j);
-}
-
-// Push: a warp per spiking neuron, lanes over its out-edges; red.global.add
-// into ring slot (t + delay) % D, channel = the source's type.
-__global__ void __launch_bounds__(DELIV_THREADS) k_deliver_push(DelivArgs a)
-{
-    const uint64_t t = *a.step;
-    const int cnt = a.counts[t & 1];
-    const int* list = a.list + (size_t)(t & 1) * a.n_pad;
-    const int s0 = (int)(t % (uint64_t)a.D);
-    const unsigned long long rbase = a.raster ? *a.rcount : 0ull;
-    const int lane = threadIdx.x & 31;
-    const int nwarps = gridDim.x * (DELIV_THREADS / 32);
-    for (int f = blockIdx.x * (DELIV_THREADS / 32) + (threadIdx.x >> 5); f < cnt; f += nwarps) {
-        const int j = list[f];
-        const int ch = a.is_inh[j] ? 1 : 0;
-        const int64_t beg = a.row_ptr[j], end = a.row_ptr[j + 1];
-        for (int64_t e = beg + lane; e < end; e += 32) {
-            const int k = a.col[e];
-            int sl = s0 + (int)a.delay[e];
-            if (sl >= a.D) sl -= a.D;
-            atomicAdd(a.ring + 2 * ((size_t)sl * a.n_pad + k) + ch, a.weight[e]);
-        }
-        if (lane == 0) record_raster(a, t, rbase, f, j);
-    }
-    deliver_finish(a, t, cnt, rbase);
-}
 
 // Pull: a warp per postsynaptic neuron sums its CSC column against the spike
 // bitmap of step t + 1 - delay and writes the complete input of step t + 1.
 // Deterministic: the column order and the warp reduction order are fixed.
-__global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(DelivArgs a)
+__global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
 {
-    const uint64_t t = *a.step;
-    const int cnt = a.counts[t & 1];
-    const int* list = a.list + (size_t)(t & 1) * a.n_pad;
+    const uint64_t t = *a.base + (uint64_t)a.q;
     const int s1 = (int)((t + 1) % (uint64_t)a.D);
-    const unsigned long long rbase = a.raster ? *a.rcount : 0ull;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * (DELIV_THREADS / 32) + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * (DELIV_THREADS / 32);
@@ -350,9 +339,6 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(DelivArgs a)
         acc_i = nn_warp_sumf(acc_i);
         if (lane == 0) reinterpret_cast<float2*>(out)[k] = make_float2(acc_e, acc_i);
     }
-    for (int f = gw; f < cnt; f += nwarps)
-        if (lane == 0) record_raster(a, t, rbase, f, list[f]);
-    deliver_finish(a, t, cnt, rbase);
 }
 
 // paracrine: b = u + src ; src = 0
@@ -630,7 +616,7 @@ extern "C" void nn_net_spec_default(nn_net_spec* sp, int kind)
     sp->block_dmax = 40;
 }
 
-static StepArgs step_args(nn_sim* s)
+static StepArgs step_args(nn_sim* s, int q)
 {
     StepArgs a;
     a.V = s->f[NN_F_V]; a.m = s->f[NN_F_M]; a.h = s->f[NN_F_H]; a.nn = s->f[NN_F_N];
@@ -642,33 +628,36 @@ static StepArgs step_args(nn_sim* s)
     a.bitmap = s->bitmap;
     a.list = s->list;
     a.counts = s->counts;
-    a.step = s->step;
+    a.base = s->step;
+    a.q = q;
+    const bool push = s->cfg.delivery == NN_DELIVERY_PUSH;
+    a.row_ptr = push ? s->row_ptr : nullptr;
+    a.col = s->col;
+    a.weight = s->weight;
+    a.delay = s->delay;
+    a.is_inh = s->is_inh;
+    a.total = s->total;
+    a.rcount = s->rcount;
+    a.raster = s->raster;
+    a.rcap = s->cfg.raster_capacity;
     a.vox = s->vox;
     a.src = s->grid > 0 ? s->src : nullptr;
     a.err = s->err;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
-    a.zero_ring = s->cfg.delivery == NN_DELIVERY_PUSH;
+    a.zero_ring = push;
     a.seed = s->cfg.seed;
     a.p = nn_hh_to_dev(s->cfg.hp);
     return a;
 }
 
-static DelivArgs deliv_args(nn_sim* s)
+static PullArgs pull_args(nn_sim* s, int q)
 {
-    DelivArgs a;
-    a.row_ptr = s->row_ptr; a.col = s->col; a.weight = s->weight; a.delay = s->delay;
+    PullArgs a;
     a.col_ptr = s->col_ptr; a.csc_src = s->csc_src; a.csc_w = s->csc_w; a.csc_d = s->csc_d;
-    a.is_inh = s->is_inh;
     a.bitmap = s->bitmap;
     a.ring = reinterpret_cast<float*>(s->ring);
-    a.list = s->list;
-    a.counts = s->counts;
-    a.step = s->step;
-    a.total = s->total;
-    a.rcount = s->rcount;
-    a.raster = s->raster;
-    a.rcap = s->cfg.raster_capacity;
-    a.ticket = s->ticket;
+    a.base = s->step;
+    a.q = q;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
     return a;
 }
@@ -717,7 +706,6 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
     if (st == NN_OK) st = nn_alloc(ctx, &s->total, 1);
     if (st == NN_OK) st = nn_alloc(ctx, &s->rcount, 1);
     if (st == NN_OK && cfg->raster_capacity > 0) st = nn_alloc(ctx, &s->raster, (size_t)cfg->raster_capacity);
-    if (st == NN_OK) st = nn_alloc(ctx, &s->ticket, 1);
     if (st == NN_OK) st = nn_alloc(ctx, &s->err, 1);
     if (st == NN_OK) st = nn_alloc(ctx, &s->is_inh, NP);
     if (st == NN_OK && s->grid > 0) {
@@ -747,7 +735,6 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
     cudaMemsetAsync(s->step, 0, sizeof(unsigned long long), cs);
     cudaMemsetAsync(s->total, 0, sizeof(unsigned long long), cs);
     cudaMemsetAsync(s->rcount, 0, sizeof(unsigned long long), cs);
-    cudaMemsetAsync(s->ticket, 0, sizeof(unsigned int), cs);
     cudaMemsetAsync(s->err, 0, sizeof(int), cs);
     cudaMemsetAsync(s->is_inh, 0, NP, cs);
     if (s->grid > 0) {
@@ -778,7 +765,7 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     drop_graph(s);
     for (int q = 0; q < NN_F_COUNT; ++q) nn_release(s->f[q]);
     nn_release(s->ring); nn_release(s->bitmap); nn_release(s->list); nn_release(s->counts); nn_release(s->step);
-    nn_release(s->total); nn_release(s->rcount); nn_release(s->raster); nn_release(s->ticket); nn_release(s->err);
+    nn_release(s->total); nn_release(s->rcount); nn_release(s->raster); nn_release(s->err);
     nn_release(s->is_inh); nn_release(s->vox); nn_release(s->src); nn_release(s->u); nn_release(s->b);
     free_network(s);
     if (s->pcg) nn_pcg_destroy(s->pcg);
@@ -1123,7 +1110,7 @@ extern "C" nn_status nn_sim_init_state(nn_sim* s, float v0, float i_lo, float i_
     const double am = xr((V + 40.0) / 10.0), bm = 4.0 * std::exp(-(V + 65.0) / 18.0);
     const double ah = 0.07 * std::exp(-(V + 65.0) / 20.0), bh = 1.0 / (1.0 + std::exp(-(V + 35.0) / 10.0));
     const double an = 0.1 * xr((V + 55.0) / 10.0), bn = 0.125 * std::exp(-(V + 65.0) / 80.0);
-    StepArgs a = step_args(s);
+    StepArgs a = step_args(s, 0);
     const int L = nn_lattice_side(s->n);
     k_init_state<<<nn_grid_for(ctx, s->n_pad, 256, 16), 256, 0, ctx->stream>>>(
         a, v0, (float)(am / (am + bm)), (float)(ah / (ah + bh)), (float)(an / (an + bn)), i_lo, i_hi, s->f[NN_F_X],
@@ -1133,14 +1120,16 @@ extern "C" nn_status nn_sim_init_state(nn_sim* s, float v0, float i_lo, float i_
     return NN_OK;
 }
 
-// Enqueue one step (two kernels).
-static nn_status enqueue_step(nn_sim* s, int q)
+// Enqueue one step: the neuron update (with push delivery inline), plus the
+// pull gather in pull mode.  qk: the step's offset from the device step base;
+// qe: its timing-event slot.
+static nn_status enqueue_step(nn_sim* s, int qk, int qe)
 {
     nn_ctx* ctx = s->ctx;
     cudaStream_t cs = ctx->stream;
-    const bool tm = s->timing && q >= 0 && q < (int)s->ev_a.size();
-    if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_a[q], cs, cudaEventRecordExternal));
-    StepArgs a = step_args(s);
+    const bool tm = s->timing && qe >= 0 && qe < (int)s->ev_a.size();
+    if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_a[qe], cs, cudaEventRecordExternal));
+    StepArgs a = step_args(s, qk);
     const int warps_needed = s->n_pad / (32 * s->npt);
     const int blocks = std::max(1, std::min((warps_needed * 32 + s->tpb - 1) / s->tpb, ctx->num_sms * 16));
     switch (s->npt) {
@@ -1149,19 +1138,25 @@ static nn_status enqueue_step(nn_sim* s, int q)
         default: k_hh_step<4><<<blocks, s->tpb, 0, cs>>>(a); break;
     }
     NN_CHECK_LAUNCH(ctx, "k_hh_step");
-    if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_b[q], cs, cudaEventRecordExternal));
-    DelivArgs d = deliv_args(s);
+    if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_b[qe], cs, cudaEventRecordExternal));
     if (s->cfg.delivery == NN_DELIVERY_PULL) {
+        PullArgs d = pull_args(s, qk);
         k_deliver_pull<<<nn_grid_for(ctx, (int64_t)s->n * 32, DELIV_THREADS, 8), DELIV_THREADS, 0, cs>>>(d);
         NN_CHECK_LAUNCH(ctx, "k_deliver_pull");
-    } else {
-        k_deliver_push<<<ctx->num_sms * 2, DELIV_THREADS, 0, cs>>>(d);
-        NN_CHECK_LAUNCH(ctx, "k_deliver_push");
     }
     if (tm) {
-        NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_c[q], cs, cudaEventRecordExternal));
-        s->ev_valid[q] = 1;
+        NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_c[qe], cs, cudaEventRecordExternal));
+        s->ev_valid[qe] = 1;
     }
+    return NN_OK;
+}
+
+static int launches_per_step(const nn_sim* s) { return s->cfg.delivery == NN_DELIVERY_PULL ? 2 : 1; }
+
+static nn_status enqueue_advance(nn_sim* s, int steps)
+{
+    k_advance<<<1, 1, 0, s->ctx->stream>>>(s->step, steps);
+    NN_CHECK_LAUNCH(s->ctx, "k_advance");
     return NN_OK;
 }
 
@@ -1245,7 +1240,8 @@ static nn_status ensure_graph(nn_sim* s)
     const int64_t launches0 = ctx->launches;
     NN_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     nn_status st = NN_OK;
-    for (int q = 0; q < P && st == NN_OK; ++q) st = enqueue_step(s, q);
+    for (int q = 0; q < P && st == NN_OK; ++q) st = enqueue_step(s, q, q);
+    if (st == NN_OK) st = enqueue_advance(s, P);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(cs, &g);
     ctx->launches = launches0;
@@ -1276,11 +1272,12 @@ extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
         if (aligned && left >= P) {
             NN_TRY(ensure_graph(s));
             NN_CUDA(ctx, cudaGraphLaunch(s->graph, ctx->stream));
-            ctx->launches += 2 * (int64_t)P;
+            ctx->launches += (int64_t)launches_per_step(s) * P + 1;
             s->host_step += P;
             left -= P;
         } else {
-            NN_TRY(enqueue_step(s, (int)(s->host_step % P)));
+            NN_TRY(enqueue_step(s, 0, (int)(s->host_step % P)));
+            NN_TRY(enqueue_advance(s, 1));
             s->host_step += 1;
             left -= 1;
         }

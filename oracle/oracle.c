@@ -58,12 +58,13 @@ static inline double u01_open_closed(uint32_t x) { return (double)((x >> 8) + 1u
 
 double orc_normal_ctr(uint64_t seed, uint32_t i, uint64_t step, uint32_t purpose)
 {
+    /* one draw per neuron pair (i>>1): cos branch for even i, sin for odd i */
     uint32_t r[4];
-    philox(seed, i, (uint32_t)(step >> 1), (uint32_t)(step >> 33), purpose, r);
+    philox(seed, i >> 1, (uint32_t)step, (uint32_t)(step >> 32), purpose, r);
     double u1 = u01_open_closed(r[0]);
     double u2 = u01_closed_open(r[1]);
     double rad = sqrt(-2.0 * log(u1));
-    return (step & 1u) ? rad * sin(2.0 * M_PI * u2) : rad * cos(2.0 * M_PI * u2);
+    return (i & 1u) ? rad * sin(2.0 * M_PI * u2) : rad * cos(2.0 * M_PI * u2);
 }
 
 uint32_t orc_minstd_next(uint32_t* state)

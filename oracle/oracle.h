@@ -47,8 +47,9 @@ extern "C" {
 /* ------------------------------------------------------------------ RNG -- */
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11). */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
-/* Standard normal from the counter (i, step>>1, step>>33, purpose): Box-Muller,
- * cos branch for even step, sin branch for odd step. */
+/* Standard normal of neuron i at a step: one Philox draw per neuron pair,
+ * counter (i>>1, step, step>>32, purpose), Box-Muller with the cos branch for
+ * even i and the sin branch for odd i. */
 double orc_normal_ctr(uint64_t seed, uint32_t i, uint64_t step, uint32_t purpose);
 
 /* std::minstd_rand0 (libstdc++ std::default_random_engine): x <- 16807 x mod (2^31-1). */
