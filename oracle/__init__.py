@@ -36,7 +36,7 @@ class OrcSim(C.Structure):
     _fields_ = [("hp", OrcHHParams), ("n", C.c_int), ("D", C.c_int), ("net", P(OrcCSR)),
                 ("is_inh", C.c_void_p), ("i_drive", C.c_void_p), ("gna_scale", C.c_void_p),
                 ("u_par", C.c_void_p), ("seed", C.c_uint64), ("y", C.c_void_p), ("ring", C.c_void_p),
-                ("vox", C.c_void_p), ("src", C.c_void_p)]
+                ("vox", C.c_void_p), ("src", C.c_void_p), ("margin", C.c_void_p)]
 
 
 V = C.c_void_p
@@ -271,17 +271,22 @@ class Sim:
         self.ring = np.zeros(2 * D * self.n, np.float64)
         self.vox = None if vox is None else np.ascontiguousarray(vox, np.int32)
         self.src = np.zeros(grid_cells, np.float64) if grid_cells else None
+        self._margin = np.zeros(self.n, np.float64)
         self.s = OrcSim(self.hp, self.n, D, C.pointer(net.s), self.is_inh.ctypes.data, self.i_drive.ctypes.data,
                         None if self.gna is None else self.gna.ctypes.data, None, seed, self.y.ctypes.data,
                         self.ring.ctypes.data, None if self.vox is None else self.vox.ctypes.data,
-                        None if self.src is None else self.src.ctypes.data)
+                        None if self.src is None else self.src.ctypes.data, self._margin.ctypes.data)
         self.t = 0
         self._spk = np.zeros(self.n, np.int32)
+        self.margins: dict[tuple[int, int], float] = {}  # (step, neuron) -> threshold-crossing margin (mV)
 
     def step(self) -> np.ndarray:
         ns = lib().orc_sim_step(C.byref(self.s), self.t, ptr(self._spk))
+        spk = self._spk[:ns].copy()
+        for j in spk:
+            self.margins[(self.t, int(j))] = float(self._margin[j])
         self.t += 1
-        return self._spk[:ns].copy()
+        return spk
 
     def state(self) -> np.ndarray:
         return self.y.T.copy()  # (6, n): V, m, h, n, ge, gi

@@ -591,6 +591,10 @@ int orc_sim_step(orc_sim* s, uint64_t step, int32_t* spikes)
         const double v_old = y[0];
         orc_hh_rk4(hp, gs, iext, up, y);
         spikes[i] = (v_old < hp->v_thresh && y[0] >= hp->v_thresh) ? 1 : 0;
+        if (spikes[i] && s->margin) {
+            const double a = hp->v_thresh - v_old, b = y[0] - hp->v_thresh;
+            s->margin[i] = a < b ? a : b;
+        }
     }
     for (int i = 0; i < n; ++i)
         if (spikes[i]) spikes[ns++] = i;

