@@ -332,4 +332,27 @@ NN_API nn_status nn_pcg_apply(nn_pcg* pc, const float* d_x, float* d_y);
 NN_API nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter,
                               int* iters, double* relres);
 
+/* No counterpart in the reference.  The same solve as nn_pcg_create +
+ * nn_pcg_solve + nn_pcg_destroy for callers that may not allocate device
+ * memory: a host framework that owns the GPU's memory budget and forbids
+ * allocations by the code it calls, or a real-time loop that cannot take the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  It allocates nothing:
+ * its work vectors and reduction scratch live in one fixed device array of
+ * about 5.4 MB that every GPU loading this library holds until the process
+ * exits.  The caller passes the inputs (d_Dcell may be NULL, d_b) and the
+ * output d_x (initial guess in, solution out), all device pointers, and the
+ * cudaStream_t to run on (NULL = the legacy default stream).
+ * Limit: nx*ny*nz <= NN_PCG_NOALLOC_MAX_CELLS (64^3); larger grids return
+ * NN_ERR_UNSUPPORTED without launching anything.  Returns NN_ERR_NOT_CONVERGED
+ * if rtol is not reached in max_iter iterations.
+ * The first call on a device looks up the scratch's device address (which
+ * also loads the library's kernels on that device): make that first call
+ * before any stream capture.  All calls share the one scratch, so calls whose
+ * work overlaps on the GPU (different streams, threads or processes' streams
+ * of this library instance) race; serialise them. */
+#define NN_PCG_NOALLOC_MAX_CELLS (64 * 64 * 64)
+NN_API nn_status nn_pcg_solve_noalloc(void* stream, int nx, int ny, int nz, double alpha, double beta,
+                                      const float* d_Dcell, const float* d_b, float* d_x, double rtol,
+                                      int max_iter, int* iters, double* relres);
+
 #endif

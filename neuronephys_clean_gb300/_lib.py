@@ -130,6 +130,8 @@ _SIGS = {
     "nn_pcg_destroy": (c_int, [c_void_p]),
     "nn_pcg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
     "nn_pcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
+    "nn_pcg_solve_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_double, c_void_p, c_void_p,
+                                     c_void_p, c_double, c_int, P(c_int), P(c_double)]),
 }
 
 _lib = None

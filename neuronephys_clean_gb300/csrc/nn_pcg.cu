@@ -14,7 +14,9 @@
 // p is double-buffered because the direction update reads neighbours.
 // Products are accumulated in FP32 within a thread's strip of cells and in
 // FP64 from the warp level up.
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "nn_internal.cuh"
 
@@ -459,4 +461,108 @@ extern "C" nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, doub
     NN_TRY(nn_pcg_run(pc, d_b, d_x, rtol, max_iter, iters, relres, &conv));
     if (!conv) return nn_fail(pc->ctx, NN_ERR_NOT_CONVERGED, "PCG did not reach rtol %g in %d iterations", rtol, max_iter);
     return NN_OK;
+}
+
+// ========================================================= no allocation ==
+// nn_pcg_solve_noalloc: the same Jacobi-PCG as nn_pcg_create + nn_pcg_solve,
+// for callers that may not allocate device memory (a host framework that owns
+// the GPU's memory budget, or a real-time loop that cannot take the device-wide
+// synchronisation of cudaMalloc/cudaFree).  Its work vectors, reduction
+// partials and flags live in the fixed file-scope array below, which every GPU
+// that loads this library holds until the process exits.  One scratch serves
+// all calls on a device, so calls whose work overlaps on the GPU race.
+
+namespace {
+constexpr size_t NA_ALIGN(size_t b) { return (b + 255) & ~(size_t)255; }
+constexpr int NA_MAX_BLOCKS = 4096;  // reduction partials: grid-stride blocks per kernel
+constexpr size_t NA_VEC = NA_ALIGN((size_t)NN_PCG_NOALLOC_MAX_CELLS * sizeof(float));
+constexpr size_t NA_OFF_R = 0, NA_OFF_P0 = NA_VEC, NA_OFF_P1 = 2 * NA_VEC, NA_OFF_AP = 3 * NA_VEC,
+                 NA_OFF_INVD = 4 * NA_VEC, NA_OFF_SCAL = 5 * NA_VEC;
+constexpr size_t NA_OFF_PART = NA_OFF_SCAL + NA_ALIGN(S_COUNT * sizeof(double));
+constexpr size_t NA_OFF_TICKET = NA_OFF_PART + NA_ALIGN(3 * (size_t)NA_MAX_BLOCKS * sizeof(double));
+constexpr size_t NA_OFF_FLAGS = NA_OFF_TICKET + 256;
+constexpr size_t NA_BYTES = NA_OFF_FLAGS + 256;
+constexpr int NA_MAX_DEVICES = 64;
+}  // namespace
+
+// Host code sees this name as a host-side stand-in; the device address comes
+// from cudaGetSymbolAddress (see noalloc_scratch below).
+static __device__ __align__(256) unsigned char g_pcg_noalloc_scratch[NA_BYTES];
+
+// Device address of the scratch on the current device, looked up once per
+// device (the first call on a device does this, which also loads the module on
+// that device; make that first call before any stream capture).
+static nn_status noalloc_scratch(int dev, unsigned char** out)
+{
+    static std::mutex mu;
+    static unsigned char* addr[NA_MAX_DEVICES] = {};
+    if (dev < 0 || dev >= NA_MAX_DEVICES) return NN_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return NN_ERR_CUDA;
+        }
+        addr[dev] = (unsigned char*)p;
+    }
+    *out = addr[dev];
+    return NN_OK;
+}
+
+extern "C" nn_status nn_pcg_solve_noalloc(void* stream, int nx, int ny, int nz, double alpha, double beta,
+                                          const float* d_Dcell, const float* d_b, float* d_x, double rtol,
+                                          int max_iter, int* iters, double* relres)
+{
+    if (nx < 1 || ny < 1 || nz < 1 || !d_b || !d_x || !(alpha >= 0.0) || !(beta > -1.0) || !(rtol > 0.0) ||
+        max_iter < 0)
+        return NN_ERR_INVALID_ARG;
+    const int64_t G = (int64_t)nx * ny * nz;
+    if (G > (int64_t)NN_PCG_NOALLOC_MAX_CELLS) return NN_ERR_UNSUPPORTED;  // larger than the fixed scratch
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return NN_ERR_NO_DEVICE;
+    }
+    unsigned char* base = nullptr;
+    NN_TRY(noalloc_scratch(dev, &base));
+    // A context on the caller's stream that owns nothing.
+    nn_ctx ctx;
+    ctx.device = dev;
+    ctx.stream = (cudaStream_t)stream;
+    if (cudaDeviceGetAttribute(&ctx.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return NN_ERR_CUDA;
+    }
+    nn_pcg pc;
+    pc.ctx = &ctx;
+    pc.nx = nx; pc.ny = ny; pc.nz = nz;
+    pc.G = G;
+    pc.alpha = alpha;
+    pc.beta = beta;
+    pc.Dcell = d_Dcell;
+    pc.inv_diag_const = (float)(1.0 / (1.0 + beta + 6.0 * alpha));
+    pc.nblocks = std::min(nn_grid_for(&ctx, G, PCG_THREADS, 8), NA_MAX_BLOCKS);
+    pc.r = (float*)(base + NA_OFF_R);
+    pc.p0 = (float*)(base + NA_OFF_P0);
+    pc.p1 = (float*)(base + NA_OFF_P1);
+    pc.Ap = (float*)(base + NA_OFF_AP);
+    pc.invd = d_Dcell ? (float*)(base + NA_OFF_INVD) : nullptr;
+    pc.scal = (double*)(base + NA_OFF_SCAL);
+    pc.partials = (double*)(base + NA_OFF_PART);
+    pc.ticket = (unsigned int*)(base + NA_OFF_TICKET);
+    pc.flags = (int*)(base + NA_OFF_FLAGS);
+    // what must start at zero: the arrival ticket and the first direction
+    // buffer (the first update multiplies it by beta = 0)
+    NN_CUDA(&ctx, cudaMemsetAsync(pc.ticket, 0, sizeof(unsigned int), ctx.stream));
+    NN_CUDA(&ctx, cudaMemsetAsync(pc.p0, 0, sizeof(float) * (size_t)G, ctx.stream));
+    if (d_Dcell) {
+        Op o = make_op(&pc);
+        k_pcg_invdiag<<<pc.nblocks, PCG_THREADS, 0, ctx.stream>>>(o, pc.invd);
+        NN_CHECK_LAUNCH(&ctx, "k_pcg_invdiag");
+    }
+    int conv = 0;
+    NN_TRY(nn_pcg_run(&pc, d_b, d_x, rtol, max_iter, iters, relres, &conv));
+    return conv ? NN_OK : NN_ERR_NOT_CONVERGED;
 }
