@@ -1,0 +1,558 @@
+// Single-kernel-per-iteration preconditioned CG (Chronopoulos & Gear, "s-step
+// iterative methods for symmetric linear systems", J. Comput. Appl. Math. 25,
+// 1989) for the constant-coefficient 7-point backward-Euler operator
+//   A = (1 + beta) I + alpha L,   L the 7-point Laplacian with zero values
+// outside the grid (homogeneous Dirichlet), Jacobi preconditioner M = 1/diag.
+//
+// The recurrences need one grid-wide reduction per iteration:
+//   p_i = u_i + b_i p_{i-1}        s_i = w_i + b_i s_{i-1}      (s = A p)
+//   x  += a_i p_i                  r  -= a_i s_i
+//   u   = M r                      w   = A u
+//   g = (r, u), d = (w, u), rho = (r, r)   -> one reduction
+//   b_{i+1} = g / g_old,  a_{i+1} = g / (d - b_{i+1} g / a_i)
+// One kernel does all of it: a block owns a 32 x 8 x 16 tile and marches in
+// z; planes of r, w and s (with a one-cell halo, the TMA box starting 16-byte
+// aligned at x0 - 4) are staged into shared memory by cp.async.bulk.tensor
+// through a 4-deep mbarrier pipeline; out-of-range boxes are zero-filled by
+// the TMA unit, which is exactly the Dirichlet boundary.  u = M r_new is formed
+// for the tile plus halo in a 3-plane ring, w = A u for the plane behind it.
+// r, w and s are double-buffered (the next iteration reads the halo of cells
+// other blocks write); p and x are updated in place.  The last block to finish
+// sums the block partials in FP64 and forms the next iteration's scalars, so
+// no host round trip separates iterations.  Every mbarrier wait is bounded.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+
+#include "nn_internal.cuh"
+
+namespace {
+constexpr int CG_THREADS = 256;
+constexpr int TX = 32, TY = 8, ZC = 16;
+constexpr int BXW = 40, BYW = 10;            // TMA box: x from x0 - 4, y from y0 - 1
+constexpr int RX = TX + 2, RY = TY + 2;      // u region (tile + halo)
+constexpr int PLANE_BYTES = BXW * BYW * 4;   // 1600
+constexpr int PLANE_STRIDE = 1664;           // 128-byte multiple
+constexpr int NARR = 3;                      // r, w, s
+constexpr int STAGES = 4;
+constexpr int STAGE_BYTES = NARR * PLANE_STRIDE;
+constexpr int U_BYTES = 3 * RY * RX * 4;
+constexpr int SMEM_BYTES = 128 + STAGES * STAGE_BYTES + U_BYTES + STAGES * 8 + 64;
+constexpr uint32_t WAIT_LIMIT = 1u << 20;
+constexpr int HALO_CELLS = 2 * RX + 2 * TY;  // 84
+
+enum { C_GAMMA = 0, C_ALPHA, C_BETA, C_RR, C_BB, C_DELTA, C_COUNT };
+
+struct CgArgs {
+    int nx, ny, nz;
+    float op_alpha, onepb, invd;
+    float* p;
+    float* x;
+    float* r_out;
+    float* w_out;
+    float* s_out;
+    double* scal;
+    double* partials;
+    unsigned int* ticket;
+    int* flags;  // [0] stop (1 converged, 2 max_iter, 3 error) [1] iterations [2] wait timeout
+    double rtol2;
+    int max_iter;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
+{
+    const uint32_t addr = smem_u32(bar);
+    for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_plane(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ float warp_sumf(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block partials of nsum values (FP32 per thread and warp, FP64 across warps
+// and blocks); the last block to arrive writes the grid totals to out[].
+__device__ bool cg_reduce(int nsum, const float* v, double* partials, unsigned int* ticket, double* out)
+{
+    __shared__ double ws[3][CG_THREADS / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = 0; q < nsum; ++q) {
+        const float s = warp_sumf(v[q]);
+        if (lane == 0) ws[q][w] = (double)s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < nsum; ++q) {
+            double s = 0.0;
+            for (int u = 0; u < CG_THREADS / 32; ++u) s += ws[q][u];
+            partials[(size_t)q * gridDim.x + blockIdx.x] = s;
+        }
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    for (int q = 0; q < nsum; ++q) {
+        const volatile double* pp = partials + (size_t)q * gridDim.x;
+        double s = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += CG_THREADS) s += pp[b];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        __syncthreads();
+        if (lane == 0) ws[q][w] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int u = 0; u < CG_THREADS / 32; ++u) t += ws[q][u];
+            out[q] = t;
+        }
+    }
+    if (threadIdx.x == 0) *ticket = 0;
+    __syncthreads();
+    return true;
+}
+
+// r0 = b - A x0 (neighbour loads; once per solve); bb = (b, b)
+__global__ void __launch_bounds__(CG_THREADS) k_cg_init_r(CgArgs a, const float* b, const float* x, float* r)
+{
+    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, G = sz * a.nz;
+    float bb = 0.0f;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < G; c += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % a.nx), j = (int)((c / a.nx) % a.ny), k = (int)(c / sz);
+        const float xc = x[c];
+        float nb = 0.0f;
+        nb += i > 0 ? x[c - 1] : 0.0f;
+        nb += i < a.nx - 1 ? x[c + 1] : 0.0f;
+        nb += j > 0 ? x[c - sy] : 0.0f;
+        nb += j < a.ny - 1 ? x[c + sy] : 0.0f;
+        nb += k > 0 ? x[c - sz] : 0.0f;
+        nb += k < a.nz - 1 ? x[c + sz] : 0.0f;
+        const float ax = (a.onepb + 6.0f * a.op_alpha) * xc - a.op_alpha * nb;
+        const float bv = b[c];
+        r[c] = bv - ax;
+        bb += bv * bv;
+    }
+    float v[1] = {bb};
+    double out[1];
+    if (cg_reduce(1, v, a.partials, a.ticket, out) && threadIdx.x == 0) a.scal[C_BB] = out[0];
+}
+
+// w0 = A (M r0), p = 0, s = 0; g0, d0, rho0 -> a0, b0 = 0
+__global__ void __launch_bounds__(CG_THREADS) k_cg_init_w(CgArgs a, const float* r, float* w, float* s)
+{
+    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, G = sz * a.nz;
+    float g = 0.0f, d = 0.0f, rr = 0.0f;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < G; c += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c % a.nx), j = (int)((c / a.nx) % a.ny), k = (int)(c / sz);
+        const float rc = r[c];
+        float nb = 0.0f;
+        nb += i > 0 ? r[c - 1] : 0.0f;
+        nb += i < a.nx - 1 ? r[c + 1] : 0.0f;
+        nb += j > 0 ? r[c - sy] : 0.0f;
+        nb += j < a.ny - 1 ? r[c + sy] : 0.0f;
+        nb += k > 0 ? r[c - sz] : 0.0f;
+        nb += k < a.nz - 1 ? r[c + sz] : 0.0f;
+        const float uc = a.invd * rc;
+        const float wc = a.invd * ((a.onepb + 6.0f * a.op_alpha) * rc - a.op_alpha * nb);
+        w[c] = wc;
+        s[c] = 0.0f;
+        a.p[c] = 0.0f;
+        g += rc * uc;
+        d += wc * uc;
+        rr += rc * rc;
+    }
+    float v[3] = {g, d, rr};
+    double out[3];
+    if (cg_reduce(3, v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+        a.scal[C_GAMMA] = out[0];
+        a.scal[C_DELTA] = out[1];
+        a.scal[C_RR] = out[2];
+        a.scal[C_ALPHA] = out[1] != 0.0 ? out[0] / out[1] : 0.0;
+        a.scal[C_BETA] = 0.0;
+        a.flags[1] = 0;
+        a.flags[2] = 0;
+        a.flags[0] = (out[2] <= a.rtol2 * a.scal[C_BB]) ? 1 : 0;
+    }
+}
+
+// One CG iteration (see the file comment).  One tile per block.
+__global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ CUtensorMap tm_r,
+                                                        const __grid_constant__ CUtensorMap tm_w,
+                                                        const __grid_constant__ CUtensorMap tm_s, CgArgs a)
+{
+    if (a.flags[0]) return;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+    unsigned char* stage_base = smem;
+    float* U = (float*)(smem + STAGES * STAGE_BYTES);  // [3][RY][RX]
+    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + U_BYTES);
+    __shared__ int abort_flag;
+
+    const int tid = threadIdx.x;
+    const int tiles_x = (a.nx + TX - 1) / TX, tiles_y = (a.ny + TY - 1) / TY;
+    const int tx = blockIdx.x % tiles_x;
+    const int ty = (blockIdx.x / tiles_x) % tiles_y;
+    const int tz = blockIdx.x / (tiles_x * tiles_y);
+    const int x0 = tx * TX, y0 = ty * TY, z0 = tz * ZC;
+    const int z1 = min(z0 + ZC, a.nz);
+    const int np = z1 - z0 + 2;  // planes z0-1 .. z1
+    const float alpha = (float)a.scal[C_ALPHA], beta = (float)a.scal[C_BETA];
+    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny;
+
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int q = 0; q < STAGES; ++q) mbar_init(&bars[q], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int j = 0; j < STAGES && j < np; ++j) {
+            unsigned char* st = stage_base + j * STAGE_BYTES;
+            mbar_expect_tx(&bars[j], NARR * PLANE_BYTES);
+            tma_load_plane(st, &tm_r, x0 - 4, y0 - 1, z0 - 1 + j, &bars[j]);
+            tma_load_plane(st + PLANE_STRIDE, &tm_w, x0 - 4, y0 - 1, z0 - 1 + j, &bars[j]);
+            tma_load_plane(st + 2 * PLANE_STRIDE, &tm_s, x0 - 4, y0 - 1, z0 - 1 + j, &bars[j]);
+        }
+    }
+
+    // interior cell of this thread
+    const int ix = tid & 31, iy = tid >> 5;
+    const int gx = x0 + ix, gy = y0 + iy;
+    const bool col_in = gx < a.nx && gy < a.ny;
+    float acc_g = 0.0f, acc_r = 0.0f, acc_d = 0.0f;
+
+    for (int j = 0; j < np; ++j) {
+        const int k = z0 - 1 + j;
+        const int sidx = j % STAGES;
+        const bool ok = mbar_wait(&bars[sidx], (uint32_t)((j / STAGES) & 1));
+        if (!ok) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) break;
+        const float* R = (const float*)(stage_base + sidx * STAGE_BYTES);
+        const float* W = (const float*)(stage_base + sidx * STAGE_BYTES + PLANE_STRIDE);
+        const float* S = (const float*)(stage_base + sidx * STAGE_BYTES + 2 * PLANE_STRIDE);
+        float* Uk = U + (j % 3) * RY * RX;
+        const bool plane_in = k >= 0 && k < a.nz;
+        // interior cells: s, r, u and the pointwise p, x updates for owned planes
+        {
+            const int bx = ix + 4, by = iy + 1;
+            const float sv = W[by * BXW + bx] + beta * S[by * BXW + bx];
+            const float rv_old = R[by * BXW + bx];
+            const float rv = rv_old - alpha * sv;
+            const bool in = col_in && plane_in;
+            const float uv = in ? a.invd * rv : 0.0f;
+            Uk[by * RX + bx - 3] = uv;
+            if (in && k >= z0 && k < z1) {
+                const int64_t c = gx + sy * gy + sz * k;
+                const float pv = a.invd * rv_old + beta * a.p[c];
+                a.p[c] = pv;
+                a.x[c] += alpha * pv;
+                a.s_out[c] = sv;
+                a.r_out[c] = rv;
+                acc_g += rv * uv;
+                acc_r += rv * rv;
+            }
+        }
+        // halo ring of the u region
+        if (tid < HALO_CELLS) {
+            int bx, by;
+            if (tid < RX) { bx = 3 + tid; by = 0; }
+            else if (tid < 2 * RX) { bx = 3 + tid - RX; by = RY - 1; }
+            else if (tid < 2 * RX + TY) { bx = 3; by = 1 + tid - 2 * RX; }
+            else { bx = 3 + RX - 1; by = 1 + tid - 2 * RX - TY; }
+            const int hx = x0 - 4 + bx, hy = y0 - 1 + by;
+            const bool in = plane_in && hx >= 0 && hx < a.nx && hy >= 0 && hy < a.ny;
+            const float sv = W[by * BXW + bx] + beta * S[by * BXW + bx];
+            const float rv = R[by * BXW + bx] - alpha * sv;
+            Uk[by * RX + bx - 3] = in ? a.invd * rv : 0.0f;
+        }
+        __syncthreads();
+        // refill this stage with the plane STAGES ahead
+        if (tid == 0 && j + STAGES < np) {
+            unsigned char* st = stage_base + sidx * STAGE_BYTES;
+            const int kz = z0 - 1 + j + STAGES;
+            mbar_expect_tx(&bars[sidx], NARR * PLANE_BYTES);
+            tma_load_plane(st, &tm_r, x0 - 4, y0 - 1, kz, &bars[sidx]);
+            tma_load_plane(st + PLANE_STRIDE, &tm_w, x0 - 4, y0 - 1, kz, &bars[sidx]);
+            tma_load_plane(st + 2 * PLANE_STRIDE, &tm_s, x0 - 4, y0 - 1, kz, &bars[sidx]);
+        }
+        // w = A u for the plane behind (k - 1), owned when j >= 2
+        if (j >= 2) {
+            const int kb = k - 1;
+            const float* Um = U + ((j - 2) % 3) * RY * RX;  // plane k - 2
+            const float* Uc = U + ((j - 1) % 3) * RY * RX;  // plane k - 1
+            const int bx = ix + 1, by = iy + 1;               // in u-region coordinates
+            if (col_in && kb < z1) {
+                const float uc = Uc[by * RX + bx];
+                const float nb = Uc[by * RX + bx - 1] + Uc[by * RX + bx + 1] + Uc[(by - 1) * RX + bx] +
+                                 Uc[(by + 1) * RX + bx] + Um[by * RX + bx] + Uk[by * RX + bx];
+                const float wv = (a.onepb + 6.0f * a.op_alpha) * uc - a.op_alpha * nb;
+                a.w_out[gx + sy * gy + sz * kb] = wv;
+                acc_d += wv * uc;
+            }
+        }
+        __syncthreads();
+    }
+    if (abort_flag) {
+        if (tid == 0) {
+            a.flags[2] = 1;
+            a.flags[0] = 3;
+        }
+        return;
+    }
+    float v[3] = {acc_g, acc_d, acc_r};
+    double out[3];
+    if (cg_reduce(3, v, a.partials, a.ticket, out) && threadIdx.x == 0) {
+        const double g = out[0], d = out[1], rr = out[2];
+        const int it = a.flags[1] + 1;
+        a.flags[1] = it;
+        a.scal[C_RR] = rr;
+        const double bnew = g / a.scal[C_GAMMA];
+        const double denom = d - bnew * g / a.scal[C_ALPHA];
+        a.scal[C_BETA] = bnew;
+        a.scal[C_ALPHA] = denom != 0.0 ? g / denom : 0.0;
+        a.scal[C_GAMMA] = g;
+        a.scal[C_DELTA] = d;
+        if (rr <= a.rtol2 * a.scal[C_BB]) a.flags[0] = 1;
+        else if (it >= a.max_iter) a.flags[0] = 2;
+        else if (!(std::isfinite(a.scal[C_ALPHA]) && std::isfinite(a.scal[C_BETA]))) a.flags[0] = 3;
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+bool make_map(CUtensorMap* m, float* base, int nx, int ny, int nz)
+{
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t gdim[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    cuuint64_t gstride[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    cuuint32_t box[3] = {BXW, BYW, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+}  // namespace
+
+// --------------------------------------------------------------- host side --
+
+struct nn_cg_plan {
+    nn_ctx* ctx = nullptr;
+    int nx = 0, ny = 0, nz = 0;
+    int64_t G = 0;
+    float op_alpha = 0, onepb = 0, invd = 0;
+    float *r[2] = {}, *w[2] = {}, *s[2] = {}, *p = nullptr;
+    CUtensorMap map_r[2], map_w[2], map_s[2];
+    double* scal = nullptr;
+    double* partials = nullptr;
+    unsigned int* ticket = nullptr;
+    int* flags = nullptr;
+    int tiles = 0, init_blocks = 0;
+    // timing of the iteration kernels
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_a, ev_b;
+    float last_ms = 0.0f;
+    int last_iters = 0;
+};
+
+void nn_cg_plan_destroy(nn_cg_plan* pl)
+{
+    if (!pl) return;
+    if (pl->ctx) cudaStreamSynchronize(pl->ctx->stream);
+    for (int q = 0; q < 2; ++q) {
+        nn_release(pl->r[q]);
+        nn_release(pl->w[q]);
+        nn_release(pl->s[q]);
+    }
+    nn_release(pl->p);
+    nn_release(pl->scal);
+    nn_release(pl->partials);
+    nn_release(pl->ticket);
+    nn_release(pl->flags);
+    for (auto e : pl->ev_a) cudaEventDestroy(e);
+    for (auto e : pl->ev_b) cudaEventDestroy(e);
+    nn_ctx* ctx = pl->ctx;
+    delete pl;
+    nn_ctx_release(ctx);
+}
+
+// The TMA path needs rows that are a multiple of 16 bytes (nx % 4 == 0) and a
+// driver exposing cuTensorMapEncodeTiled; otherwise it reports UNSUPPORTED and
+// the caller keeps the two-kernel PCG.
+nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, nn_cg_plan** out)
+{
+    *out = nullptr;
+    if (nx % 4 != 0 || nx < 4 || ny < 1 || nz < 1 || !encode_fn()) return NN_ERR_UNSUPPORTED;
+    nn_cg_plan* pl = new nn_cg_plan();
+    pl->ctx = ctx;
+    nn_ctx_retain(ctx);
+    pl->nx = nx; pl->ny = ny; pl->nz = nz;
+    pl->G = (int64_t)nx * ny * nz;
+    pl->op_alpha = (float)alpha;
+    pl->onepb = (float)(1.0 + beta);
+    pl->invd = (float)(1.0 / (1.0 + beta + 6.0 * alpha));
+    pl->tiles = ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY) * ((nz + ZC - 1) / ZC);
+    pl->init_blocks = nn_grid_for(ctx, pl->G, CG_THREADS, 8);
+    const size_t G = (size_t)pl->G;
+    const int nparts = std::max(pl->tiles, pl->init_blocks);
+    nn_status st = NN_OK;
+    for (int q = 0; q < 2 && st == NN_OK; ++q) {
+        st = nn_alloc(ctx, &pl->r[q], G);
+        if (st == NN_OK) st = nn_alloc(ctx, &pl->w[q], G);
+        if (st == NN_OK) st = nn_alloc(ctx, &pl->s[q], G);
+    }
+    if (st == NN_OK) st = nn_alloc(ctx, &pl->p, G);
+    if (st == NN_OK) st = nn_alloc(ctx, &pl->scal, C_COUNT);
+    if (st == NN_OK) st = nn_alloc(ctx, &pl->partials, (size_t)3 * nparts);
+    if (st == NN_OK) st = nn_alloc(ctx, &pl->ticket, 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &pl->flags, 4);
+    for (int q = 0; q < 2 && st == NN_OK; ++q)
+        if (!make_map(&pl->map_r[q], pl->r[q], nx, ny, nz) || !make_map(&pl->map_w[q], pl->w[q], nx, ny, nz) ||
+            !make_map(&pl->map_s[q], pl->s[q], nx, ny, nz))
+            st = NN_ERR_UNSUPPORTED;
+    if (st == NN_OK) {
+        cudaError_t e = cudaFuncSetAttribute(k_cg_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) st = nn_cuda_check(ctx, e, "cudaFuncSetAttribute(k_cg_iter)");
+    }
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemsetAsync(pl->ticket, 0, sizeof(unsigned int), ctx->stream), "memset");
+    if (st != NN_OK) {
+        nn_cg_plan_destroy(pl);
+        return st;
+    }
+    *out = pl;
+    return NN_OK;
+}
+
+void nn_cg_set_timing(nn_cg_plan* pl, bool on) { pl->timing = on; }
+void nn_cg_last_timing(const nn_cg_plan* pl, float* ms, int* iters)
+{
+    *ms = pl->last_ms;
+    *iters = pl->last_iters;
+}
+
+static CgArgs cg_args(nn_cg_plan* pl, float* x, double rtol, int max_iter, int parity_out)
+{
+    CgArgs a;
+    a.nx = pl->nx; a.ny = pl->ny; a.nz = pl->nz;
+    a.op_alpha = pl->op_alpha; a.onepb = pl->onepb; a.invd = pl->invd;
+    a.p = pl->p;
+    a.x = x;
+    a.r_out = pl->r[parity_out];
+    a.w_out = pl->w[parity_out];
+    a.s_out = pl->s[parity_out];
+    a.scal = pl->scal;
+    a.partials = pl->partials;
+    a.ticket = pl->ticket;
+    a.flags = pl->flags;
+    a.rtol2 = rtol * rtol;
+    a.max_iter = max_iter;
+    return a;
+}
+
+// Solve A x = b (x holds the initial guess).  Iterations are enqueued in
+// chunks; the host reads the device flags once per chunk.
+nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
+                    double* relres, int* converged)
+{
+    nn_ctx* ctx = pl->ctx;
+    cudaStream_t cs = ctx->stream;
+    NN_CUDA(ctx, cudaMemsetAsync(pl->ticket, 0, sizeof(unsigned int), cs));  // clean after an aborted solve
+    CgArgs a0 = cg_args(pl, d_x, rtol, max_iter, 0);
+    k_cg_init_r<<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, d_b, d_x, pl->r[0]);
+    NN_CHECK_LAUNCH(ctx, "k_cg_init_r");
+    k_cg_init_w<<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, pl->r[0], pl->w[0], pl->s[0]);
+    NN_CHECK_LAUNCH(ctx, "k_cg_init_w");
+    int h_flags[4] = {0, 0, 0, 0};
+    int it = 0, nchunks = 0;
+    const int chunk = 16;
+    while (true) {
+        NN_CUDA(ctx, cudaMemcpyAsync(h_flags, pl->flags, sizeof h_flags, cudaMemcpyDeviceToHost, cs));
+        NN_CUDA(ctx, cudaStreamSynchronize(cs));
+        if (h_flags[0] || it >= max_iter) break;
+        if (pl->timing) {
+            if ((int)pl->ev_a.size() <= nchunks) {
+                cudaEvent_t e1, e2;
+                NN_CUDA(ctx, cudaEventCreate(&e1));
+                NN_CUDA(ctx, cudaEventCreate(&e2));
+                pl->ev_a.push_back(e1);
+                pl->ev_b.push_back(e2);
+            }
+            NN_CUDA(ctx, cudaEventRecord(pl->ev_a[nchunks], cs));
+        }
+        for (int q = 0; q < chunk && it < max_iter; ++q, ++it) {
+            const int pin = it & 1, pout = pin ^ 1;
+            CgArgs a = cg_args(pl, d_x, rtol, max_iter, pout);
+            k_cg_iter<<<pl->tiles, CG_THREADS, SMEM_BYTES, cs>>>(pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], a);
+            NN_CHECK_LAUNCH(ctx, "k_cg_iter");
+        }
+        if (pl->timing) NN_CUDA(ctx, cudaEventRecord(pl->ev_b[nchunks], cs));
+        ++nchunks;
+    }
+    double h_scal[C_COUNT];
+    NN_CUDA(ctx, cudaMemcpyAsync(h_scal, pl->scal, sizeof h_scal, cudaMemcpyDeviceToHost, cs));
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    if (h_flags[2]) return nn_fail(ctx, NN_ERR_TIMEOUT, "k_cg_iter: a TMA pipeline wait timed out");
+    if (pl->timing) {
+        float tot = 0.0f;
+        for (int c = 0; c < nchunks; ++c) {
+            float ms = 0.0f;
+            NN_CUDA(ctx, cudaEventElapsedTime(&ms, pl->ev_a[c], pl->ev_b[c]));
+            tot += ms;
+        }
+        pl->last_ms = tot;
+        pl->last_iters = h_flags[1];
+    }
+    if (iters) *iters = h_flags[1];
+    if (relres) *relres = h_scal[C_BB] > 0 ? std::sqrt(h_scal[C_RR] / h_scal[C_BB]) : 0.0;
+    if (converged) *converged = h_flags[0] == 1;
+    return NN_OK;
+}

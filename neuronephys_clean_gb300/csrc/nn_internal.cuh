@@ -139,6 +139,16 @@ __host__ __device__ inline int nn_lattice_side(int n)
 nn_status nn_scan_exclusive_i64(nn_ctx* ctx, const int64_t* d_in, int64_t* d_out, int64_t n);
 nn_status nn_build_csc(nn_ctx* ctx, int n, int64_t nnz, const int64_t* d_row_ptr, const int32_t* d_col,
                        int64_t* d_col_ptr, uint32_t* d_edge_of);
+struct nn_pcg;
+nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
+                          double* relres, int* converged);
+struct nn_cg_plan;
+nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, nn_cg_plan** out);
+void nn_cg_plan_destroy(nn_cg_plan* pl);
+nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
+                    double* relres, int* converged);
+void nn_cg_set_timing(nn_cg_plan* pl, bool on);
+void nn_cg_last_timing(const nn_cg_plan* pl, float* ms, int* iters);
 double nn_host_inv_phi(double p);
 void nn_host_gauss_table(double sigma_sites, int16_t* table4096);
 

@@ -39,11 +39,21 @@ struct nn_pcg {
     std::vector<cudaEvent_t> ev_a, ev_b;
     float last_ms = 0.0f;
     int last_iters = 0;
+    // single-kernel TMA iteration (constant D, nx % 4 == 0); null: two-kernel path
+    nn_cg_plan* fast = nullptr;
 };
 
-void nn_pcg_set_timing(nn_pcg* pc, bool on) { pc->timing = on; }
+void nn_pcg_set_timing(nn_pcg* pc, bool on)
+{
+    pc->timing = on;
+    if (pc->fast) nn_cg_set_timing(pc->fast, on);
+}
 void nn_pcg_last_timing(const nn_pcg* pc, float* ms, int* iters)
 {
+    if (pc->fast) {
+        nn_cg_last_timing(pc->fast, ms, iters);
+        return;
+    }
     *ms = pc->last_ms;
     *iters = pc->last_iters;
 }
@@ -321,6 +331,12 @@ extern "C" nn_status nn_pcg_create(nn_ctx* ctx, int nx, int ny, int nz, double a
         ctx->launches++;
     }
     st = nn_cuda_check(ctx, cudaGetLastError(), "nn_pcg_create");
+    if (st == NN_OK && !d_Dcell && !std::getenv("NN_PCG_TWO_KERNEL")) {
+        // constant coefficients: the single-kernel TMA iteration where supported
+        nn_status fs = nn_cg_plan_create(ctx, nx, ny, nz, alpha, beta, &pc->fast);
+        if (fs != NN_OK && fs != NN_ERR_UNSUPPORTED) st = fs;
+        ctx->last_error.clear();
+    }
     if (st != NN_OK) {
         nn_pcg_destroy(pc);
         return st;
@@ -335,6 +351,7 @@ extern "C" nn_status nn_pcg_destroy(nn_pcg* pc)
     if (pc->ctx) cudaStreamSynchronize(pc->ctx->stream);
     nn_release(pc->r); nn_release(pc->p0); nn_release(pc->p1); nn_release(pc->Ap); nn_release(pc->scal);
     nn_release(pc->partials); nn_release(pc->ticket); nn_release(pc->flags); nn_release(pc->invd);
+    if (pc->fast) nn_cg_plan_destroy(pc->fast);
     for (auto e : pc->ev_a) cudaEventDestroy(e);
     for (auto e : pc->ev_b) cudaEventDestroy(e);
     nn_ctx* ctx = pc->ctx;
@@ -458,9 +475,17 @@ extern "C" nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, doub
 {
     if (!pc || !d_b || !d_x || !(rtol > 0.0) || max_iter < 0) return NN_ERR_INVALID_ARG;
     int conv = 0;
-    NN_TRY(nn_pcg_run(pc, d_b, d_x, rtol, max_iter, iters, relres, &conv));
+    NN_TRY(nn_pcg_run_best(pc, d_b, d_x, rtol, max_iter, iters, relres, &conv));
     if (!conv) return nn_fail(pc->ctx, NN_ERR_NOT_CONVERGED, "PCG did not reach rtol %g in %d iterations", rtol, max_iter);
     return NN_OK;
+}
+
+// The single-kernel TMA iteration when the grid allows it, else two kernels.
+nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
+                          double* relres, int* converged)
+{
+    if (pc->fast) return nn_cg_run(pc->fast, d_b, d_x, rtol, max_iter, iters, relres, converged);
+    return nn_pcg_run(pc, d_b, d_x, rtol, max_iter, iters, relres, converged);
 }
 
 // ========================================================= no allocation ==

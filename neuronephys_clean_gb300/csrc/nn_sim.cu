@@ -1216,7 +1216,7 @@ static nn_status paracrine_solve(nn_sim* s)
     NN_CHECK_LAUNCH(ctx, "k_par_rhs");
     int it = 0, conv = 0;
     double rel = 0.0;
-    NN_TRY(nn_pcg_run(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, &it, &rel, &conv));
+    NN_TRY(nn_pcg_run_best(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, &it, &rel, &conv));
     s->stats.iterations = it;
     s->stats.relres = rel;
     s->stats.converged = conv;
