@@ -46,7 +46,7 @@ WORKLOADS = {
 
 # Algorithmic bytes per unit:
 HH_BYTES_PER_NEURON_STEP = 60      # R: V,m,h,n,ge,gi,I (28 B) + ring (E,I) slot (8 B); W: 6 state floats (24 B)
-PCG_BYTES_PER_CELL_ITER = 40       # R: r,p_old (dir+apply), x,p,r,Ap (update); W: p,Ap,x,r -> 10 floats
+PCG_BYTES_PER_CELL_ITER = 40       # k_cg_iter R: r,w,s,p,x; W: r,w,s,p,x -> 10 floats per cell
 PUSH_BYTES_PER_EVENT = 13          # 4 B target + 4 B weight + 1 B delay + 4 B ring read-modify-write
 
 # DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
@@ -232,7 +232,7 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
                "traffic": (NCU_TRAFFIC_PER_UNIT["hh_step"] * n) if NCU_TRAFFIC_PER_UNIT["hh_step"] else None,
                "algorithmic_bytes": n * HH_BYTES_PER_NEURON_STEP, "launch_ms": kt.hh_step_ms,
                "peak_source": peak_kind}
-    pcg_roof = {"bound": "hbm", "kernel": "k_pcg_dir_apply+k_pcg_update (one PCG iteration)", "achieved": pcg_ach,
+    pcg_roof = {"bound": "hbm", "kernel": "k_cg_iter (one PCG iteration)", "achieved": pcg_ach,
                 "peak": hbm_peak, "unit": "GB/s", "frac": pcg_ach / hbm_peak if pcg_ach else None,
                 "traffic": (NCU_TRAFFIC_PER_UNIT["pcg_iteration"] * G) if NCU_TRAFFIC_PER_UNIT["pcg_iteration"] else None,
                 "algorithmic_bytes": G * PCG_BYTES_PER_CELL_ITER, "launch_ms": it_ms, "peak_source": peak_kind}

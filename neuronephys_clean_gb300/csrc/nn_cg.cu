@@ -34,9 +34,10 @@ constexpr int BXW = 40, BYW = 10;            // TMA box: x from x0 - 4, y from y
 constexpr int RX = TX + 2, RY = TY + 2;      // u region (tile + halo)
 constexpr int PLANE_BYTES = BXW * BYW * 4;   // 1600
 constexpr int PLANE_STRIDE = 1664;           // 128-byte multiple
-constexpr int NARR = 3;                      // r, w, s
+constexpr int NARR = 3;                      // r, w, s (with halo)
+constexpr int PX_BYTES = TX * TY * 4;        // p, x interior boxes (owned planes only)
 constexpr int STAGES = 4;
-constexpr int STAGE_BYTES = NARR * PLANE_STRIDE;
+constexpr int STAGE_BYTES = NARR * PLANE_STRIDE + 2 * PX_BYTES;
 constexpr int U_BYTES = 3 * RY * RX * 4;
 constexpr int SMEM_BYTES = 128 + STAGES * STAGE_BYTES + U_BYTES + STAGES * 8 + 64;
 constexpr uint32_t WAIT_LIMIT = 1u << 20;
@@ -212,7 +213,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init_w(CgArgs a, const float*
 // One CG iteration (see the file comment).  One tile per block.
 __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ CUtensorMap tm_r,
                                                         const __grid_constant__ CUtensorMap tm_w,
-                                                        const __grid_constant__ CUtensorMap tm_s, CgArgs a)
+                                                        const __grid_constant__ CUtensorMap tm_s,
+                                                        const __grid_constant__ CUtensorMap tm_p,
+                                                        const __grid_constant__ CUtensorMap tm_x, CgArgs a)
 {
     if (a.flags[0]) return;
     extern __shared__ unsigned char smem_raw[];
@@ -239,15 +242,24 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0) {
-        for (int j = 0; j < STAGES && j < np; ++j) {
-            unsigned char* st = stage_base + j * STAGE_BYTES;
-            mbar_expect_tx(&bars[j], NARR * PLANE_BYTES);
-            tma_load_plane(st, &tm_r, x0 - 4, y0 - 1, z0 - 1 + j, &bars[j]);
-            tma_load_plane(st + PLANE_STRIDE, &tm_w, x0 - 4, y0 - 1, z0 - 1 + j, &bars[j]);
-            tma_load_plane(st + 2 * PLANE_STRIDE, &tm_s, x0 - 4, y0 - 1, z0 - 1 + j, &bars[j]);
+    // plane j (z = z0 - 1 + j) into stage j % STAGES: r, w, s with halo, and
+    // for owned planes p, x of the tile
+    auto issue = [&](int j) {
+        unsigned char* st = stage_base + (j % STAGES) * STAGE_BYTES;
+        uint64_t* bar = &bars[j % STAGES];
+        const int kz = z0 - 1 + j;
+        const bool own = j >= 1 && j <= np - 2;
+        mbar_expect_tx(bar, NARR * PLANE_BYTES + (own ? 2 * PX_BYTES : 0));
+        tma_load_plane(st, &tm_r, x0 - 4, y0 - 1, kz, bar);
+        tma_load_plane(st + PLANE_STRIDE, &tm_w, x0 - 4, y0 - 1, kz, bar);
+        tma_load_plane(st + 2 * PLANE_STRIDE, &tm_s, x0 - 4, y0 - 1, kz, bar);
+        if (own) {
+            tma_load_plane(st + 3 * PLANE_STRIDE, &tm_p, x0, y0, kz, bar);
+            tma_load_plane(st + 3 * PLANE_STRIDE + PX_BYTES, &tm_x, x0, y0, kz, bar);
         }
-    }
+    };
+    if (tid == 0)
+        for (int j = 0; j < STAGES && j < np; ++j) issue(j);
 
     // interior cell of this thread
     const int ix = tid & 31, iy = tid >> 5;
@@ -265,6 +277,8 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
         const float* R = (const float*)(stage_base + sidx * STAGE_BYTES);
         const float* W = (const float*)(stage_base + sidx * STAGE_BYTES + PLANE_STRIDE);
         const float* S = (const float*)(stage_base + sidx * STAGE_BYTES + 2 * PLANE_STRIDE);
+        const float* Ps = (const float*)(stage_base + sidx * STAGE_BYTES + 3 * PLANE_STRIDE);
+        const float* Xs = (const float*)(stage_base + sidx * STAGE_BYTES + 3 * PLANE_STRIDE + PX_BYTES);
         float* Uk = U + (j % 3) * RY * RX;
         const bool plane_in = k >= 0 && k < a.nz;
         // interior cells: s, r, u and the pointwise p, x updates for owned planes
@@ -278,9 +292,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
             Uk[by * RX + bx - 3] = uv;
             if (in && k >= z0 && k < z1) {
                 const int64_t c = gx + sy * gy + sz * k;
-                const float pv = a.invd * rv_old + beta * a.p[c];
+                const float pv = a.invd * rv_old + beta * Ps[iy * TX + ix];
                 a.p[c] = pv;
-                a.x[c] += alpha * pv;
+                a.x[c] = Xs[iy * TX + ix] + alpha * pv;
                 a.s_out[c] = sv;
                 a.r_out[c] = rv;
                 acc_g += rv * uv;
@@ -302,14 +316,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
         }
         __syncthreads();
         // refill this stage with the plane STAGES ahead
-        if (tid == 0 && j + STAGES < np) {
-            unsigned char* st = stage_base + sidx * STAGE_BYTES;
-            const int kz = z0 - 1 + j + STAGES;
-            mbar_expect_tx(&bars[sidx], NARR * PLANE_BYTES);
-            tma_load_plane(st, &tm_r, x0 - 4, y0 - 1, kz, &bars[sidx]);
-            tma_load_plane(st + PLANE_STRIDE, &tm_w, x0 - 4, y0 - 1, kz, &bars[sidx]);
-            tma_load_plane(st + 2 * PLANE_STRIDE, &tm_s, x0 - 4, y0 - 1, kz, &bars[sidx]);
-        }
+        if (tid == 0 && j + STAGES < np) issue(j + STAGES);
         // w = A u for the plane behind (k - 1), owned when j >= 2
         if (j >= 2) {
             const int kb = k - 1;
@@ -369,13 +376,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-bool make_map(CUtensorMap* m, float* base, int nx, int ny, int nz)
+bool make_map(CUtensorMap* m, float* base, int nx, int ny, int nz, bool halo_box)
 {
     auto fn = encode_fn();
     if (!fn) return false;
     cuuint64_t gdim[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
     cuuint64_t gstride[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
-    cuuint32_t box[3] = {BXW, BYW, 1};
+    cuuint32_t box[3] = {halo_box ? (cuuint32_t)BXW : (cuuint32_t)TX, halo_box ? (cuuint32_t)BYW : (cuuint32_t)TY, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
@@ -391,7 +398,7 @@ struct nn_cg_plan {
     int64_t G = 0;
     float op_alpha = 0, onepb = 0, invd = 0;
     float *r[2] = {}, *w[2] = {}, *s[2] = {}, *p = nullptr;
-    CUtensorMap map_r[2], map_w[2], map_s[2];
+    CUtensorMap map_r[2], map_w[2], map_s[2], map_p;
     double* scal = nullptr;
     double* partials = nullptr;
     unsigned int* ticket = nullptr;
@@ -456,9 +463,11 @@ nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, d
     if (st == NN_OK) st = nn_alloc(ctx, &pl->ticket, 1);
     if (st == NN_OK) st = nn_alloc(ctx, &pl->flags, 4);
     for (int q = 0; q < 2 && st == NN_OK; ++q)
-        if (!make_map(&pl->map_r[q], pl->r[q], nx, ny, nz) || !make_map(&pl->map_w[q], pl->w[q], nx, ny, nz) ||
-            !make_map(&pl->map_s[q], pl->s[q], nx, ny, nz))
+        if (!make_map(&pl->map_r[q], pl->r[q], nx, ny, nz, true) ||
+            !make_map(&pl->map_w[q], pl->w[q], nx, ny, nz, true) ||
+            !make_map(&pl->map_s[q], pl->s[q], nx, ny, nz, true))
             st = NN_ERR_UNSUPPORTED;
+    if (st == NN_OK && !make_map(&pl->map_p, pl->p, nx, ny, nz, false)) st = NN_ERR_UNSUPPORTED;
     if (st == NN_OK) {
         cudaError_t e = cudaFuncSetAttribute(k_cg_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) st = nn_cuda_check(ctx, e, "cudaFuncSetAttribute(k_cg_iter)");
@@ -506,6 +515,9 @@ nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, i
     nn_ctx* ctx = pl->ctx;
     cudaStream_t cs = ctx->stream;
     NN_CUDA(ctx, cudaMemsetAsync(pl->ticket, 0, sizeof(unsigned int), cs));  // clean after an aborted solve
+    CUtensorMap map_x;  // the caller's solution vector
+    if (((uintptr_t)d_x & 15) || !make_map(&map_x, d_x, pl->nx, pl->ny, pl->nz, false))
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_cg_run: x must be a 16-byte aligned device vector");
     CgArgs a0 = cg_args(pl, d_x, rtol, max_iter, 0);
     k_cg_init_r<<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, d_b, d_x, pl->r[0]);
     NN_CHECK_LAUNCH(ctx, "k_cg_init_r");
@@ -531,7 +543,8 @@ nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, i
         for (int q = 0; q < chunk && it < max_iter; ++q, ++it) {
             const int pin = it & 1, pout = pin ^ 1;
             CgArgs a = cg_args(pl, d_x, rtol, max_iter, pout);
-            k_cg_iter<<<pl->tiles, CG_THREADS, SMEM_BYTES, cs>>>(pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], a);
+            k_cg_iter<<<pl->tiles, CG_THREADS, SMEM_BYTES, cs>>>(pl->map_r[pin], pl->map_w[pin], pl->map_s[pin],
+                                                                 pl->map_p, map_x, a);
             NN_CHECK_LAUNCH(ctx, "k_cg_iter");
         }
         if (pl->timing) NN_CUDA(ctx, cudaEventRecord(pl->ev_b[nchunks], cs));

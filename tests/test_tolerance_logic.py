@@ -2,14 +2,14 @@
 import numpy as np
 import pytest
 
-from tolerance import assert_rasters_match, trajectory_errors
+from tolerance import assert_rasters_match, assert_trajectory, perturbed_neurons, trajectory_errors
 
 
 def test_raster_shift_accepted_only_at_small_margin():
     ref = {(t, j): 1.0 for t, j in [(10, 1), (20, 2), (30, 3)]} | {(40, 4): 0.001}
-    assert assert_rasters_match(set(ref), ref) == 0
+    assert assert_rasters_match(set(ref), ref) == []
     got = set(ref) - {(40, 4)} | {(41, 4)}
-    assert assert_rasters_match(got, ref, max_frac=0.5) == 1
+    assert assert_rasters_match(got, ref, max_frac=0.5) == [(40, 4)]
     with pytest.raises(AssertionError):   # same shift, but the crossing was not marginal
         assert_rasters_match(set(ref) - {(30, 3)} | {(31, 3)}, ref, max_frac=0.5)
     with pytest.raises(AssertionError):   # a spike the oracle does not have
@@ -27,3 +27,21 @@ def test_trajectory_criterion_separates_steep_neurons():
     assert trajectory_errors(got, ref, prev, 0.01)["violations"] == 0
     got[0, 0] += 0.01                     # 1.5e-4 relative at rest: violation
     assert trajectory_errors(got, ref, prev, 0.01)["violations"] == 1
+
+
+def test_perturbed_neurons_are_held_to_the_wider_bound():
+    rp = np.array([0, 2, 2, 3])
+    col = np.array([1, 2, 0])
+    mask = perturbed_neurons([(10, 0)], rp, col, 3)
+    assert mask.tolist() == [True, True, True]
+    mask = perturbed_neurons([(10, 1)], rp, col, 3)
+    assert mask.tolist() == [False, True, False]
+    ref = np.array([[-65.0, -60.0, -70.0], [0.05] * 3, [0.6] * 3, [0.3] * 3])
+    got = ref.copy()
+    got[0, 1] += 0.5                        # 1e-2 relative on a perturbed neuron
+    assert_trajectory(got, ref, ref, 0.01, exclude=mask)
+    with pytest.raises(AssertionError):
+        assert_trajectory(got, ref, ref, 0.01)
+    got[0, 1] += 10.0                       # beyond the 5e-2 bound
+    with pytest.raises(AssertionError):
+        assert_trajectory(got, ref, ref, 0.01, exclude=mask)

@@ -46,30 +46,49 @@ def trajectory_errors(got: np.ndarray, ref: np.ndarray, ref_prev: np.ndarray, dt
     }
 
 
-def assert_trajectory(got, ref, ref_prev, dt_ms, rtol=1e-4):
+def assert_trajectory(got, ref, ref_prev, dt_ms, rtol=1e-4, exclude=None, exclude_bound=5e-2):
+    """exclude: neurons perturbed by an accepted one-step spike shift (the
+    shifted neurons and their postsynaptic targets, which received that input
+    one step apart); they are held to exclude_bound relative instead."""
+    got, ref, ref_prev = (np.asarray(a, np.float64) for a in (got, ref, ref_prev))
+    if exclude is not None and np.any(exclude):
+        keep = ~np.asarray(exclude, bool)
+        floors = np.array([1.0, 1e-3, 1e-3, 1e-3])[:, None]
+        rel_ex = np.abs(got[:, ~keep] - ref[:, ~keep]) / (np.abs(ref[:, ~keep]) + floors)
+        assert rel_ex.max() < exclude_bound, rel_ex.max()
+        got, ref, ref_prev = got[:, keep], ref[:, keep], ref_prev[:, keep]
     e = trajectory_errors(got, ref, ref_prev, dt_ms, rtol)
     assert e["violations"] == 0, e
     return e
 
 
+def perturbed_neurons(shifted, row_ptr, col, n) -> np.ndarray:
+    """Neurons whose spike was shifted by one step, and their targets."""
+    mask = np.zeros(n, bool)
+    for (_, j) in shifted:
+        mask[j] = True
+        mask[col[row_ptr[j]:row_ptr[j + 1]]] = True
+    return mask
+
+
 MARGIN_MV = 0.01
 
 
-def assert_rasters_match(got: set, ref_margins: dict, max_frac: float = 0.005) -> int:
+def assert_rasters_match(got: set, ref_margins: dict, max_frac: float = 0.005) -> list:
     """Spike rasters as sets of (step, neuron).  They must be identical except
     for spikes shifted by exactly one step whose FP64 threshold crossing lies
     within MARGIN_MV of the step boundary (V before or after the crossing step
     within 0.01 mV of the threshold), at most max_frac of the spikes.  Returns
-    the number of shifted spikes."""
+    the shifted oracle spikes."""
     ref = set(ref_margins)
     only_ref, only_got = ref - got, got - ref
-    shifted = 0
-    for (t, j) in only_ref:
+    shifted = []
+    for (t, j) in sorted(only_ref):
         partner = [(t + d, j) for d in (-1, 1) if (t + d, j) in only_got]
         assert partner, f"spike {(t, j)} of the oracle is missing on the device"
         assert ref_margins[(t, j)] < MARGIN_MV, f"spike {(t, j)} shifted with margin {ref_margins[(t, j)]} mV"
         only_got.discard(partner[0])
-        shifted += 1
+        shifted.append((t, j))
     assert not only_got, f"device spikes without an oracle counterpart: {sorted(only_got)[:5]}"
-    assert shifted <= max_frac * max(len(ref), 1), (shifted, len(ref))
+    assert len(shifted) <= max_frac * max(len(ref), 1), (len(shifted), len(ref))
     return shifted
