@@ -40,6 +40,12 @@ WORKLOADS = {
     "c2": dict(workload="hh_1M_gauss_k100_d20_grid128", n=1_000_000, kind="gauss", k=100, sigma=0.1,
                w_mu=-1.0, w_sigma=1.0, dmax=20, inh=0.2, i_lo=6.0, i_hi=12.0, grid=128, timescale=100,
                par_D=1.0, par_decay=0.0, total_steps=1000),
+    "c5": dict(workload="cg_256cube_lognormalD_s1_l8_uptake0.1", kind="cg", grid=256, sigma=1.0, corr=8.0,
+               D0=1.0, uptake=0.1, dt_s=1e-3, neurons=20000, rate=2.0,
+               # iterations of the FP64 oracle PCG to 1e-6 on this seeded instance
+               # (oracle.pcg7 run to convergence once; the CPU arms time a bounded
+               # number of iterations and scale by this count)
+               fp64_iters=329),
     "c1": dict(workload="hh_1k_er_p0.01_grid32", n=1000, kind="er", p=0.01, w_max=0.5, dmax=1, inh=0.2,
                i_lo=5.0, i_hi=15.0, grid=32, timescale=100, par_D=1.0, par_decay=0.0, total_steps=10000),
 }
@@ -47,6 +53,7 @@ WORKLOADS = {
 # Algorithmic bytes per unit:
 HH_BYTES_PER_NEURON_STEP = 60      # R: V,m,h,n,ge,gi,I (28 B) + ring (E,I) slot (8 B); W: 6 state floats (24 B)
 PCG_BYTES_PER_CELL_ITER = 40       # k_cg_iter R: r,w,s,p,x; W: r,w,s,p,x -> 10 floats per cell
+PCG_HET_BYTES_PER_CELL_ITER = 48   # k_cg_iter<HET>: + D and 1/diag reads
 PUSH_BYTES_PER_EVENT = 13          # 4 B target + 4 B weight + 1 B delay + 4 B ring read-modify-write
 
 # DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
@@ -332,6 +339,135 @@ def cpu_baseline(sim, wl: dict, args) -> dict:
                                vox)
 
 
+def cg_problem(wl: dict):
+    from neuronephys_clean_gb300 import fields
+    g = wl["grid"]
+    shape = (g, g, g)
+    D = fields.lognormal_diffusivity(shape, wl["sigma"], wl["corr"], seed=1)
+    b = fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=2)
+    alpha, beta = fields.be_coefficients(g, wl["dt_s"], wl["D0"], wl["uptake"])
+    return shape, D, b, alpha, beta
+
+
+def run_cg(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
+    """One bench step = one solve of A x = b from x = 0 to a 1e-6 relative
+    residual on the 256^3 heterogeneous grid (Jacobi-PCG, single-kernel TMA
+    iteration)."""
+    import neuronephys_clean_gb300 as nn
+    ctx = nn.Context(local_rank)
+    shape, D, b, alpha, beta = cg_problem(wl)
+    G = int(np.prod(shape))
+    dD, db, dx = ctx.to_device(D.ravel()), ctx.to_device(b), ctx.empty((G,), np.float32)
+    pc = nn.PCG(ctx, shape[2], shape[1], shape[0], alpha, beta, dD)
+    pc.set_kernel_timing(True)
+    for _ in range(args.warmup):
+        dx.zero()
+        pc.solve(db, dx, 1e-6, 20000)
+    ctx.synchronize()
+    launches0 = ctx.kernel_launches
+    clocks = ClockSampler(local_rank)
+    barrier(dist)
+    clocks.start()
+    times, iters, kern_ms, rel = [], [], [], 0.0
+    for _ in range(args.steps):
+        ctx.time_begin()
+        dx.zero()
+        it, rel = pc.solve(db, dx, 1e-6, 20000)
+        times.append(ctx.time_end())
+        ms_k, _ = pc.kernel_time()
+        kern_ms.append(ms_k)
+        iters.append(it)
+    clock_info = clocks.stop()
+    barrier(dist)
+    launches = ctx.kernel_launches - launches0
+    total_ms = sum(times)
+    per_solve, tmax = aggregate(1.0, total_ms / 1e3 / args.steps, dist)
+    ms_solve = tmax * 1e3
+    it_mean = statistics.mean(iters)
+    it_ms = statistics.mean(kern_ms) / it_mean
+    hbm_peak, peak_kind = measured_peaks()
+    ach = G * PCG_HET_BYTES_PER_CELL_ITER / (it_ms * 1e-3) / 1e9
+    x = dx.numpy()
+    # e2e: rhs from pinned host memory, solution back to pinned host memory
+    pin_b = nn.PinnedArray((G,), np.float32)
+    pin_x = nn.PinnedArray((G,), np.float32)
+    pin_b.array[:] = b
+    e2e_s = []
+    for _ in range(max(1, args.e2e_steps)):
+        t0 = time.perf_counter()
+        db.copy_from(pin_b.array)
+        dx.zero()
+        pc.solve(db, dx, 1e-6, 20000)
+        lib_x = dx.numpy()
+        pin_x.array[:] = lib_x
+        e2e_s.append(time.perf_counter() - t0)
+    pin_b.free()
+    pin_x.free()
+    if rank != 0:
+        return None
+    line = {
+        "metric": "CG time-to-1e-6", "value": ms_solve, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_solve, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 reductions)", "data": "synthetic (seeded lognormal D, Poisson sources)",
+        "config": {"workload": wl["workload"], "grid": wl["grid"], "alpha": alpha, "beta": beta,
+                   "preconditioner": "jacobi", "l2": "inputs larger than L2 (9 x 67 MB vectors)"},
+        "cg": {"iterations": it_mean, "relres": rel, "ms_per_iteration": it_ms,
+               "solution_norm": float(np.linalg.norm(x.astype(np.float64)))},
+        "roofline": {"bound": "hbm", "kernel": "k_cg_iter<HET> (one PCG iteration)", "achieved": ach,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None,
+                     "algorithmic_bytes": G * PCG_HET_BYTES_PER_CELL_ITER, "launch_ms": it_ms,
+                     "peak_source": peak_kind},
+        "gpu_launches": int(launches),
+        "clocks": clock_info,
+        "e2e": {"value": 1e3 * statistics.mean(e2e_s), "unit": "ms", "h2d_bytes_per_step": 4 * G,
+                "d2h_bytes_per_step": 4 * G},
+    }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_cg(wl, shape, D, b, alpha, beta, wl["fp64_iters"], args.cpu_steps)
+    pc.close()
+    ctx.close()
+    return line
+
+
+def cpu_baseline_cg(wl, shape, D, b, alpha, beta, iterations, sample_iters) -> dict:
+    """FP64 oracle PCG on the host cores: two bounded runs (k and 4k
+    iterations) separate the setup from the per-iteration time, scaled to the
+    iteration count of the full solve."""
+    import oracle
+    G = int(np.prod(shape))
+    k = max(1, sample_iters) * 4
+    t = []
+    for m in (k, 4 * k):
+        t0 = time.perf_counter()
+        oracle.pcg7(b, np.zeros(G), shape, alpha, beta, D, rtol=1e-30, max_iter=m)
+        t.append(time.perf_counter() - t0)
+    per_it = (t[1] - t[0]) / (3 * k)
+    setup = max(0.0, t[0] - k * per_it)
+    ms = 1e3 * (setup + per_it * iterations)
+    return {"value": ms, "unit": "ms", "cores": int(oracle.lib().orc_num_threads()), "kind": "port",
+            "sample": f"{k} and {4 * k} FP64 PCG iterations on the same {shape[0]}^3 problem "
+                      f"(setup {1e3 * setup:.0f} ms, {1e3 * per_it:.1f} ms/iteration), scaled to {iterations:.0f}"}
+
+
+def run_cg_reference(args, wl: dict, rank: int) -> dict | None:
+    if rank != 0:
+        return None
+    shape, D, b, alpha, beta = cg_problem(wl)
+    times = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline_cg(wl, shape, D, b, alpha, beta, wl["fp64_iters"], args.cpu_steps)
+        if i >= args.warmup:
+            times.append(cb["value"])
+    ms_solve = statistics.mean(times)
+    return {"metric": "CG time-to-1e-6", "value": ms_solve, "unit": "ms", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_solve, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic (seeded lognormal D, Poisson sources)",
+            "config": {"workload": wl["workload"], "grid": wl["grid"]},
+            "cpu_baseline": dict(cb, value=ms_solve),
+            "e2e": {"value": ms_solve, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def run_reference(args, wl: dict, rank: int) -> dict | None:
     """The reference arm: the CPU oracle port of the same workload, all host threads."""
     if rank != 0:
@@ -388,7 +524,7 @@ def main() -> None:
     rank, world, local_rank = dist_env()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
-        line = run_reference(args, wl, rank)
+        line = (run_cg_reference if wl.get("kind") == "cg" else run_reference)(args, wl, rank)
         if line is not None:
             print(json.dumps(line), flush=True)
         return
@@ -402,7 +538,7 @@ def main() -> None:
     if rank != 0:
         build()  # no-op once rank 0 built it
     args.cpu_baseline = args.cpu_baseline and rank == 0 and world == 1
-    line = run_ours(args, wl, dist, rank, local_rank)
+    line = (run_cg if wl.get("kind") == "cg" else run_ours)(args, wl, dist, rank, local_rank)
     if line is not None:
         print(json.dumps(line), flush=True)
 

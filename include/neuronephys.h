@@ -331,6 +331,12 @@ NN_API nn_status nn_pcg_apply(nn_pcg* pc, const float* d_x, float* d_y);
 /* Solve A x = b to ||r|| <= rtol ||b||; d_x holds the initial guess. */
 NN_API nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter,
                               int* iters, double* relres);
+/* No counterpart in the reference (it has no timing hooks).  With timing on,
+ * each solve brackets its iteration kernels with CUDA events;
+ * nn_pcg_kernel_time returns their total (ms) and the iteration count of
+ * the last solve. */
+NN_API nn_status nn_pcg_set_kernel_timing(nn_pcg* pc, int enable);
+NN_API nn_status nn_pcg_kernel_time(nn_pcg* pc, float* ms, int* iters);
 
 /* No counterpart in the reference.  The same solve as nn_pcg_create +
  * nn_pcg_solve + nn_pcg_destroy for callers that may not allocate device
@@ -354,5 +360,40 @@ NN_API nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, double r
 NN_API nn_status nn_pcg_solve_noalloc(void* stream, int nx, int ny, int nz, double alpha, double beta,
                                       const float* d_Dcell, const float* d_b, float* d_x, double rtol,
                                       int max_iter, int* iters, double* relres);
+
+
+/* ==========================================================================
+ * Learned preconditioner building blocks (no counterpart in the reference).
+ * Activations use a zero-padded, channel-blocked BF16 layout (nn_act_layout
+ * gives the bytes of a tensor with `channels` channels on an nz x ny x nx
+ * grid; channels a multiple of 8).  3x3x3 "same" convolutions run on the
+ * tensor cores with FP32 accumulation.  Weights are FP32 w[27][cin][cout]
+ * (tap = (dz+1)*9 + (dy+1)*3 + dx+1) packed to BF16 by
+ * nn_conv3d_pack_weights; with adjoint set the packed operator is the
+ * input-gradient convolution (taps mirrored, cin and cout exchanged), run by
+ * nn_conv3d_forward with the channel counts exchanged.  Supported
+ * (cin, cout): (16,16) (16,32) (32,32) (32,64) (64,64) (96,32) (48,16) and
+ * their exchanges.
+ * ========================================================================== */
+NN_API nn_status nn_act_layout(int nz, int ny, int nx, int channels, int64_t* block_stride, int64_t* guard,
+                               int64_t* bytes);
+/* dense FP32 [channels][nz][ny][nx] <-> padded BF16 activation (the
+ * activation's pads must be zero: allocate with nn_malloc + nn_memset_d). */
+NN_API nn_status nn_act_pack(nn_ctx* ctx, int nz, int ny, int nx, int channels, const float* d_dense, void* d_act);
+NN_API nn_status nn_act_unpack(nn_ctx* ctx, int nz, int ny, int nx, int channels, const void* d_act,
+                               float* d_dense);
+/* d_packed: 27 * cin * cout * 2 bytes, 16-byte aligned. */
+NN_API nn_status nn_conv3d_pack_weights(nn_ctx* ctx, int cin, int cout, const float* d_w, int adjoint,
+                                        void* d_packed);
+/* y = relu?(conv(x) + bias), then zeroed where d_mask (same layout as y,
+ * nullable) is <= 0; d_bias and d_y32 (dense FP32 copy of channel 0) nullable.
+ * Synchronises; NN_ERR_TIMEOUT if a pipeline wait gave up. */
+NN_API nn_status nn_conv3d_forward(nn_ctx* ctx, int nz, int ny, int nx, int cin, int cout, const void* d_x,
+                                   const void* d_wpacked, const float* d_bias, int relu, const void* d_mask,
+                                   void* d_y, float* d_y32);
+/* d_dw[27][cin][cout] += sum_o x(o + tap) gy(o); d_db[cout] += sum_o gy(o)
+ * (nullable).  FP32 accumulation. */
+NN_API nn_status nn_conv3d_wgrad(nn_ctx* ctx, int nz, int ny, int nx, int cin, int cout, const void* d_x,
+                                 const void* d_gy, float* d_dw, float* d_db);
 
 #endif

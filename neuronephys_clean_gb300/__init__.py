@@ -538,6 +538,15 @@ class PCG:
                "pcg_solve")
         return it.value, rel.value
 
+    def set_kernel_timing(self, on: bool = True) -> None:
+        _check(lib().nn_pcg_set_kernel_timing(self.handle, int(on)), self.ctx, "pcg_set_kernel_timing")
+
+    def kernel_time(self) -> tuple[float, int]:
+        """(ms of the iteration kernels, iterations) of the last solve."""
+        ms, it = C.c_float(0), C.c_int(0)
+        _check(lib().nn_pcg_kernel_time(self.handle, C.byref(ms), C.byref(it)), self.ctx, "pcg_kernel_time")
+        return ms.value, it.value
+
     def close(self):
         if self.handle:
             lib().nn_pcg_destroy(self.handle)
@@ -548,3 +557,52 @@ class PCG:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------- learned preconditioner layers --
+
+def act_bytes(shape, channels: int) -> int:
+    """Bytes of a padded BF16 activation with `channels` channels on shape (nz, ny, nx)."""
+    nz, ny, nx = shape
+    b = C.c_int64()
+    _check(lib().nn_act_layout(nz, ny, nx, channels, None, None, C.byref(b)), None, "nn_act_layout")
+    return int(b.value)
+
+
+class Activation(DeviceArray):
+    """Padded channel-blocked BF16 activation (zeros in pads and guards)."""
+
+    def __init__(self, ctx: Context, shape, channels: int):
+        super().__init__(ctx, (act_bytes(shape, channels),), np.uint8)
+        self.grid, self.channels = tuple(shape), channels
+        self.zero()
+
+    def pack(self, dense: DeviceArray) -> None:
+        nz, ny, nx = self.grid
+        _check(lib().nn_act_pack(self.ctx.handle, nz, ny, nx, self.channels, dense.ptr, self.ptr), self.ctx, "act_pack")
+
+    def unpack(self) -> np.ndarray:
+        nz, ny, nx = self.grid
+        d = DeviceArray(self.ctx, (self.channels, nz, ny, nx), np.float32)
+        _check(lib().nn_act_unpack(self.ctx.handle, nz, ny, nx, self.channels, self.ptr, d.ptr), self.ctx, "act_unpack")
+        return d.numpy()
+
+
+def conv3d_pack_weights(ctx: Context, w: DeviceArray, cin: int, cout: int, adjoint: bool = False) -> DeviceArray:
+    out = DeviceArray(ctx, (27 * cin * cout * 2,), np.uint8)
+    _check(lib().nn_conv3d_pack_weights(ctx.handle, cin, cout, w.ptr, int(adjoint), out.ptr), ctx, "conv3d_pack")
+    return out
+
+
+def conv3d_forward(ctx: Context, x: Activation, wpacked: DeviceArray, y: Activation, bias: DeviceArray | None = None,
+                   relu: bool = False, mask: Activation | None = None, y32: DeviceArray | None = None) -> None:
+    nz, ny, nx = x.grid
+    _check(lib().nn_conv3d_forward(ctx.handle, nz, ny, nx, x.channels, y.channels, x.ptr, wpacked.ptr,
+                                   None if bias is None else bias.ptr, int(relu), None if mask is None else mask.ptr,
+                                   y.ptr, None if y32 is None else y32.ptr), ctx, "conv3d_forward")
+
+
+def conv3d_wgrad(ctx: Context, x: Activation, gy: Activation, dw: DeviceArray, db: DeviceArray | None = None) -> None:
+    nz, ny, nx = x.grid
+    _check(lib().nn_conv3d_wgrad(ctx.handle, nz, ny, nx, x.channels, gy.channels, x.ptr, gy.ptr, dw.ptr,
+                                 None if db is None else db.ptr), ctx, "conv3d_wgrad")

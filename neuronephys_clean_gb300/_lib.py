@@ -130,6 +130,16 @@ _SIGS = {
     "nn_pcg_destroy": (c_int, [c_void_p]),
     "nn_pcg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
     "nn_pcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
+    "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
+    "nn_act_layout": (c_int, [c_int, c_int, c_int, c_int, P(c_int64), P(c_int64), P(c_int64)]),
+    "nn_act_pack": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
+    "nn_act_unpack": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
+    "nn_conv3d_pack_weights": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p]),
+    "nn_conv3d_forward": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int,
+                                  c_void_p, c_void_p, c_void_p]),
+    "nn_conv3d_wgrad": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                c_void_p]),
+    "nn_pcg_kernel_time": (c_int, [c_void_p, P(c_float), P(c_int)]),
     "nn_pcg_solve_noalloc": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_double, c_void_p, c_void_p,
                                      c_void_p, c_double, c_int, P(c_int), P(c_double)]),
 }

@@ -1,8 +1,11 @@
 // Single-kernel-per-iteration preconditioned CG (Chronopoulos & Gear, "s-step
 // iterative methods for symmetric linear systems", J. Comput. Appl. Math. 25,
 // 1989) for the constant-coefficient 7-point backward-Euler operator
-//   A = (1 + beta) I + alpha L,   L the 7-point Laplacian with zero values
-// outside the grid (homogeneous Dirichlet), Jacobi preconditioner M = 1/diag.
+//   A = (1 + beta) I + alpha L_D,  (L_D v)_c = sum over the 6 faces f of
+//   c_f (v_c - v_nb), zero values outside the grid (homogeneous Dirichlet),
+// Jacobi preconditioner M = 1/diag.  With constant coefficients every c_f = 1;
+// with a cell field D (the HET variant) c_f is the harmonic mean of D on the
+// two sides of the face, D_c on a boundary face.
 //
 // The recurrences need one grid-wide reduction per iteration:
 //   p_i = u_i + b_i p_{i-1}        s_i = w_i + b_i s_{i-1}      (s = A p)
@@ -16,6 +19,9 @@
 // through a 4-deep mbarrier pipeline; out-of-range boxes are zero-filled by
 // the TMA unit, which is exactly the Dirichlet boundary.  u = M r_new is formed
 // for the tile plus halo in a 3-plane ring, w = A u for the plane behind it.
+// The HET variant also stages D and 1/diag with the same halo and keeps D in
+// a 3-plane ring beside u for the face coefficients (48 instead of 40 bytes
+// of DRAM traffic per cell and iteration).
 // r, w and s are double-buffered (the next iteration reads the halo of cells
 // other blocks write); p and x are updated in place.  The last block to finish
 // sums the block partials in FP64 and forms the next iteration's scalars, so
@@ -29,17 +35,23 @@
 
 namespace {
 constexpr int CG_THREADS = 256;
-constexpr int TX = 32, TY = 8, ZC = 16;
+constexpr int TX = 32, TY = 8;             // tile; its depth in z (zc) is chosen per plan
 constexpr int BXW = 40, BYW = 10;            // TMA box: x from x0 - 4, y from y0 - 1
 constexpr int RX = TX + 2, RY = TY + 2;      // u region (tile + halo)
 constexpr int PLANE_BYTES = BXW * BYW * 4;   // 1600
 constexpr int PLANE_STRIDE = 1664;           // 128-byte multiple
-constexpr int NARR = 3;                      // r, w, s (with halo)
 constexpr int PX_BYTES = TX * TY * 4;        // p, x interior boxes (owned planes only)
-constexpr int STAGES = 4;
-constexpr int STAGE_BYTES = NARR * PLANE_STRIDE + 2 * PX_BYTES;
-constexpr int U_BYTES = 3 * RY * RX * 4;
-constexpr int SMEM_BYTES = 128 + STAGES * STAGE_BYTES + U_BYTES + STAGES * 8 + 64;
+constexpr int STAGES = 3;
+constexpr int U_BYTES = 3 * RY * RX * 4;     // one 3-plane ring over the u region
+
+template <bool HET>
+struct Layout {
+    static constexpr int NARR = HET ? 5 : 3;  // r, w, s (+ D, 1/diag), with halo
+    static constexpr int STAGE_BYTES = NARR * PLANE_STRIDE + 2 * PX_BYTES;
+    static constexpr int RING_BYTES = (HET ? 2 : 1) * U_BYTES;  // u (+ D)
+    static constexpr int SMEM_BYTES = 128 + STAGES * STAGE_BYTES + RING_BYTES + STAGES * 8 + 64;
+};
+static_assert(Layout<true>::SMEM_BYTES <= 227 * 1024, "shared memory");
 constexpr uint32_t WAIT_LIMIT = 1u << 20;
 constexpr int HALO_CELLS = 2 * RX + 2 * TY;  // 84
 
@@ -47,7 +59,10 @@ enum { C_GAMMA = 0, C_ALPHA, C_BETA, C_RR, C_BB, C_DELTA, C_COUNT };
 
 struct CgArgs {
     int nx, ny, nz;
-    float op_alpha, onepb, invd;
+    int zc;                       // tile depth in z
+    float op_alpha, onepb, invd;  // invd: 1/diag for constant coefficients
+    const float* D;               // HET: cell field
+    const float* invdv;           // HET: 1/diag per cell
     float* p;
     float* x;
     float* r_out;
@@ -147,22 +162,44 @@ __device__ bool cg_reduce(int nsum, const float* v, double* partials, unsigned i
     return true;
 }
 
+__device__ __forceinline__ float face_coef(float dc, float dn, bool inside)
+{
+    return inside ? __fdividef(2.0f * dc * dn, dc + dn) : dc;
+}
+
+// (A v)_c with v read through v(index) (zero outside the grid).
+template <bool HET, class V>
+__device__ __forceinline__ float apply_A(const CgArgs& a, int64_t c, int i, int j, int k, V v)
+{
+    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny;
+    const bool in[6] = {i > 0, i < a.nx - 1, j > 0, j < a.ny - 1, k > 0, k < a.nz - 1};
+    const int64_t off[6] = {-1, 1, -sy, sy, -sz, sz};
+    const float vc = v(c);
+    if (!HET) {
+        float nb = 0.0f;
+#pragma unroll
+        for (int f = 0; f < 6; ++f) nb += in[f] ? v(c + off[f]) : 0.0f;
+        return (a.onepb + 6.0f * a.op_alpha) * vc - a.op_alpha * nb;
+    }
+    const float dc = a.D[c];
+    float acc = 0.0f;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        const float cf = face_coef(dc, in[f] ? a.D[c + off[f]] : 0.0f, in[f]);
+        acc += cf * (vc - (in[f] ? v(c + off[f]) : 0.0f));
+    }
+    return a.onepb * vc + a.op_alpha * acc;
+}
+
 // r0 = b - A x0 (neighbour loads; once per solve); bb = (b, b)
+template <bool HET>
 __global__ void __launch_bounds__(CG_THREADS) k_cg_init_r(CgArgs a, const float* b, const float* x, float* r)
 {
-    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, G = sz * a.nz;
+    const int64_t sz = (int64_t)a.nx * a.ny, G = sz * a.nz;
     float bb = 0.0f;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < G; c += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(c % a.nx), j = (int)((c / a.nx) % a.ny), k = (int)(c / sz);
-        const float xc = x[c];
-        float nb = 0.0f;
-        nb += i > 0 ? x[c - 1] : 0.0f;
-        nb += i < a.nx - 1 ? x[c + 1] : 0.0f;
-        nb += j > 0 ? x[c - sy] : 0.0f;
-        nb += j < a.ny - 1 ? x[c + sy] : 0.0f;
-        nb += k > 0 ? x[c - sz] : 0.0f;
-        nb += k < a.nz - 1 ? x[c + sz] : 0.0f;
-        const float ax = (a.onepb + 6.0f * a.op_alpha) * xc - a.op_alpha * nb;
+        const float ax = apply_A<HET>(a, c, i, j, k, [&](int64_t q) { return x[q]; });
         const float bv = b[c];
         r[c] = bv - ax;
         bb += bv * bv;
@@ -173,22 +210,22 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init_r(CgArgs a, const float*
 }
 
 // w0 = A (M r0), p = 0, s = 0; g0, d0, rho0 -> a0, b0 = 0
+template <bool HET>
 __global__ void __launch_bounds__(CG_THREADS) k_cg_init_w(CgArgs a, const float* r, float* w, float* s)
 {
-    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, G = sz * a.nz;
+    const int64_t sz = (int64_t)a.nx * a.ny, G = sz * a.nz;
     float g = 0.0f, d = 0.0f, rr = 0.0f;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < G; c += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(c % a.nx), j = (int)((c / a.nx) % a.ny), k = (int)(c / sz);
         const float rc = r[c];
-        float nb = 0.0f;
-        nb += i > 0 ? r[c - 1] : 0.0f;
-        nb += i < a.nx - 1 ? r[c + 1] : 0.0f;
-        nb += j > 0 ? r[c - sy] : 0.0f;
-        nb += j < a.ny - 1 ? r[c + sy] : 0.0f;
-        nb += k > 0 ? r[c - sz] : 0.0f;
-        nb += k < a.nz - 1 ? r[c + sz] : 0.0f;
-        const float uc = a.invd * rc;
-        const float wc = a.invd * ((a.onepb + 6.0f * a.op_alpha) * rc - a.op_alpha * nb);
+        float uc, wc;
+        if (HET) {
+            uc = a.invdv[c] * rc;
+            wc = apply_A<true>(a, c, i, j, k, [&](int64_t q) { return a.invdv[q] * r[q]; });
+        } else {
+            uc = a.invd * rc;
+            wc = a.invd * apply_A<false>(a, c, i, j, k, [&](int64_t q) { return r[q]; });
+        }
         w[c] = wc;
         s[c] = 0.0f;
         a.p[c] = 0.0f;
@@ -210,19 +247,27 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init_w(CgArgs a, const float*
     }
 }
 
-// One CG iteration (see the file comment).  One tile per block.
+// One CG iteration (see the file comment).  One tile per block.  tm_d and
+// tm_m (D and 1/diag) are read only by the HET variant.
+template <bool HET>
 __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ CUtensorMap tm_r,
                                                         const __grid_constant__ CUtensorMap tm_w,
                                                         const __grid_constant__ CUtensorMap tm_s,
+                                                        const __grid_constant__ CUtensorMap tm_d,
+                                                        const __grid_constant__ CUtensorMap tm_m,
                                                         const __grid_constant__ CUtensorMap tm_p,
                                                         const __grid_constant__ CUtensorMap tm_x, CgArgs a)
 {
+    using L = Layout<HET>;
+    constexpr int STAGE_BYTES = L::STAGE_BYTES;
+    constexpr int PX_OFF = L::NARR * PLANE_STRIDE;  // p, x boxes after the halo planes
     if (a.flags[0]) return;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     unsigned char* stage_base = smem;
     float* U = (float*)(smem + STAGES * STAGE_BYTES);  // [3][RY][RX]
-    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + U_BYTES);
+    float* Dr = U + 3 * RY * RX;                        // HET: D ring [3][RY][RX]
+    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + L::RING_BYTES);
     __shared__ int abort_flag;
 
     const int tid = threadIdx.x;
@@ -230,8 +275,8 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
     const int tx = blockIdx.x % tiles_x;
     const int ty = (blockIdx.x / tiles_x) % tiles_y;
     const int tz = blockIdx.x / (tiles_x * tiles_y);
-    const int x0 = tx * TX, y0 = ty * TY, z0 = tz * ZC;
-    const int z1 = min(z0 + ZC, a.nz);
+    const int x0 = tx * TX, y0 = ty * TY, z0 = tz * a.zc;
+    const int z1 = min(z0 + a.zc, a.nz);
     const int np = z1 - z0 + 2;  // planes z0-1 .. z1
     const float alpha = (float)a.scal[C_ALPHA], beta = (float)a.scal[C_BETA];
     const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny;
@@ -249,13 +294,17 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
         uint64_t* bar = &bars[j % STAGES];
         const int kz = z0 - 1 + j;
         const bool own = j >= 1 && j <= np - 2;
-        mbar_expect_tx(bar, NARR * PLANE_BYTES + (own ? 2 * PX_BYTES : 0));
+        mbar_expect_tx(bar, L::NARR * PLANE_BYTES + (own ? 2 * PX_BYTES : 0));
         tma_load_plane(st, &tm_r, x0 - 4, y0 - 1, kz, bar);
         tma_load_plane(st + PLANE_STRIDE, &tm_w, x0 - 4, y0 - 1, kz, bar);
         tma_load_plane(st + 2 * PLANE_STRIDE, &tm_s, x0 - 4, y0 - 1, kz, bar);
+        if (HET) {
+            tma_load_plane(st + 3 * PLANE_STRIDE, &tm_d, x0 - 4, y0 - 1, kz, bar);
+            tma_load_plane(st + 4 * PLANE_STRIDE, &tm_m, x0 - 4, y0 - 1, kz, bar);
+        }
         if (own) {
-            tma_load_plane(st + 3 * PLANE_STRIDE, &tm_p, x0, y0, kz, bar);
-            tma_load_plane(st + 3 * PLANE_STRIDE + PX_BYTES, &tm_x, x0, y0, kz, bar);
+            tma_load_plane(st + PX_OFF, &tm_p, x0, y0, kz, bar);
+            tma_load_plane(st + PX_OFF + PX_BYTES, &tm_x, x0, y0, kz, bar);
         }
     };
     if (tid == 0)
@@ -277,9 +326,12 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
         const float* R = (const float*)(stage_base + sidx * STAGE_BYTES);
         const float* W = (const float*)(stage_base + sidx * STAGE_BYTES + PLANE_STRIDE);
         const float* S = (const float*)(stage_base + sidx * STAGE_BYTES + 2 * PLANE_STRIDE);
-        const float* Ps = (const float*)(stage_base + sidx * STAGE_BYTES + 3 * PLANE_STRIDE);
-        const float* Xs = (const float*)(stage_base + sidx * STAGE_BYTES + 3 * PLANE_STRIDE + PX_BYTES);
+        const float* Dst = (const float*)(stage_base + sidx * STAGE_BYTES + 3 * PLANE_STRIDE);
+        const float* Mst = (const float*)(stage_base + sidx * STAGE_BYTES + 4 * PLANE_STRIDE);
+        const float* Ps = (const float*)(stage_base + sidx * STAGE_BYTES + PX_OFF);
+        const float* Xs = (const float*)(stage_base + sidx * STAGE_BYTES + PX_OFF + PX_BYTES);
         float* Uk = U + (j % 3) * RY * RX;
+        float* Dk = Dr + (j % 3) * RY * RX;
         const bool plane_in = k >= 0 && k < a.nz;
         // interior cells: s, r, u and the pointwise p, x updates for owned planes
         {
@@ -288,11 +340,13 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
             const float rv_old = R[by * BXW + bx];
             const float rv = rv_old - alpha * sv;
             const bool in = col_in && plane_in;
-            const float uv = in ? a.invd * rv : 0.0f;
+            const float mi = HET ? Mst[by * BXW + bx] : a.invd;
+            const float uv = in ? mi * rv : 0.0f;
             Uk[by * RX + bx - 3] = uv;
+            if (HET) Dk[by * RX + bx - 3] = Dst[by * BXW + bx];
             if (in && k >= z0 && k < z1) {
                 const int64_t c = gx + sy * gy + sz * k;
-                const float pv = a.invd * rv_old + beta * Ps[iy * TX + ix];
+                const float pv = mi * rv_old + beta * Ps[iy * TX + ix];
                 a.p[c] = pv;
                 a.x[c] = Xs[iy * TX + ix] + alpha * pv;
                 a.s_out[c] = sv;
@@ -312,7 +366,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
             const bool in = plane_in && hx >= 0 && hx < a.nx && hy >= 0 && hy < a.ny;
             const float sv = W[by * BXW + bx] + beta * S[by * BXW + bx];
             const float rv = R[by * BXW + bx] - alpha * sv;
-            Uk[by * RX + bx - 3] = in ? a.invd * rv : 0.0f;
+            const float mi = HET ? Mst[by * BXW + bx] : a.invd;
+            Uk[by * RX + bx - 3] = in ? mi * rv : 0.0f;
+            if (HET) Dk[by * RX + bx - 3] = Dst[by * BXW + bx];
         }
         __syncthreads();
         // refill this stage with the plane STAGES ahead
@@ -325,14 +381,29 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
             const int bx = ix + 1, by = iy + 1;               // in u-region coordinates
             if (col_in && kb < z1) {
                 const float uc = Uc[by * RX + bx];
-                const float nb = Uc[by * RX + bx - 1] + Uc[by * RX + bx + 1] + Uc[(by - 1) * RX + bx] +
-                                 Uc[(by + 1) * RX + bx] + Um[by * RX + bx] + Uk[by * RX + bx];
-                const float wv = (a.onepb + 6.0f * a.op_alpha) * uc - a.op_alpha * nb;
+                float wv;
+                if (HET) {
+                    const float* Dm = Dr + ((j - 2) % 3) * RY * RX;
+                    const float* Dc = Dr + ((j - 1) % 3) * RY * RX;
+                    const float dc = Dc[by * RX + bx];
+                    float acc = face_coef(dc, Dc[by * RX + bx - 1], gx > 0) * (uc - Uc[by * RX + bx - 1]);
+                    acc += face_coef(dc, Dc[by * RX + bx + 1], gx < a.nx - 1) * (uc - Uc[by * RX + bx + 1]);
+                    acc += face_coef(dc, Dc[(by - 1) * RX + bx], gy > 0) * (uc - Uc[(by - 1) * RX + bx]);
+                    acc += face_coef(dc, Dc[(by + 1) * RX + bx], gy < a.ny - 1) * (uc - Uc[(by + 1) * RX + bx]);
+                    acc += face_coef(dc, Dm[by * RX + bx], kb > 0) * (uc - Um[by * RX + bx]);
+                    acc += face_coef(dc, Dk[by * RX + bx], kb < a.nz - 1) * (uc - Uk[by * RX + bx]);
+                    wv = a.onepb * uc + a.op_alpha * acc;
+                } else {
+                    const float nb = Uc[by * RX + bx - 1] + Uc[by * RX + bx + 1] + Uc[(by - 1) * RX + bx] +
+                                     Uc[(by + 1) * RX + bx] + Um[by * RX + bx] + Uk[by * RX + bx];
+                    wv = (a.onepb + 6.0f * a.op_alpha) * uc - a.op_alpha * nb;
+                }
                 a.w_out[gx + sy * gy + sz * kb] = wv;
                 acc_d += wv * uc;
             }
         }
-        __syncthreads();
+        // no barrier here: the next plane's post-wait barrier already orders
+        // this w-phase before any write to the u ring or any stage refill
     }
     if (abort_flag) {
         if (tid == 0) {
@@ -397,13 +468,15 @@ struct nn_cg_plan {
     int nx = 0, ny = 0, nz = 0;
     int64_t G = 0;
     float op_alpha = 0, onepb = 0, invd = 0;
+    const float* D = nullptr;      // caller's cell field (HET), not owned
+    const float* invdv = nullptr;  // 1/diag per cell (HET), not owned
     float *r[2] = {}, *w[2] = {}, *s[2] = {}, *p = nullptr;
-    CUtensorMap map_r[2], map_w[2], map_s[2], map_p;
+    CUtensorMap map_r[2], map_w[2], map_s[2], map_p, map_d, map_m;
     double* scal = nullptr;
     double* partials = nullptr;
     unsigned int* ticket = nullptr;
     int* flags = nullptr;
-    int tiles = 0, init_blocks = 0;
+    int tiles = 0, init_blocks = 0, zc = 16;
     // timing of the iteration kernels
     bool timing = false;
     std::vector<cudaEvent_t> ev_a, ev_b;
@@ -432,13 +505,17 @@ void nn_cg_plan_destroy(nn_cg_plan* pl)
     nn_ctx_release(ctx);
 }
 
-// The TMA path needs rows that are a multiple of 16 bytes (nx % 4 == 0) and a
-// driver exposing cuTensorMapEncodeTiled; otherwise it reports UNSUPPORTED and
-// the caller keeps the two-kernel PCG.
-nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, nn_cg_plan** out)
+// The TMA path needs rows that are a multiple of 16 bytes (nx % 4 == 0),
+// 16-byte aligned D and 1/diag, and a driver exposing cuTensorMapEncodeTiled;
+// otherwise it reports UNSUPPORTED and the caller keeps the two-kernel PCG.
+// D and invdv (both null for constant coefficients) stay owned by the caller.
+nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, const float* D,
+                            const float* invdv, nn_cg_plan** out)
 {
     *out = nullptr;
     if (nx % 4 != 0 || nx < 4 || ny < 1 || nz < 1 || !encode_fn()) return NN_ERR_UNSUPPORTED;
+    if ((D == nullptr) != (invdv == nullptr) || ((uintptr_t)D & 15) || ((uintptr_t)invdv & 15))
+        return NN_ERR_UNSUPPORTED;
     nn_cg_plan* pl = new nn_cg_plan();
     pl->ctx = ctx;
     nn_ctx_retain(ctx);
@@ -447,10 +524,12 @@ nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, d
     pl->op_alpha = (float)alpha;
     pl->onepb = (float)(1.0 + beta);
     pl->invd = (float)(1.0 / (1.0 + beta + 6.0 * alpha));
-    pl->tiles = ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY) * ((nz + ZC - 1) / ZC);
+    pl->D = D;
+    pl->invdv = invdv;
     pl->init_blocks = nn_grid_for(ctx, pl->G, CG_THREADS, 8);
     const size_t G = (size_t)pl->G;
-    const int nparts = std::max(pl->tiles, pl->init_blocks);
+    const int max_tiles = ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY) * ((nz + 3) / 4);  // zc >= 4
+    const int nparts = std::max(max_tiles, pl->init_blocks);
     nn_status st = NN_OK;
     for (int q = 0; q < 2 && st == NN_OK; ++q) {
         st = nn_alloc(ctx, &pl->r[q], G);
@@ -468,9 +547,43 @@ nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, d
             !make_map(&pl->map_s[q], pl->s[q], nx, ny, nz, true))
             st = NN_ERR_UNSUPPORTED;
     if (st == NN_OK && !make_map(&pl->map_p, pl->p, nx, ny, nz, false)) st = NN_ERR_UNSUPPORTED;
+    if (st == NN_OK && D &&
+        (!make_map(&pl->map_d, const_cast<float*>(D), nx, ny, nz, true) ||
+         !make_map(&pl->map_m, const_cast<float*>(invdv), nx, ny, nz, true)))
+        st = NN_ERR_UNSUPPORTED;
     if (st == NN_OK) {
-        cudaError_t e = cudaFuncSetAttribute(k_cg_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        cudaError_t e = D ? cudaFuncSetAttribute(k_cg_iter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 Layout<true>::SMEM_BYTES)
+                          : cudaFuncSetAttribute(k_cg_iter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 Layout<false>::SMEM_BYTES);
         if (e != cudaSuccess) st = nn_cuda_check(ctx, e, "cudaFuncSetAttribute(k_cg_iter)");
+        // all of the unified L1/shared storage as shared memory: 8 blocks per SM
+        e = D ? cudaFuncSetAttribute(k_cg_iter<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100)
+              : cudaFuncSetAttribute(k_cg_iter<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        if (st == NN_OK && e != cudaSuccess) st = nn_cuda_check(ctx, e, "cudaFuncSetAttribute(carveout)");
+    }
+    if (st == NN_OK) {
+        // tile depth: the fewest plane steps per block over the waves the grid
+        // needs at the kernel's occupancy; each z-chunk of depth zc streams
+        // zc + 2 planes
+        int per_sm = 0;
+        cudaError_t e = D ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_iter<true>, CG_THREADS,
+                                                                          Layout<true>::SMEM_BYTES)
+                          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_iter<false>, CG_THREADS,
+                                                                          Layout<false>::SMEM_BYTES);
+        if (e != cudaSuccess) st = nn_cuda_check(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        const int64_t slots = (int64_t)std::max(per_sm, 1) * ctx->num_sms;
+        const int64_t cols = (int64_t)((nx + TX - 1) / TX) * ((ny + TY - 1) / TY);
+        int64_t best = -1;
+        for (int zc : {16, 12, 8, 6, 4}) {
+            const int64_t tiles = cols * ((nz + zc - 1) / zc);
+            const int64_t cost = ((tiles + slots - 1) / slots) * (zc + 2);
+            if (best < 0 || cost < best) {
+                best = cost;
+                pl->zc = zc;
+                pl->tiles = (int)tiles;
+            }
+        }
     }
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemsetAsync(pl->ticket, 0, sizeof(unsigned int), ctx->stream), "memset");
     if (st != NN_OK) {
@@ -492,7 +605,10 @@ static CgArgs cg_args(nn_cg_plan* pl, float* x, double rtol, int max_iter, int p
 {
     CgArgs a;
     a.nx = pl->nx; a.ny = pl->ny; a.nz = pl->nz;
+    a.zc = pl->zc;
     a.op_alpha = pl->op_alpha; a.onepb = pl->onepb; a.invd = pl->invd;
+    a.D = pl->D;
+    a.invdv = pl->invdv;
     a.p = pl->p;
     a.x = x;
     a.r_out = pl->r[parity_out];
@@ -519,9 +635,16 @@ nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, i
     if (((uintptr_t)d_x & 15) || !make_map(&map_x, d_x, pl->nx, pl->ny, pl->nz, false))
         return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_cg_run: x must be a 16-byte aligned device vector");
     CgArgs a0 = cg_args(pl, d_x, rtol, max_iter, 0);
-    k_cg_init_r<<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, d_b, d_x, pl->r[0]);
-    NN_CHECK_LAUNCH(ctx, "k_cg_init_r");
-    k_cg_init_w<<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, pl->r[0], pl->w[0], pl->s[0]);
+    const bool het = pl->D != nullptr;
+    if (het) {
+        k_cg_init_r<true><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, d_b, d_x, pl->r[0]);
+        NN_CHECK_LAUNCH(ctx, "k_cg_init_r");
+        k_cg_init_w<true><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, pl->r[0], pl->w[0], pl->s[0]);
+    } else {
+        k_cg_init_r<false><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, d_b, d_x, pl->r[0]);
+        NN_CHECK_LAUNCH(ctx, "k_cg_init_r");
+        k_cg_init_w<false><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, pl->r[0], pl->w[0], pl->s[0]);
+    }
     NN_CHECK_LAUNCH(ctx, "k_cg_init_w");
     int h_flags[4] = {0, 0, 0, 0};
     int it = 0, nchunks = 0;
@@ -543,8 +666,12 @@ nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, i
         for (int q = 0; q < chunk && it < max_iter; ++q, ++it) {
             const int pin = it & 1, pout = pin ^ 1;
             CgArgs a = cg_args(pl, d_x, rtol, max_iter, pout);
-            k_cg_iter<<<pl->tiles, CG_THREADS, SMEM_BYTES, cs>>>(pl->map_r[pin], pl->map_w[pin], pl->map_s[pin],
-                                                                 pl->map_p, map_x, a);
+            if (het)
+                k_cg_iter<true><<<pl->tiles, CG_THREADS, Layout<true>::SMEM_BYTES, cs>>>(
+                    pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], pl->map_d, pl->map_m, pl->map_p, map_x, a);
+            else
+                k_cg_iter<false><<<pl->tiles, CG_THREADS, Layout<false>::SMEM_BYTES, cs>>>(
+                    pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], pl->map_p, pl->map_p, pl->map_p, map_x, a);
             NN_CHECK_LAUNCH(ctx, "k_cg_iter");
         }
         if (pl->timing) NN_CUDA(ctx, cudaEventRecord(pl->ev_b[nchunks], cs));

@@ -35,12 +35,10 @@ inline nn_hh_dev nn_hh_to_dev(const nn_hh_params& p)
 
 __device__ __forceinline__ float nn_xexprel(float u, float emu)
 {
-    // branch (not select): warps are mostly uniform here, so only one side runs
-    if (fabsf(u) < 0.5f) {
-        const float u2 = u * u;
-        return 1.0f + u * 0.5f + u2 * (1.0f / 12.0f + u2 * (-1.0f / 720.0f + u2 * (1.0f / 30240.0f)));
-    }
-    return __fdividef(u, 1.0f - emu);
+    const float u2 = u * u;
+    const float series = 1.0f + u * 0.5f + u2 * (1.0f / 12.0f + u2 * (-1.0f / 720.0f + u2 * (1.0f / 30240.0f)));
+    const float direct = __fdividef(u, 1.0f - emu);
+    return fabsf(u) < 0.5f ? series : direct;
 }
 
 struct nn_rates { float am, bm, ah, bh, an, bn; };

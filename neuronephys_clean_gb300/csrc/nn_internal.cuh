@@ -143,7 +143,8 @@ struct nn_pcg;
 nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
                           double* relres, int* converged);
 struct nn_cg_plan;
-nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, nn_cg_plan** out);
+nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, const float* D,
+                            const float* invdv, nn_cg_plan** out);
 void nn_cg_plan_destroy(nn_cg_plan* pl);
 nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
                     double* relres, int* converged);

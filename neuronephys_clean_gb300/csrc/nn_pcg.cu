@@ -39,7 +39,7 @@ struct nn_pcg {
     std::vector<cudaEvent_t> ev_a, ev_b;
     float last_ms = 0.0f;
     int last_iters = 0;
-    // single-kernel TMA iteration (constant D, nx % 4 == 0); null: two-kernel path
+    // single-kernel TMA iteration (nx % 4 == 0, aligned D); null: two-kernel path
     nn_cg_plan* fast = nullptr;
 };
 
@@ -331,9 +331,9 @@ extern "C" nn_status nn_pcg_create(nn_ctx* ctx, int nx, int ny, int nz, double a
         ctx->launches++;
     }
     st = nn_cuda_check(ctx, cudaGetLastError(), "nn_pcg_create");
-    if (st == NN_OK && !d_Dcell && !std::getenv("NN_PCG_TWO_KERNEL")) {
-        // constant coefficients: the single-kernel TMA iteration where supported
-        nn_status fs = nn_cg_plan_create(ctx, nx, ny, nz, alpha, beta, &pc->fast);
+    if (st == NN_OK && !std::getenv("NN_PCG_TWO_KERNEL")) {
+        // the single-kernel TMA iteration where supported
+        nn_status fs = nn_cg_plan_create(ctx, nx, ny, nz, alpha, beta, d_Dcell, pc->invd, &pc->fast);
         if (fs != NN_OK && fs != NN_ERR_UNSUPPORTED) st = fs;
         ctx->last_error.clear();
     }
@@ -477,6 +477,20 @@ extern "C" nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, doub
     int conv = 0;
     NN_TRY(nn_pcg_run_best(pc, d_b, d_x, rtol, max_iter, iters, relres, &conv));
     if (!conv) return nn_fail(pc->ctx, NN_ERR_NOT_CONVERGED, "PCG did not reach rtol %g in %d iterations", rtol, max_iter);
+    return NN_OK;
+}
+
+extern "C" nn_status nn_pcg_set_kernel_timing(nn_pcg* pc, int enable)
+{
+    if (!pc) return NN_ERR_INVALID_ARG;
+    nn_pcg_set_timing(pc, enable != 0);
+    return NN_OK;
+}
+
+extern "C" nn_status nn_pcg_kernel_time(nn_pcg* pc, float* ms, int* iters)
+{
+    if (!pc || !ms || !iters) return NN_ERR_INVALID_ARG;
+    nn_pcg_last_timing(pc, ms, iters);
     return NN_OK;
 }
 

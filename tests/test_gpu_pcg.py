@@ -62,20 +62,24 @@ def test_not_converged_status(ctx):
     assert e.value.status == 4
 
 
+@pytest.mark.parametrize("hetero", [False, True])
 @pytest.mark.parametrize("shape", [(18, 20, 36), (33, 40, 64), (26, 28, 30)])
-def test_single_kernel_and_two_kernel_paths_agree(ctx, orc, shape, monkeypatch):
-    """The TMA single-kernel iteration (constant D, nx % 4 == 0; partial tiles
-    and z-chunks here) and the two-kernel path solve to the same answer."""
+def test_single_kernel_and_two_kernel_paths_agree(ctx, orc, shape, hetero, monkeypatch):
+    """The TMA single-kernel iteration (nx % 4 == 0; partial tiles and
+    z-chunks here; constant and lognormal D) and the two-kernel path solve to
+    the same answer."""
     nz, ny, nx = shape
     G = nx * ny * nz
     rng = np.random.default_rng(4)
+    D = lognormal_field(shape, rng) if hetero else None
+    dD = ctx.to_device(D.ravel()) if hetero else None
     b = rng.random(G).astype(np.float32)
     b[rng.integers(0, G, 40)] += 3.0
     alpha, beta = 5.0, 0.05
-    fast = nn.PCG(ctx, nx, ny, nz, alpha, beta)
+    fast = nn.PCG(ctx, nx, ny, nz, alpha, beta, dD)
     monkeypatch.setenv("NN_PCG_TWO_KERNEL", "1")
-    two = nn.PCG(ctx, nx, ny, nz, alpha, beta)
-    ref, _, _ = orc.pcg7(b, np.zeros(G), shape, alpha, beta, rtol=1e-12)
+    two = nn.PCG(ctx, nx, ny, nz, alpha, beta, dD)
+    ref, _, _ = orc.pcg7(b, np.zeros(G), shape, alpha, beta, D, rtol=1e-12)
     its = []
     for pc in (fast, two):
         db, dx = ctx.to_device(b), ctx.to_device(np.zeros(G, np.float32))
