@@ -45,7 +45,7 @@ WORKLOADS = {
                # iterations of the FP64 oracle PCG to 1e-6 on this seeded instance
                # (oracle.pcg7 run to convergence once; the CPU arms time a bounded
                # number of iterations and scale by this count)
-               fp64_iters=329),
+               fp64_iters=329, train_rhs=6, train_steps=400),
     "c1": dict(workload="hh_1k_er_p0.01_grid32", n=1000, kind="er", p=0.01, w_max=0.5, dmax=1, inh=0.2,
                i_lo=5.0, i_hi=15.0, grid=32, timescale=100, par_D=1.0, par_decay=0.0, total_steps=10000),
 }
@@ -232,8 +232,9 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     hh_ach = n * HH_BYTES_PER_NEURON_STEP / (kt.hh_step_ms * 1e-3) / 1e9 if kt.hh_step_ms > 0 else None
     it_ms = kt.solve_ms / kt.solve_iterations if kt.solve_iterations else None
     pcg_ach = G * PCG_BYTES_PER_CELL_ITER / (it_ms * 1e-3) / 1e9 if it_ms else None
+    # time per bench step: P neuron updates and P / timescale solves
     per_period_hh = kt.hh_step_ms * P
-    per_period_pcg = kt.solve_ms
+    per_period_pcg = kt.solve_ms * (P // wl["timescale"])
     hh_roof = {"bound": "hbm", "kernel": "k_hh_step", "achieved": hh_ach, "peak": hbm_peak, "unit": "GB/s",
                "frac": hh_ach / hbm_peak if hh_ach else None,
                "traffic": (NCU_TRAFFIC_PER_UNIT["hh_step"] * n) if NCU_TRAFFIC_PER_UNIT["hh_step"] else None,
@@ -422,11 +423,47 @@ def run_cg(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "e2e": {"value": 1e3 * statistics.mean(e2e_s), "unit": "ms", "h2d_bytes_per_step": 4 * G,
                 "d2h_bytes_per_step": 4 * G},
     }
+    if args.learned:
+        line["learned"] = learned_cg(nn, ctx, pc, wl, shape, db, ms_solve, it_mean, args)
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_cg(wl, shape, D, b, alpha, beta, wl["fp64_iters"], args.cpu_steps)
     pc.close()
     ctx.close()
     return line
+
+
+def learned_cg(nn, ctx, pc, wl, shape, db, plain_ms, plain_iters, args) -> dict:
+    """The learned two-grid preconditioner inside flexible CG on the same
+    problem: pairs from the plain solver's iterates on fresh right-hand sides,
+    Adam training on the GPU, then timed solves of the bench right-hand side."""
+    from neuronephys_clean_gb300 import fields
+    G = int(np.prod(shape))
+    lp = nn.LearnedPreconditioner(pc, seed=7)
+    t0 = time.perf_counter()
+    rhs = [fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=1000 + j) for j in range(wl["train_rhs"])]
+    pairs = lp.add_solver_pairs(rhs)
+    ctx.synchronize()
+    t_pairs = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = lp.train(wl["train_steps"], 1e-3)
+    t_train = time.perf_counter() - t0
+    dx = ctx.empty((G,), np.float32)
+    times, its = [], []
+    for _ in range(max(1, args.steps // 2)):
+        dx.zero()
+        ctx.time_begin()
+        it, rel = lp.solve(db, dx, 1e-6, 5000)
+        times.append(ctx.time_end())
+        its.append(it)
+    lp.use_network(False)
+    dx.zero()
+    it_smooth, _ = lp.solve(db, dx, 1e-6, 5000)
+    lp.close()
+    ms = statistics.mean(times)
+    return {"ms_to_tol": ms, "iterations": statistics.mean(its), "relres": rel, "vs_plain_time": ms / plain_ms,
+            "vs_plain_iterations": statistics.mean(its) / plain_iters, "iterations_without_network": it_smooth,
+            "training": {"pairs": pairs, "pair_generation_s": t_pairs, "adam_steps": wl["train_steps"],
+                         "train_s": t_train, "final_loss": loss}}
 
 
 def cpu_baseline_cg(wl, shape, D, b, alpha, beta, iterations, sample_iters) -> dict:
@@ -520,6 +557,8 @@ def main() -> None:
     ap.add_argument("--settle", type=int, default=2000, help="untimed timesteps before the warm-up")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-learned", dest="learned", action="store_false",
+                    help="CG workload: skip the learned-preconditioner comparison")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     wl = WORKLOADS[args.workload]

@@ -396,4 +396,36 @@ NN_API nn_status nn_conv3d_forward(nn_ctx* ctx, int nz, int ny, int nx, int cin,
 NN_API nn_status nn_conv3d_wgrad(nn_ctx* ctx, int nz, int ny, int nx, int cin, int cout, const void* d_x,
                                  const void* d_gy, float* d_dw, float* d_db);
 
+
+/* Learned two-grid preconditioner for the 7-point operator of an nn_pcg
+ * (grid sides multiples of 8): Jacobi smoothing on the fine grid and a
+ * coarse-grid correction by a 3-level 3D conv U-Net (16/32/64 channels, BF16
+ * tensor-core convolutions) on the 2x coarser grid, inside flexible CG.
+ * Training data: nn_learned_add_pair(r, e) with A e = r on the fine grid
+ * (e.g. r = b - A x_k and e = x* - x_k from any solve); nn_learned_train
+ * runs Adam steps over the stored pairs.  nn_learned_solve iterates to the
+ * same relative residual as nn_pcg_solve.  The nn_pcg (and its cell field)
+ * must outlive the nn_learned. */
+typedef struct nn_learned nn_learned;
+NN_API nn_status nn_learned_create(nn_pcg* pc, uint64_t seed, nn_learned** out);
+NN_API nn_status nn_learned_destroy(nn_learned* lp);
+NN_API nn_status nn_learned_add_pair(nn_learned* lp, const float* d_r, const float* d_e);
+NN_API nn_status nn_learned_train(nn_learned* lp, int steps, float lr, float* mean_loss);
+/* z = M r (device vectors of the fine grid). */
+NN_API nn_status nn_learned_apply(nn_learned* lp, const float* d_r, float* d_z);
+/* 0: leave the network out of M (smoothing only), for comparisons. */
+NN_API nn_status nn_learned_use_network(nn_learned* lp, int enable);
+NN_API nn_status nn_learned_solve(nn_learned* lp, const float* d_b, float* d_x, double rtol, int max_iter,
+                                  int* iters, double* relres);
+/* Parameters as one flat FP32 host vector (per layer w[27][cin][cout], b[cout]). */
+NN_API nn_status nn_learned_num_params(nn_learned* lp, int64_t* n);
+NN_API nn_status nn_learned_get_params(nn_learned* lp, float* h_out);
+NN_API nn_status nn_learned_set_params(nn_learned* lp, const float* h_in);
+/* Gradient check: forward + backward of the network on a coarse-grid input
+ * d_rc and target d_target; loss = 0.5 sum (y - t/s)^2 (s = rms of d_rc),
+ * parameter gradients to h_grad (flat order), network output y to d_y
+ * (both nullable).  No parameter update. */
+NN_API nn_status nn_learned_net_gradient(nn_learned* lp, const float* d_rc, const float* d_target, float* h_grad,
+                                         double* loss, float* d_y);
+
 #endif

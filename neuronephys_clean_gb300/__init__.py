@@ -31,6 +31,7 @@ __all__ = ["NNError", "Context", "DeviceArray", "HHEphys", "AtomicCoupling", "Ad
 NN_SIGNAL_COUNT, NN_SIGNAL_OUTPUT = 0, 1
 NN_DELIVERY_PUSH, NN_DELIVERY_PULL = 0, 1
 NN_NET_ER, NN_NET_GAUSS, NN_NET_BLOCK = 1, 2, 3
+NN_ERR_NOT_CONVERGED = 4
 FIELDS = {name: i for i, name in enumerate(
     ["V", "M", "H", "N", "GE", "GI", "IDRIVE", "GNA_SCALE", "X", "Y", "Z", "UPAR"])}
 # reference SoA slots (src/defines.cuh:57-78)
@@ -606,3 +607,96 @@ def conv3d_wgrad(ctx: Context, x: Activation, gy: Activation, dw: DeviceArray, d
     nz, ny, nx = x.grid
     _check(lib().nn_conv3d_wgrad(ctx.handle, nz, ny, nx, x.channels, gy.channels, x.ptr, gy.ptr, dw.ptr,
                                  None if db is None else db.ptr), ctx, "conv3d_wgrad")
+
+
+class LearnedPreconditioner:
+    """Two-grid preconditioner with a U-Net coarse correction for a PCG's
+    operator (nn_learned_*), and the flexible CG that uses it."""
+
+    def __init__(self, pcg: PCG, seed: int = 0):
+        self.pcg, self.ctx = pcg, pcg.ctx
+        self.handle = C.c_void_p()
+        _check(lib().nn_learned_create(pcg.handle, seed, C.byref(self.handle)), self.ctx, "nn_learned_create")
+
+    def add_pair(self, r: DeviceArray, e: DeviceArray) -> None:
+        _check(lib().nn_learned_add_pair(self.handle, r.ptr, e.ptr), self.ctx, "learned_add_pair")
+
+    def add_solver_pairs(self, rhs, snapshots=(0, 1, 2, 4, 8, 16, 32, 64), rtol: float = 1e-7) -> int:
+        """Training pairs from the plain solver's own iterates: for each
+        right-hand side b (host arrays), solve to rtol for x*, then for every
+        snapshot k restart from zero for k iterations and add
+        (b - A x_k, x* - x_k).  Returns the number of pairs added."""
+        pc, ctx = self.pcg, self.ctx
+        G = int(np.prod(pc.shape))
+        t = ctx.empty((G,), np.float32)
+        added = 0
+        for b in rhs:
+            b = np.ascontiguousarray(b, np.float32).ravel()
+            db = ctx.to_device(b)
+            xs = ctx.to_device(np.zeros(G, np.float32))
+            pc.solve(db, xs, rtol, 100000)
+            xstar = xs.numpy()
+            for k in snapshots:
+                xk = ctx.to_device(np.zeros(G, np.float32))
+                if k:
+                    try:
+                        pc.solve(db, xk, 1e-30, k)
+                    except NNError as e:
+                        if e.status != NN_ERR_NOT_CONVERGED:
+                            raise
+                pc.apply(xk, t)
+                self.add_pair(ctx.to_device(b - t.numpy()), ctx.to_device(xstar - xk.numpy()))
+                added += 1
+        return added
+
+    def train(self, steps: int, lr: float = 1e-3) -> float:
+        loss = C.c_float(0)
+        _check(lib().nn_learned_train(self.handle, steps, lr, C.byref(loss)), self.ctx, "learned_train")
+        return loss.value
+
+    def apply(self, r: DeviceArray, z: DeviceArray) -> None:
+        _check(lib().nn_learned_apply(self.handle, r.ptr, z.ptr), self.ctx, "learned_apply")
+
+    def use_network(self, on: bool) -> None:
+        _check(lib().nn_learned_use_network(self.handle, int(on)), self.ctx, "learned_use_network")
+
+    def solve(self, b: DeviceArray, x: DeviceArray, rtol: float = 1e-6, max_iter: int = 10000) -> tuple[int, float]:
+        it, rel = C.c_int(0), C.c_double(0)
+        _check(lib().nn_learned_solve(self.handle, b.ptr, x.ptr, rtol, max_iter, C.byref(it), C.byref(rel)),
+               self.ctx, "learned_solve")
+        return it.value, rel.value
+
+    def num_params(self) -> int:
+        n = C.c_int64()
+        _check(lib().nn_learned_num_params(self.handle, C.byref(n)), self.ctx, "learned_num_params")
+        return int(n.value)
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params(), np.float32)
+        _check(lib().nn_learned_get_params(self.handle, _ptr(out)), self.ctx, "learned_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.num_params()
+        _check(lib().nn_learned_set_params(self.handle, _ptr(p)), self.ctx, "learned_set_params")
+
+    def net_gradient(self, rc: DeviceArray, target: DeviceArray):
+        """(loss, flat parameter gradient, network output) on a coarse-grid input."""
+        g = np.empty(self.num_params(), np.float32)
+        loss = C.c_double(0)
+        y = DeviceArray(self.ctx, rc.shape, np.float32)
+        _check(lib().nn_learned_net_gradient(self.handle, rc.ptr, target.ptr, _ptr(g), C.byref(loss), y.ptr),
+               self.ctx, "learned_net_gradient")
+        return loss.value, g, y.numpy()
+
+    def close(self):
+        if self.handle:
+            lib().nn_learned_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

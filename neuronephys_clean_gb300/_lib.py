@@ -131,6 +131,17 @@ _SIGS = {
     "nn_pcg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
     "nn_pcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
+    "nn_learned_create": (c_int, [c_void_p, c_uint64, P(c_void_p)]),
+    "nn_learned_destroy": (c_int, [c_void_p]),
+    "nn_learned_add_pair": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "nn_learned_train": (c_int, [c_void_p, c_int, c_float, P(c_float)]),
+    "nn_learned_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "nn_learned_use_network": (c_int, [c_void_p, c_int]),
+    "nn_learned_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
+    "nn_learned_num_params": (c_int, [c_void_p, P(c_int64)]),
+    "nn_learned_get_params": (c_int, [c_void_p, c_void_p]),
+    "nn_learned_set_params": (c_int, [c_void_p, c_void_p]),
+    "nn_learned_net_gradient": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, P(c_double), c_void_p]),
     "nn_act_layout": (c_int, [c_int, c_int, c_int, c_int, P(c_int64), P(c_int64), P(c_int64)]),
     "nn_act_pack": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "nn_act_unpack": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),

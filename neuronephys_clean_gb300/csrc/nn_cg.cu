@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
     const int z1 = min(z0 + a.zc, a.nz);
     const int np = z1 - z0 + 2;  // planes z0-1 .. z1
     const float alpha = (float)a.scal[C_ALPHA], beta = (float)a.scal[C_BETA];
-    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny;
+    const int sy = a.nx, sz = a.nx * a.ny;  // grids below 2^31 cells (plan check)
 
     if (tid == 0) {
         abort_flag = 0;
@@ -319,8 +319,10 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
     for (int j = 0; j < np; ++j) {
         const int k = z0 - 1 + j;
         const int sidx = j % STAGES;
-        const bool ok = mbar_wait(&bars[sidx], (uint32_t)((j / STAGES) & 1));
-        if (!ok) abort_flag = 1;
+        // one thread polls the barrier (spinning threads would take issue
+        // slots from the working warps); the block barrier then publishes the
+        // landed plane to everyone
+        if (tid == 0 && !mbar_wait(&bars[sidx], (uint32_t)((j / STAGES) & 1))) abort_flag = 1;
         __syncthreads();
         if (abort_flag) break;
         const float* R = (const float*)(stage_base + sidx * STAGE_BYTES);
@@ -345,7 +347,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
             Uk[by * RX + bx - 3] = uv;
             if (HET) Dk[by * RX + bx - 3] = Dst[by * BXW + bx];
             if (in && k >= z0 && k < z1) {
-                const int64_t c = gx + sy * gy + sz * k;
+                const int c = gx + sy * gy + sz * k;
                 const float pv = mi * rv_old + beta * Ps[iy * TX + ix];
                 a.p[c] = pv;
                 a.x[c] = Xs[iy * TX + ix] + alpha * pv;
@@ -514,6 +516,7 @@ nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, d
 {
     *out = nullptr;
     if (nx % 4 != 0 || nx < 4 || ny < 1 || nz < 1 || !encode_fn()) return NN_ERR_UNSUPPORTED;
+    if ((int64_t)nx * ny * nz > INT32_MAX) return NN_ERR_UNSUPPORTED;
     if ((D == nullptr) != (invdv == nullptr) || ((uintptr_t)D & 15) || ((uintptr_t)invdv & 15))
         return NN_ERR_UNSUPPORTED;
     nn_cg_plan* pl = new nn_cg_plan();

@@ -142,6 +142,11 @@ nn_status nn_build_csc(nn_ctx* ctx, int n, int64_t nnz, const int64_t* d_row_ptr
 struct nn_pcg;
 nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
                           double* relres, int* converged);
+// operator data of a PCG object: dims, 1/diag (per cell, or the constant
+// when invd is null), the caller's cell field D (may be null)
+void nn_pcg_info(const nn_pcg* pc, nn_ctx** ctx, int* nx, int* ny, int* nz, const float** invd, float* invd_const,
+                 const float** D);
+
 struct nn_cg_plan;
 nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, const float* D,
                             const float* invdv, nn_cg_plan** out);

@@ -480,6 +480,18 @@ extern "C" nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, doub
     return NN_OK;
 }
 
+void nn_pcg_info(const nn_pcg* pc, nn_ctx** ctx, int* nx, int* ny, int* nz, const float** invd, float* invd_const,
+                 const float** D)
+{
+    *ctx = pc->ctx;
+    *nx = pc->nx;
+    *ny = pc->ny;
+    *nz = pc->nz;
+    *invd = pc->invd;
+    *invd_const = pc->inv_diag_const;
+    *D = pc->Dcell;
+}
+
 extern "C" nn_status nn_pcg_set_kernel_timing(nn_pcg* pc, int enable)
 {
     if (!pc) return NN_ERR_INVALID_ARG;

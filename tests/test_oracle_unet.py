@@ -34,3 +34,18 @@ def test_bf16_rounding():
     r = U.bf16(v)
     assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0 + 2 ** -6 and r[3] == -2.5
     assert abs(r[4] - 3.0e-3) <= 3.0e-3 * 2 ** -8
+
+
+def test_unet_backprop_matches_finite_differences():
+    rng = np.random.default_rng(2)
+    p = np.concatenate([np.concatenate([rng.standard_normal(27 * ci * co) * np.sqrt(2 / (27 * ci)),
+                                        rng.standard_normal(co) * 0.1]) for _, ci, co in U.LAYERS])
+    rc, t, ld = (rng.standard_normal((8, 8, 8)) for _ in range(3))
+    loss, g, _ = U.unet_loss_and_grad(p, rc, t, ld, rounding=False)
+    offs = np.cumsum([0] + [27 * ci * co + co for _, ci, co in U.LAYERS])
+    for l in range(len(U.LAYERS)):
+        for idx in (offs[l] + 3, offs[l + 1] - 2):   # a weight and a bias of every layer
+            p2 = p.copy()
+            p2[idx] += 1e-6
+            fd = (U.unet_loss_and_grad(p2, rc, t, ld, rounding=False)[0] - loss) / 1e-6
+            assert np.isclose(fd, g[idx], rtol=1e-4, atol=1e-6 * max(1.0, abs(loss))), (l, idx, fd, g[idx])
