@@ -40,6 +40,9 @@ WORKLOADS = {
     "c2": dict(workload="hh_1M_gauss_k100_d20_grid128", n=1_000_000, kind="gauss", k=100, sigma=0.1,
                w_mu=-1.0, w_sigma=1.0, dmax=20, inh=0.2, i_lo=6.0, i_hi=12.0, grid=128, timescale=100,
                par_D=1.0, par_decay=0.0, total_steps=1000),
+    "c3": dict(workload="hh_10M_block200_k100_d40_grid192", n=10_000_000, kind="block", k=100, n_regions=200,
+               size_sigma=1.0, density_sigma=1.0, w_mu=-1.0, w_sigma=1.0, dmax=40, inh=0.2, i_lo=6.0, i_hi=12.0,
+               grid=192, timescale=100, par_D=1.0, par_decay=0.0, total_steps=500),
     "c5": dict(workload="cg_256cube_lognormalD_s1_l8_uptake0.1", kind="cg", grid=256, sigma=1.0, corr=8.0,
                D0=1.0, uptake=0.1, dt_s=1e-3, neurons=20000, rate=2.0,
                # iterations of the FP64 oracle PCG to 1e-6 on this seeded instance
@@ -167,8 +170,9 @@ class ClockSampler:
 
 # --------------------------------------------------------------- our arm ---
 
-def build_sim(nn, ctx, wl: dict, seed: int = 1):
+def build_sim(nn, ctx, wl: dict, seed: int = 1, delivery: int = 0):
     c = nn.default_config(wl["n"])
+    c.delivery = delivery
     c.seed = seed
     c.max_delay = max(1, wl["dmax"])
     c.grid = wl["grid"]
@@ -182,6 +186,11 @@ def build_sim(nn, ctx, wl: dict, seed: int = 1):
         sp = nn.default_net_spec(nn.NN_NET_GAUSS)
         sp.k, sp.sigma, sp.w_mu, sp.w_sigma, sp.dmax = wl["k"], wl["sigma"], wl["w_mu"], wl["w_sigma"], wl["dmax"]
         sp.inh_fraction, sp.inh_random = wl["inh"], 1
+    elif wl["kind"] == "block":
+        sp = nn.default_net_spec(nn.NN_NET_BLOCK)
+        sp.k, sp.n_regions, sp.block_dmax = wl["k"], wl["n_regions"], wl["dmax"]
+        sp.region_size_sigma, sp.density_sigma = wl["size_sigma"], wl["density_sigma"]
+        sp.w_mu, sp.w_sigma, sp.inh_fraction, sp.inh_random = wl["w_mu"], wl["w_sigma"], wl["inh"], 1
     else:
         sp = nn.default_net_spec(nn.NN_NET_ER)
         sp.p, sp.w_max, sp.inh_fraction, sp.inh_random = wl["p"], wl["w_max"], wl["inh"], 0
@@ -274,7 +283,8 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "data": "synthetic (seeded counter-based generators)",
         "config": {"workload": wl["workload"], "neurons": n, "synapses": nnz, "timesteps_per_step": P,
                    "dt_ms": 0.01, "grid": wl["grid"], "delivery": "push", "parallelism": "replicas",
-                   "l2": "inputs larger than L2 (CSR 0.9 GB, ring 168 MB, state 28 MB per step)"},
+                   "l2": f"inputs larger than L2 (CSR {nnz * 9 / 1e9:.1f} GB, ring "
+                         f"{(wl['dmax'] + 1) * n * 8 / 1e6:.0f} MB, state {n * 28 / 1e6:.0f} MB per step)"},
         "synaptic_events_per_s": events / seconds if seconds else None,
         "spikes_in_timed_region": spikes,
         "cg": {"iterations_last_solve": st.iterations, "relres_last_solve": st.relres,
@@ -338,6 +348,45 @@ def cpu_baseline(sim, wl: dict, args) -> dict:
     vox = (ix + g * (iy + g * iz)).astype(np.int32)
     return cpu_baseline_sample(wl, (rp, col, w, d), state6, sim.get_field("IDRIVE"), inh, 1, args.cpu_steps, True,
                                vox)
+
+
+def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | None:
+    """Spike delivery alone on the workload's network at firing fractions
+    1e-4 .. 3e-1 of the neurons per step: push scatter (13 B per synaptic
+    event) and pull CSC gather (9 B per synapse + 8 B ring write per neuron),
+    CUDA-event timed, achieved algorithmic GB/s against the measured HBM peak."""
+    if rank != 0:
+        return None
+    import neuronephys_clean_gb300 as nn
+    ctx = nn.Context(local_rank)
+    wl = dict(wl, grid=0)
+    sim = build_sim(nn, ctx, wl, delivery=nn.NN_DELIVERY_PULL)
+    n, nnz = wl["n"], sim.nnz
+    rp = sim.get_network()[0]
+    hbm_peak, peak_kind = measured_peaks()
+    rng = np.random.default_rng(5)
+    rows = []
+    for frac in (1e-4, 3e-4, 1e-3, 3e-3, 1e-2, 3e-2, 1e-1, 3e-1):
+        cnt = max(1, int(frac * n))
+        lst = np.sort(rng.choice(n, cnt, replace=False)).astype(np.int32)
+        events = int((rp[lst + 1] - rp[lst]).sum())
+        dl = ctx.to_device(lst)
+        res = {"fraction": frac, "spikes": cnt, "events": events}
+        for mode, name, reps in ((nn.NN_DELIVERY_PUSH, "push", 20), (nn.NN_DELIVERY_PULL, "pull", 5)):
+            sim.deliver_spikes(dl, cnt, mode)
+            ctx.time_begin()
+            for _ in range(reps):
+                sim.deliver_spikes(dl, cnt, mode)
+            ms = ctx.time_end() / reps
+            nbytes = events * PUSH_BYTES_PER_EVENT if mode == nn.NN_DELIVERY_PUSH else nnz * 9 + n * 8 + n // 8
+            res[name] = {"ms": ms, "GBs": nbytes / (ms * 1e-3) / 1e9, "frac_of_peak": nbytes / (ms * 1e-3) / 1e9 / hbm_peak}
+        rows.append(res)
+    cross = next((r["fraction"] for r in rows if r["pull"]["ms"] < r["push"]["ms"]), None)
+    sim.close()
+    ctx.close()
+    return {"metric": "spike delivery GB/s vs firing fraction", "workload": wl["workload"], "neurons": n,
+            "synapses": nnz, "peak_GBs": hbm_peak, "peak_source": peak_kind, "sweep": rows,
+            "push_pull_crossover_fraction": cross}
 
 
 def cg_problem(wl: dict):
@@ -557,6 +606,8 @@ def main() -> None:
     ap.add_argument("--settle", type=int, default=2000, help="untimed timesteps before the warm-up")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--delivery-sweep", action="store_true",
+                    help="time push / pull spike delivery alone over firing fractions (one JSON line)")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="CG workload: skip the learned-preconditioner comparison")
     args = ap.parse_args()
@@ -577,7 +628,10 @@ def main() -> None:
     if rank != 0:
         build()  # no-op once rank 0 built it
     args.cpu_baseline = args.cpu_baseline and rank == 0 and world == 1
-    line = (run_cg if wl.get("kind") == "cg" else run_ours)(args, wl, dist, rank, local_rank)
+    if args.delivery_sweep:
+        line = run_delivery_sweep(args, wl, rank, local_rank)
+    else:
+        line = (run_cg if wl.get("kind") == "cg" else run_ours)(args, wl, dist, rank, local_rank)
     if line is not None:
         print(json.dumps(line), flush=True)
 

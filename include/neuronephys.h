@@ -287,6 +287,17 @@ NN_API nn_status nn_sim_init_state(nn_sim* s, float v0, float i_lo, float i_hi);
 
 /* Advance nsteps on the device (no host synchronisation). */
 NN_API nn_status nn_sim_step(nn_sim* s, int nsteps);
+/* Deliver an explicit list of spiking neurons (device int array, current
+ * step) through the network: mode NN_DELIVERY_PUSH scatters their out-edges
+ * into the delay ring as the step kernel does; NN_DELIVERY_PULL (simulation
+ * created in pull mode) sets them in the current step's bitmap and runs the
+ * CSC gather of the next step's input, for measuring the gather (the next
+ * nn_sim_step recomputes that input from the simulation's own spikes).  The
+ * reference's counterpart is
+ * AtomicCoupling::operator() given a firing list (src/coupling.cu:103-141);
+ * here it serves callers with spikes from elsewhere and measurement of the
+ * delivery path alone.  Asynchronous on the context stream. */
+NN_API nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int count, int mode);
 /* End-to-end call: copy the state (6*n floats: V,m,h,n,ge,gi planes) from
  * host memory, advance nsteps, copy the state back and return the number of
  * spikes emitted. */

@@ -475,6 +475,9 @@ class Simulation:
     def step(self, nsteps: int = 1) -> None:
         _check(lib().nn_sim_step(self.handle, nsteps), self.ctx, "step")
 
+    def deliver_spikes(self, d_list: "DeviceArray", count: int, mode: int = NN_DELIVERY_PUSH) -> None:
+        _check(lib().nn_sim_deliver_spikes(self.handle, d_list.ptr, count, mode), self.ctx, "sim_deliver_spikes")
+
     def run_host(self, state_in: np.ndarray, nsteps: int, state_out: np.ndarray) -> int:
         sp = C.c_int64()
         _check(lib().nn_sim_run_host(self.handle, _ptr(state_in), nsteps, _ptr(state_out), C.byref(sp)), self.ctx,

@@ -131,6 +131,7 @@ _SIGS = {
     "nn_pcg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
     "nn_pcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
+    "nn_sim_deliver_spikes": (c_int, [c_void_p, c_void_p, c_int, c_int]),
     "nn_learned_create": (c_int, [c_void_p, c_uint64, P(c_void_p)]),
     "nn_learned_destroy": (c_int, [c_void_p]),
     "nn_learned_add_pair": (c_int, [c_void_p, c_void_p, c_void_p]),

@@ -341,6 +341,41 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
     }
 }
 
+// Push delivery of an explicit spike list at the current step: the same
+// scatter as the fused neuron update (a warp per spike, lanes over its
+// out-edges, red.global.add into ring slot (t + d) % D), for callers that
+// produce spikes elsewhere and for timing the delivery path on its own.
+__global__ void __launch_bounds__(DELIV_THREADS) k_deliver_list(const int* list, int count, const int64_t* row_ptr,
+                                                                const int32_t* col, const float* weight,
+                                                                const uint8_t* delay, const uint8_t* is_inh,
+                                                                float* ring, const unsigned long long* base,
+                                                                int n_pad, int D)
+{
+    const int slot = (int)(*base % (uint64_t)D);
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (DELIV_THREADS / 32) + (threadIdx.x >> 5);
+    const int nwarps = gridDim.x * (DELIV_THREADS / 32);
+    for (int q = gw; q < count; q += nwarps) {
+        const int j = list[q];
+        const int chn = is_inh[j] ? 1 : 0;
+        const int64_t beg = row_ptr[j], end = row_ptr[j + 1];
+        for (int64_t e = beg + lane; e < end; e += 32) {
+            int sl = slot + (int)delay[e];
+            if (sl >= D) sl -= D;
+            atomicAdd(ring + 2 * ((size_t)sl * n_pad + col[e]) + chn, weight[e]);
+        }
+    }
+}
+
+// spike bitmap of the current step from a list (pull delivery)
+__global__ void k_list_bitmap(const int* list, int count, uint32_t* bitmap, const unsigned long long* base, int D,
+                              int words)
+{
+    uint32_t* bm = bitmap + (size_t)(*base % (uint64_t)D) * words;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < count; q += gridDim.x * blockDim.x)
+        atomicOr(bm + (list[q] >> 5), 1u << (list[q] & 31));
+}
+
 // paracrine: b = u + src ; src = 0
 __global__ void k_par_rhs(const float* u, float* src, float* b, int64_t G)
 {
@@ -1283,6 +1318,35 @@ extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
         }
         if (s->grid > 0 && (s->host_step % s->cfg.timescale) == 0) NN_TRY(paracrine_solve(s));
     }
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int count, int mode)
+{
+    if (!s || (count > 0 && !d_list) || count < 0 || count > s->n) return NN_ERR_INVALID_ARG;
+    if (!s->row_ptr) return nn_fail(s->ctx, NN_ERR_INVALID_ARG, "nn_sim_deliver_spikes: no network");
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    if (mode == NN_DELIVERY_PUSH) {
+        if (count == 0) return NN_OK;
+        k_deliver_list<<<nn_grid_for(ctx, (int64_t)count * 32, DELIV_THREADS, 16), DELIV_THREADS, 0, cs>>>(
+            d_list, count, s->row_ptr, s->col, s->weight, s->delay, s->is_inh, reinterpret_cast<float*>(s->ring),
+            s->step, s->n_pad, s->D);
+        NN_CHECK_LAUNCH(ctx, "k_deliver_list");
+        return NN_OK;
+    }
+    if (mode != NN_DELIVERY_PULL) return NN_ERR_INVALID_ARG;
+    if (!s->bitmap || !s->col_ptr)
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_deliver_spikes: pull needs a simulation in pull mode");
+    NN_CUDA(ctx, cudaMemsetAsync(s->bitmap, 0, sizeof(uint32_t) * (size_t)s->D * s->words, cs));
+    if (count > 0) {
+        k_list_bitmap<<<nn_grid_for(ctx, count, 256, 4), 256, 0, cs>>>(d_list, count, s->bitmap, s->step, s->D,
+                                                                       s->words);
+        NN_CHECK_LAUNCH(ctx, "k_list_bitmap");
+    }
+    PullArgs d = pull_args(s, 0);
+    k_deliver_pull<<<nn_grid_for(ctx, (int64_t)s->n * 32, DELIV_THREADS, 8), DELIV_THREADS, 0, cs>>>(d);
+    NN_CHECK_LAUNCH(ctx, "k_deliver_pull");
     return NN_OK;
 }
 

@@ -64,6 +64,8 @@ _SIGS = {
     "orc_csr_to_csc": (None, [P(OrcCSR), V, V, V, V, V]),
     "orc_gen_er": (None, [C.c_int, C.c_double, C.c_float, C.c_uint64, P(OrcCSR)]),
     "orc_gauss_table": (None, [C.c_double, V]),
+    "orc_gen_block": (None, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
+                             C.c_uint64, C.c_void_p]),
     "orc_gen_gauss": (None, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_uint64,
                              P(OrcCSR)]),
     "orc_lattice_positions": (None, [C.c_int, C.c_uint64, V, V, V]),
@@ -231,6 +233,17 @@ def gen_gauss(n: int, k: int, sigma: float, mu: float, sg: float, dmax: int, see
     d = np.zeros(n * k, np.uint8)
     s = OrcCSR(n, 0, rp.ctypes.data, col.ctypes.data, w.ctypes.data, d.ctypes.data)
     lib().orc_gen_gauss(n, k, sigma, mu, sg, dmax, seed, C.byref(s))
+    return CSR(rp, col, w, d)
+
+
+def gen_block(n: int, k: int, R: int, size_sigma: float, density_sigma: float, dmax: int, mu: float, sg: float,
+              seed: int) -> CSR:
+    rp = np.zeros(n + 1, np.int64)
+    col = np.zeros(n * k, np.int32)
+    w = np.zeros(n * k, np.float32)
+    d = np.zeros(n * k, np.uint8)
+    s = OrcCSR(n, 0, rp.ctypes.data, col.ctypes.data, w.ctypes.data, d.ctypes.data)
+    lib().orc_gen_block(n, k, R, size_sigma, density_sigma, dmax, mu, sg, seed, C.byref(s))
     return CSR(rp, col, w, d)
 
 

@@ -459,7 +459,7 @@ void orc_csr_to_csc(const orc_csr* a, int64_t* col_ptr, int32_t* src, float* w, 
 }
 
 /* Purposes of the counter-based streams (shared with the CUDA generators). */
-enum { P_NOISE = 1, P_DRIVE = 2, P_POS = 3, P_ER = 4, P_GAUSS = 5, P_WEIGHT = 6, P_TYPE = 7 };
+enum { P_NOISE = 1, P_DRIVE = 2, P_POS = 3, P_ER = 4, P_GAUSS = 5, P_WEIGHT = 6, P_TYPE = 7, P_BLOCK = 8, P_REGION = 9 };
 
 void orc_gen_er(int n, double p, float wmax, uint64_t seed, orc_csr* out)
 {
@@ -568,6 +568,140 @@ void orc_gen_gauss(int n, int k, double sigma, double w_mu, double w_sigma, int 
             out->delay[pos] = (uint8_t)(1u + (uint32_t)(((uint64_t)rw[2] * (uint64_t)dmax) >> 32));
         }
     }
+}
+
+/* Region-block generator of the 10M-neuron workload (the library's own
+ * generator; no reference counterpart).  Regions: lognormal(0, size_sigma)
+ * size weights and uniform centroids from Philox(seed; r, 0|1, 0, REGION);
+ * sizes 1 + largest-remainder shares of n - R.  Block densities: row r over
+ * target regions t, lognormal(0, density_sigma) x size[t], as cumulative
+ * 32-bit thresholds; delay 1 + (dmax - 1) * centroid distance / max distance,
+ * rounded.  Synapse e of neuron i: target region by the first threshold above
+ * u.x of Philox(seed; i, e, attempt, BLOCK), target neuron uniform in it
+ * (u.y), redrawn if it is i (64 attempts, then i + 1); weight as in
+ * orc_gen_gauss; delay from the region pair. */
+void orc_block_tables(int n, int R, double size_sigma, double density_sigma, int dmax, uint64_t seed,
+                      int* start, int* size, uint32_t* cum, uint8_t* pdelay)
+{
+    double* w = (double*)malloc(sizeof(double) * R * 5);
+    double *cx = w + R, *cy = w + 2 * R, *cz = w + 3 * R, *fr = w + 4 * R;
+    int* order = (int*)malloc(sizeof(int) * R);
+    double sw = 0.0;
+    for (int r = 0; r < R; ++r) {
+        uint32_t u[4], v[4];
+        philox(seed, (uint32_t)r, 0u, 0u, P_REGION, u);
+        const double u1 = u01_open_closed(u[0]), u2 = u01_closed_open(u[1]);
+        const double z = sqrt(-2.0 * log(u1)) * cos(6.283185307179586476925 * u2);
+        w[r] = exp(size_sigma * z);
+        sw += w[r];
+        cx[r] = u01_closed_open(u[2]);
+        philox(seed, (uint32_t)r, 1u, 0u, P_REGION, v);
+        cy[r] = u01_closed_open(v[0]);
+        cz[r] = u01_closed_open(v[1]);
+    }
+    const int left = n - R;
+    int assigned = 0;
+    for (int r = 0; r < R; ++r) {
+        const double want = left * w[r] / sw;
+        const int fl = (int)floor(want);
+        size[r] = 1 + fl;
+        assigned += fl;
+        fr[r] = want - fl;
+        order[r] = r;
+    }
+    /* stable sort by descending remainder (insertion sort; R is small) */
+    for (int a = 1; a < R; ++a) {
+        const int v = order[a];
+        int b = a - 1;
+        while (b >= 0 && fr[order[b]] < fr[v]) {
+            order[b + 1] = order[b];
+            --b;
+        }
+        order[b + 1] = v;
+    }
+    for (int q = 0; q < left - assigned; ++q) size[order[q]] += 1;
+    start[0] = 0;
+    for (int r = 1; r < R; ++r) start[r] = start[r - 1] + size[r - 1];
+    double dmax_dist = 0.0;
+    for (int r = 0; r < R; ++r)
+        for (int t = 0; t < R; ++t) {
+            const double d = sqrt((cx[r] - cx[t]) * (cx[r] - cx[t]) + (cy[r] - cy[t]) * (cy[r] - cy[t]) +
+                                  (cz[r] - cz[t]) * (cz[r] - cz[t]));
+            if (d > dmax_dist) dmax_dist = d;
+        }
+    double* row = (double*)malloc(sizeof(double) * R);
+    for (int r = 0; r < R; ++r) {
+        double s = 0.0;
+        for (int t = 0; t < R; ++t) {
+            uint32_t u[4];
+            philox(seed, (uint32_t)r, (uint32_t)t, 0u, P_BLOCK + 16u, u);
+            const double u1 = u01_open_closed(u[0]), u2 = u01_closed_open(u[1]);
+            const double z = sqrt(-2.0 * log(u1)) * cos(6.283185307179586476925 * u2);
+            row[t] = exp(density_sigma * z) * (double)size[t];
+            s += row[t];
+            const double dist = sqrt((cx[r] - cx[t]) * (cx[r] - cx[t]) + (cy[r] - cy[t]) * (cy[r] - cy[t]) +
+                                     (cz[r] - cz[t]) * (cz[r] - cz[t]));
+            const double dd = dmax_dist > 0 ? 1.0 + (dmax - 1) * dist / dmax_dist : 1.0;
+            long q = lround(dd);
+            if (q < 1) q = 1;
+            if (q > dmax) q = dmax;
+            pdelay[(size_t)r * R + t] = (uint8_t)q;
+        }
+        double acc = 0.0;
+        for (int t = 0; t < R; ++t) {
+            acc += row[t];
+            double th = floor(acc / s * 4294967296.0);
+            if (th > 4294967295.0) th = 4294967295.0;
+            cum[(size_t)r * R + t] = t == R - 1 ? 0xffffffffu : (uint32_t)th;
+        }
+    }
+    free(row);
+    free(order);
+    free(w);
+}
+
+void orc_gen_block(int n, int k, int R, double size_sigma, double density_sigma, int dmax, double w_mu,
+                   double w_sigma, uint64_t seed, orc_csr* out)
+{
+    int* start = (int*)malloc(sizeof(int) * R);
+    int* size = (int*)malloc(sizeof(int) * R);
+    uint32_t* cum = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)R * R);
+    uint8_t* pdelay = (uint8_t*)malloc((size_t)R * R);
+    orc_block_tables(n, R, size_sigma, density_sigma, dmax, seed, start, size, cum, pdelay);
+    out->nnz = (int64_t)n * k;
+    for (int i = 0; i <= n; ++i) out->row_ptr[i] = (int64_t)i * k;
+    int r_of = 0;
+    for (int i = 0; i < n; ++i) {
+        while (r_of + 1 < R && i >= start[r_of + 1]) ++r_of;
+        for (int e = 0; e < k; ++e) {
+            int tgt = (i + 1) % n, sreg = r_of;
+            for (int a = 0; a < 64; ++a) {
+                uint32_t u[4];
+                philox(seed, (uint32_t)i, (uint32_t)e, (uint32_t)a, P_BLOCK, u);
+                const uint32_t* row = cum + (size_t)r_of * R;
+                int lo = 0, hi = R - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (row[mid] > u[0]) hi = mid; else lo = mid + 1;
+                }
+                sreg = lo;
+                const int off = (int)(((uint64_t)u[1] * (uint64_t)size[sreg]) >> 32);
+                const int cand = start[sreg] + off;
+                if (cand == i) continue;
+                tgt = cand;
+                break;
+            }
+            uint32_t rw[4];
+            philox(seed, (uint32_t)i, (uint32_t)e, 0u, P_WEIGHT, rw);
+            const double u1 = u01_open_closed(rw[0]), u2 = u01_closed_open(rw[1]);
+            const double zz = sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2);
+            const int64_t pos = (int64_t)i * k + e;
+            out->col[pos] = tgt;
+            out->weight[pos] = (float)exp(w_mu + w_sigma * zz);
+            out->delay[pos] = pdelay[(size_t)r_of * R + sreg];
+        }
+    }
+    free(start); free(size); free(cum); free(pdelay);
 }
 
 int orc_sim_step(orc_sim* s, uint64_t step, int32_t* spikes)

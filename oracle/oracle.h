@@ -157,6 +157,10 @@ void orc_gen_er(int n, double p, float wmax, uint64_t seed, orc_csr* out);
  * lattice offsets from a discretised Gaussian table (sigma in lattice units),
  * lognormal(mu, s) weights, delay 1 + floor(u * dmax). */
 void orc_gauss_table(double sigma_sites, int16_t* table4096);
+void orc_block_tables(int n, int R, double size_sigma, double density_sigma, int dmax, uint64_t seed,
+                      int* start, int* size, uint32_t* cum, uint8_t* pdelay);
+void orc_gen_block(int n, int k, int R, double size_sigma, double density_sigma, int dmax, double w_mu,
+                   double w_sigma, uint64_t seed, orc_csr* out);
 void orc_gen_gauss(int n, int k, double sigma, double w_mu, double w_sigma, int dmax,
                    uint64_t seed, orc_csr* out);
 void orc_lattice_positions(int n, uint64_t seed, float* x, float* y, float* z);

@@ -67,6 +67,23 @@ def test_block_generator_structure(ctx):
     assert d.min() >= 1 and d.max() <= 40 and np.all(w > 0)
 
 
+def test_block_generator_bit_exact(ctx, orc):
+    """Region-block model (the 10M-neuron workload's generator) against the
+    oracle: targets and delays bit-exact, lognormal weights within 1 ulp."""
+    n, k, R, seed = 12000, 40, 60, 17
+    s = _sim(ctx, n, max_delay=40, seed=seed)
+    spec = nn.default_net_spec(nn.NN_NET_BLOCK)
+    spec.k, spec.n_regions, spec.block_dmax, spec.w_mu, spec.w_sigma = k, R, 40, -1.0, 1.0
+    s.generate_network(spec)
+    rp, col, w, d, _ = s.get_network()
+    ref = orc.gen_block(n, k, R, spec.region_size_sigma, spec.density_sigma, 40, -1.0, 1.0, seed)
+    assert np.array_equal(rp, ref.row_ptr)
+    assert np.array_equal(col, ref.col)
+    assert np.array_equal(d, ref.delay)
+    np.testing.assert_array_max_ulp(w, ref.weight, maxulp=1)
+    assert len(np.unique(d)) > 10
+
+
 @pytest.mark.parametrize("kind", ["er", "gauss"])
 def test_csc_bit_exact(ctx, orc, kind):
     if kind == "er":

@@ -186,3 +186,39 @@ def test_invalid_network_rejected(ctx):
     with pytest.raises(nn.NNError):
         s.set_network(np.array([0, 1] + [1] * 9, np.int64), np.array([3], np.int32),
                       np.array([0.1], np.float32), np.array([2], np.uint8))  # delay > max_delay
+
+
+def test_deliver_spike_list(ctx):
+    """An explicit spike list pushed through the network reaches g_e / g_i of
+    the targets one step later: the sum of the excitatory / inhibitory weights
+    onto each neuron, decayed by one RK4 step of dg/dt = -g/tau (1e-5
+    relative; FP32 sums in different orders).  The pull form runs on a
+    pull-mode simulation."""
+    n, mode = 3000, 0
+    c = nn.default_config(n)
+    c.seed, c.delivery, c.max_delay, c.raster_capacity = 4, mode, 1, 0
+    c.hp.noise_sigma = 0.0
+    s = nn.Simulation(ctx, c)
+    spec = nn.default_net_spec(nn.NN_NET_ER)
+    spec.p, spec.w_max, spec.inh_fraction = 0.02, 0.5, 0.2
+    s.generate_network(spec)
+    s.init_state(-65.0, 0.0, 0.0)           # at rest, no drive, no noise: no spikes of its own
+    rp, col, w, d, inh = s.get_network()
+    lst = np.sort(np.random.default_rng(1).choice(n, 150, replace=False)).astype(np.int32)
+    s.deliver_spikes(ctx.to_device(lst), len(lst), mode)
+    s.step(2)                               # step 0 reads slot 0, step 1 reads the delivered slot 1
+    assert s.counters()[1] == 0
+    ge = np.zeros(n)
+    gi = np.zeros(n)
+    for i in lst:
+        tgt, wt = col[rp[i]:rp[i + 1]], w[rp[i]:rp[i + 1]].astype(np.float64)
+        np.add.at(gi if inh[i] else ge, tgt, wt)
+    h = c.hp.dt / c.hp.tau_exc
+    decay = 1 - h + h * h / 2 - h ** 3 / 6 + h ** 4 / 24
+    np.testing.assert_allclose(s.get_field("GE"), ge * decay, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(s.get_field("GI"), gi * decay, rtol=1e-5, atol=1e-6)
+    c.delivery = 1
+    sp = nn.Simulation(ctx, c)
+    sp.generate_network(spec)
+    sp.deliver_spikes(ctx.to_device(lst), len(lst), 1)
+    ctx.synchronize()

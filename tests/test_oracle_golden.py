@@ -48,3 +48,15 @@ def test_minstd_and_uniform_int_known_answers(orc):
     for _ in range(10000):
         orc.lib().orc_minstd_next(C.byref(s))
     assert s.value == 1043618065
+
+
+def test_block_oracle_structure(orc):
+    """The oracle's region-block generator: fixed out-degree, no self-loops,
+    delays in range, region sizes summing to n."""
+    n, k, R = 3000, 20, 25
+    c = orc.gen_block(n, k, R, 1.0, 1.0, 40, -1.0, 1.0, 3)
+    src = np.repeat(np.arange(n), k)
+    assert np.array_equal(c.row_ptr, np.arange(n + 1) * k)
+    assert c.col.min() >= 0 and c.col.max() < n and not np.any(c.col == src)
+    assert c.delay.min() >= 1 and c.delay.max() <= 40
+    assert np.all(c.weight > 0)
