@@ -439,4 +439,70 @@ NN_API nn_status nn_learned_set_params(nn_learned* lp, const float* h_in);
 NN_API nn_status nn_learned_net_gradient(nn_learned* lp, const float* d_rc, const float* d_target, float* h_grad,
                                          double* loss, float* d_y);
 
+
+/* ==========================================================================
+ * Consumers of the step (reference: ElectrodeNet, SynchronyNet, Hebbian).
+ * ========================================================================== */
+/* ElectrodeNet(regions_inds, regions_offsets) (src/electrode_net.cuh:8-24,
+ * src_wholebrain/electrode_net.cuh:9-29): regions as index lists. */
+typedef struct nn_electrodes nn_electrodes;
+NN_API nn_status nn_electrodes_create(nn_ctx* ctx, const int* h_indices, const int* h_offsets, int n_regions,
+                                      nn_electrodes** out);
+NN_API nn_status nn_electrodes_destroy(nn_electrodes* e);
+/* DoElectrodeMeasurements(V, is_firing) (src_wholebrain/electrode_net.cu:33-48):
+ * per-region mean of d_V and, if d_is_firing (int per neuron) is given, the
+ * firing count; copied to h_avg / h_firing when those are non-NULL. */
+NN_API nn_status nn_electrodes_measure(nn_electrodes* e, const float* d_V, const int* d_is_firing, float* h_avg,
+                                       int* h_firing);
+/* MeasureAverageEntireNetwork(V, N) (src/electrode_net.cu:46-49). */
+NN_API nn_status nn_measure_average(nn_ctx* ctx, const float* d_V, int n, float* out);
+/* SynchronyNet (src_wholebrain/electrode_net.cuh:33-60, .cu:56-124). */
+typedef struct nn_synchrony nn_synchrony;
+NN_API nn_status nn_synchrony_create(nn_ctx* ctx, const int* h_region_inds, int n_inds, const int* h_sub_counts,
+                                     int n_sub, nn_synchrony** out);
+NN_API nn_status nn_synchrony_destroy(nn_synchrony* s);
+NN_API nn_status nn_synchrony_measure(nn_synchrony* s, const float* d_V);  /* MeasureVariances */
+NN_API nn_status nn_synchrony_get(nn_synchrony* s, double* h_chi);        /* GetSynchronyMeasures */
+/* Hebbian(window, inc, Nconns) (src_wholebrain/hebbian.cuh:3-23). */
+typedef struct nn_hebbian nn_hebbian;
+NN_API nn_status nn_hebbian_create(nn_ctx* ctx, int window, float inc, int64_t nconns, int n_neurons,
+                                   nn_hebbian** out);
+NN_API nn_status nn_hebbian_destroy(nn_hebbian* h);
+/* UpdateWeights(connectivity, is_firing, firing_inds) (src_wholebrain/hebbian.cu:53-69):
+ * CSR (row = presynaptic) indices / offsets, int is_firing per neuron, the
+ * list of num_firing neurons whose synapse timers are set, weights updated
+ * in place.  Asynchronous on the context stream. */
+NN_API nn_status nn_hebbian_update(nn_hebbian* h, const int* d_indices, const int* d_offsets,
+                                   const int* d_is_firing, const int* d_firing_inds, int num_firing,
+                                   float* d_weights);
+NN_API nn_status nn_hebbian_timers(nn_hebbian* h, int* h_timers);
+
+
+/* ==========================================================================
+ * On-disk inputs (reference: FileNetwork, src/network_factory.cu:154-211;
+ * FileMorphology, src/morphology.cpp:260-330).  The reference reads HDF5
+ * datasets /row_ptr, /col_idx (int32) and /x, /y, /z (float32); with no HDF5
+ * library here the same datasets travel in a raw little-endian container:
+ *   "NNCSR001" | int64 n_rows | int64 nnz | int32 row_ptr[n_rows+1] | int32 col_idx[nnz]
+ *   "NNPOS001" | int64 n | float32 x[n] | float32 y[n] | float32 z[n]
+ * The *_read calls return the sizes when the arrays are NULL.
+ * ========================================================================== */
+NN_API nn_status nn_net_file_write(const char* path, int64_t n_rows, int64_t nnz, const int32_t* h_row_ptr,
+                                   const int32_t* h_col);
+NN_API nn_status nn_net_file_read(const char* path, int64_t* n_rows, int64_t* nnz, int32_t* h_row_ptr,
+                                  int32_t* h_col);
+/* FileNetwork::Generate(N): keep rows i * sparsity (sparsity = n_rows / N)
+ * and their targets divisible by sparsity, renumbered target / sparsity, in
+ * file order.  Device arrays in and out; d_out_col needs the input nnz. */
+NN_API nn_status nn_net_subsample(nn_ctx* ctx, const int32_t* d_row_ptr, const int32_t* d_col, int64_t n_rows,
+                                  int N, int64_t* d_out_row_ptr, int32_t* d_out_col, int64_t* out_nnz);
+NN_API nn_status nn_positions_file_write(const char* path, int64_t n, const float* h_x, const float* h_y,
+                                         const float* h_z);
+NN_API nn_status nn_positions_file_read(const char* path, int64_t* n, float* h_x, float* h_y, float* h_z);
+/* FileMorphology::Generate(N): points stride * i (stride = n / N), mapped by
+ * the bounding box of all n points onto [-1, 1] (FP32, the reference's
+ * operation order). */
+NN_API nn_status nn_positions_subsample(nn_ctx* ctx, const float* d_x, const float* d_y, const float* d_z,
+                                        int64_t n, int N, float* d_ox, float* d_oy, float* d_oz);
+
 #endif

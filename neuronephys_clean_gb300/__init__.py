@@ -703,3 +703,179 @@ class LearnedPreconditioner:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------- consumers of the step --
+
+class ElectrodeNet:
+    """Mirror of the reference's ElectrodeNet: regions as index lists."""
+
+    def __init__(self, ctx: Context, regions_inds, regions_offsets):
+        self.ctx = ctx
+        idx = np.ascontiguousarray(regions_inds, np.int32)
+        off = np.ascontiguousarray(regions_offsets, np.int32)
+        self.n_regions = len(off) - 1
+        self.handle = C.c_void_p()
+        _check(lib().nn_electrodes_create(ctx.handle, _ptr(idx), _ptr(off), self.n_regions, C.byref(self.handle)),
+               ctx, "nn_electrodes_create")
+
+    def do_electrode_measurements(self, V: DeviceArray, is_firing: DeviceArray | None = None):
+        avg = np.empty(self.n_regions, np.float32)
+        fir = np.empty(self.n_regions, np.int32)
+        _check(lib().nn_electrodes_measure(self.handle, V.ptr, None if is_firing is None else is_firing.ptr,
+                                           _ptr(avg), _ptr(fir)), self.ctx, "electrodes_measure")
+        return avg, (fir if is_firing is not None else None)
+
+    @staticmethod
+    def measure_average_entire_network(ctx: Context, V: DeviceArray, n: int) -> float:
+        out = C.c_float()
+        _check(lib().nn_measure_average(ctx.handle, V.ptr, n, C.byref(out)), ctx, "measure_average")
+        return out.value
+
+    def close(self):
+        if self.handle:
+            lib().nn_electrodes_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SynchronyNet:
+    def __init__(self, ctx: Context, region_inds, sub_sample_counts):
+        self.ctx = ctx
+        idx = np.ascontiguousarray(region_inds, np.int32)
+        sub = np.ascontiguousarray(sub_sample_counts, np.int32)
+        self.n_sub = len(sub)
+        self.handle = C.c_void_p()
+        _check(lib().nn_synchrony_create(ctx.handle, _ptr(idx), len(idx), _ptr(sub), len(sub), C.byref(self.handle)),
+               ctx, "nn_synchrony_create")
+
+    def measure_variances(self, V: DeviceArray) -> None:
+        _check(lib().nn_synchrony_measure(self.handle, V.ptr), self.ctx, "synchrony_measure")
+
+    def get_synchrony_measures(self) -> np.ndarray:
+        out = np.empty(self.n_sub, np.float64)
+        _check(lib().nn_synchrony_get(self.handle, _ptr(out)), self.ctx, "synchrony_get")
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().nn_synchrony_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Hebbian:
+    """Mirror of the reference's Hebbian learner (timer window, increment)."""
+
+    def __init__(self, ctx: Context, window_duration: int, heb_inc: float, nconns: int, n_neurons: int):
+        self.ctx, self.nconns = ctx, nconns
+        self.handle = C.c_void_p()
+        _check(lib().nn_hebbian_create(ctx.handle, window_duration, heb_inc, nconns, n_neurons, C.byref(self.handle)),
+               ctx, "nn_hebbian_create")
+
+    def update_weights(self, indices: DeviceArray, offsets: DeviceArray, weights: DeviceArray, is_firing: DeviceArray,
+                       firing_inds: DeviceArray | None, num_firing: int) -> None:
+        _check(lib().nn_hebbian_update(self.handle, indices.ptr, offsets.ptr, is_firing.ptr,
+                                       None if firing_inds is None else firing_inds.ptr, num_firing, weights.ptr),
+               self.ctx, "hebbian_update")
+
+    def timers(self) -> np.ndarray:
+        out = np.empty(self.nconns, np.int32)
+        _check(lib().nn_hebbian_timers(self.handle, _ptr(out)), self.ctx, "hebbian_timers")
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().nn_hebbian_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --------------------------------------------------------- on-disk inputs --
+
+def write_network_file(path: str, row_ptr, col) -> None:
+    rp = np.ascontiguousarray(row_ptr, np.int32)
+    c = np.ascontiguousarray(col, np.int32)
+    _check(lib().nn_net_file_write(str(path).encode(), len(rp) - 1, len(c), _ptr(rp), _ptr(c)), None,
+           "nn_net_file_write")
+
+
+def read_network_file(path: str) -> tuple[np.ndarray, np.ndarray]:
+    nr, nz = C.c_int64(), C.c_int64()
+    _check(lib().nn_net_file_read(str(path).encode(), C.byref(nr), C.byref(nz), None, None), None, "nn_net_file_read")
+    rp = np.empty(nr.value + 1, np.int32)
+    col = np.empty(nz.value, np.int32)
+    _check(lib().nn_net_file_read(str(path).encode(), C.byref(nr), C.byref(nz), _ptr(rp), _ptr(col)), None,
+           "nn_net_file_read")
+    return rp, col
+
+
+class FileNetwork:
+    """Mirror of the reference's FileNetwork: connectivity from a file,
+    sub-sampled to N neurons on the device."""
+
+    def __init__(self, path: str):
+        self.path = str(path)
+        self.row_ptr = self.col = None
+
+    def generate(self, ctx: Context, N: int) -> bool:
+        try:
+            rp, col = read_network_file(self.path)
+        except NNError:
+            return False
+        if N > len(rp) - 1:
+            return False
+        drp, dcol = ctx.to_device(rp), ctx.to_device(col)
+        orp = DeviceArray(ctx, (N + 1,), np.int64)
+        ocol = DeviceArray(ctx, (max(len(col), 1),), np.int32)
+        nnz = C.c_int64()
+        _check(lib().nn_net_subsample(ctx.handle, drp.ptr, dcol.ptr, len(rp) - 1, N, orp.ptr, ocol.ptr, C.byref(nnz)),
+               ctx, "nn_net_subsample")
+        self.row_ptr = orp.numpy()
+        self.col = ocol.numpy()[:nnz.value]
+        return True
+
+
+def write_positions_file(path: str, x, y, z) -> None:
+    a = [np.ascontiguousarray(v, np.float32) for v in (x, y, z)]
+    _check(lib().nn_positions_file_write(str(path).encode(), len(a[0]), _ptr(a[0]), _ptr(a[1]), _ptr(a[2])), None,
+           "nn_positions_file_write")
+
+
+class FileMorphology:
+    """Mirror of the reference's FileMorphology: N positions in [-1, 1]."""
+
+    def __init__(self, path: str):
+        self.path = str(path)
+        self.positions = None
+
+    def generate(self, ctx: Context, N: int) -> bool:
+        n = C.c_int64()
+        if lib().nn_positions_file_read(self.path.encode(), C.byref(n), None, None, None) != 0:
+            return False
+        if N > n.value:
+            return False
+        xyz = [np.empty(n.value, np.float32) for _ in range(3)]
+        _check(lib().nn_positions_file_read(self.path.encode(), C.byref(n), *[_ptr(v) for v in xyz]), None,
+               "nn_positions_file_read")
+        d = [ctx.to_device(v) for v in xyz]
+        o = [DeviceArray(ctx, (N,), np.float32) for _ in range(3)]
+        _check(lib().nn_positions_subsample(ctx.handle, d[0].ptr, d[1].ptr, d[2].ptr, n.value, N, o[0].ptr, o[1].ptr,
+                                            o[2].ptr), ctx, "nn_positions_subsample")
+        self.positions = np.stack([v.numpy() for v in o], axis=1)
+        return True

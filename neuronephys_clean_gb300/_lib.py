@@ -132,6 +132,25 @@ _SIGS = {
     "nn_pcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
     "nn_sim_deliver_spikes": (c_int, [c_void_p, c_void_p, c_int, c_int]),
+    "nn_net_file_write": (c_int, [C.c_char_p, c_int64, c_int64, c_void_p, c_void_p]),
+    "nn_net_file_read": (c_int, [C.c_char_p, P(c_int64), P(c_int64), c_void_p, c_void_p]),
+    "nn_net_subsample": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, P(c_int64)]),
+    "nn_positions_file_write": (c_int, [C.c_char_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "nn_positions_file_read": (c_int, [C.c_char_p, P(c_int64), c_void_p, c_void_p, c_void_p]),
+    "nn_positions_subsample": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p,
+                                       c_void_p]),
+    "nn_electrodes_create": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_void_p)]),
+    "nn_electrodes_destroy": (c_int, [c_void_p]),
+    "nn_electrodes_measure": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "nn_measure_average": (c_int, [c_void_p, c_void_p, c_int, P(c_float)]),
+    "nn_synchrony_create": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, P(c_void_p)]),
+    "nn_synchrony_destroy": (c_int, [c_void_p]),
+    "nn_synchrony_measure": (c_int, [c_void_p, c_void_p]),
+    "nn_synchrony_get": (c_int, [c_void_p, c_void_p]),
+    "nn_hebbian_create": (c_int, [c_void_p, c_int, c_float, c_int64, c_int, P(c_void_p)]),
+    "nn_hebbian_destroy": (c_int, [c_void_p]),
+    "nn_hebbian_update": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "nn_hebbian_timers": (c_int, [c_void_p, c_void_p]),
     "nn_learned_create": (c_int, [c_void_p, c_uint64, P(c_void_p)]),
     "nn_learned_destroy": (c_int, [c_void_p]),
     "nn_learned_add_pair": (c_int, [c_void_p, c_void_p, c_void_p]),

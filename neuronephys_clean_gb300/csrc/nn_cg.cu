@@ -30,6 +30,7 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "nn_internal.cuh"
 
@@ -41,8 +42,9 @@ constexpr int RX = TX + 2, RY = TY + 2;      // u region (tile + halo)
 constexpr int PLANE_BYTES = BXW * BYW * 4;   // 1600
 constexpr int PLANE_STRIDE = 1664;           // 128-byte multiple
 constexpr int PX_BYTES = TX * TY * 4;        // p, x interior boxes (owned planes only)
-constexpr int STAGES = 3;
-constexpr int U_BYTES = 3 * RY * RX * 4;     // one 3-plane ring over the u region
+constexpr int STAGES = 4;
+constexpr int RING = 4;                      // u-ring slots: planes k-3 .. k
+constexpr int U_BYTES = RING * RY * RX * 4;  // one ring over the u region
 
 template <bool HET>
 struct Layout {
@@ -250,7 +252,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init_w(CgArgs a, const float*
 // One CG iteration (see the file comment).  One tile per block.  tm_d and
 // tm_m (D and 1/diag) are read only by the HET variant.
 template <bool HET>
-__global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ CUtensorMap tm_r,
+__global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant__ CUtensorMap tm_r,
                                                         const __grid_constant__ CUtensorMap tm_w,
                                                         const __grid_constant__ CUtensorMap tm_s,
                                                         const __grid_constant__ CUtensorMap tm_d,
@@ -265,8 +267,8 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     unsigned char* stage_base = smem;
-    float* U = (float*)(smem + STAGES * STAGE_BYTES);  // [3][RY][RX]
-    float* Dr = U + 3 * RY * RX;                        // HET: D ring [3][RY][RX]
+    float* U = (float*)(smem + STAGES * STAGE_BYTES);  // [RING][RY][RX]
+    float* Dr = U + RING * RY * RX;                     // HET: D ring [RING][RY][RX]
     uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES + L::RING_BYTES);
     __shared__ int abort_flag;
 
@@ -289,7 +291,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
     __syncthreads();
     // plane j (z = z0 - 1 + j) into stage j % STAGES: r, w, s with halo, and
     // for owned planes p, x of the tile
+    int last_issued = -1;  // tid 0: the last plane whose copies were issued
     auto issue = [&](int j) {
+        last_issued = j;
         unsigned char* st = stage_base + (j % STAGES) * STAGE_BYTES;
         uint64_t* bar = &bars[j % STAGES];
         const int kz = z0 - 1 + j;
@@ -310,107 +314,130 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_iter(const __grid_constant__ 
     if (tid == 0)
         for (int j = 0; j < STAGES && j < np; ++j) issue(j);
 
-    // interior cell of this thread
+    // per-thread invariants: interior cell, its offsets in a staged plane, in
+    // the u region and in a p/x box, its global index without z; the halo
+    // cell this thread fills (tid < HALO_CELLS)
     const int ix = tid & 31, iy = tid >> 5;
     const int gx = x0 + ix, gy = y0 + iy;
     const bool col_in = gx < a.nx && gy < a.ny;
+    const int ib = (iy + 1) * BXW + ix + 4;
+    const int iu = (iy + 1) * RX + ix + 1;
+    const int ip = iy * TX + ix;
+    const int cxy = gx + sy * gy;
+    int hb = 0, hu = 0;
+    bool hcol = false;
+    if (tid < HALO_CELLS) {
+        int bx, by;
+        if (tid < RX) { bx = 3 + tid; by = 0; }
+        else if (tid < 2 * RX) { bx = 3 + tid - RX; by = RY - 1; }
+        else if (tid < 2 * RX + TY) { bx = 3; by = 1 + tid - 2 * RX; }
+        else { bx = 3 + RX - 1; by = 1 + tid - 2 * RX - TY; }
+        const int hx = x0 - 4 + bx, hy = y0 - 1 + by;
+        hcol = hx >= 0 && hx < a.nx && hy >= 0 && hy < a.ny;
+        hb = by * BXW + bx;
+        hu = by * RX + bx - 3;
+    }
     float acc_g = 0.0f, acc_r = 0.0f, acc_d = 0.0f;
 
-    for (int j = 0; j < np; ++j) {
+    // One plane j; SL = j % 4 names both its stage buffer and its u-ring slot,
+    // so every shared-memory offset below is a compile-time constant.  Each
+    // warp waits for the landed plane itself; the one block barrier per plane
+    // sits between writing u (all warps) and reading its neighbours.  With
+    // four ring slots the next plane's u writes never touch the three slots a
+    // slower warp may still be reading for w.
+    const int lane = tid & 31;
+    auto plane = [&](auto sl_c, int j) {
+        constexpr int SL = decltype(sl_c)::value;
+        constexpr int SM = (SL + 2) % RING, SC = (SL + 3) % RING;  // ring slots of planes k - 2 and k - 1
         const int k = z0 - 1 + j;
-        const int sidx = j % STAGES;
-        // one thread polls the barrier (spinning threads would take issue
-        // slots from the working warps); the block barrier then publishes the
-        // landed plane to everyone
-        if (tid == 0 && !mbar_wait(&bars[sidx], (uint32_t)((j / STAGES) & 1))) abort_flag = 1;
-        __syncthreads();
-        if (abort_flag) break;
-        const float* R = (const float*)(stage_base + sidx * STAGE_BYTES);
-        const float* W = (const float*)(stage_base + sidx * STAGE_BYTES + PLANE_STRIDE);
-        const float* S = (const float*)(stage_base + sidx * STAGE_BYTES + 2 * PLANE_STRIDE);
-        const float* Dst = (const float*)(stage_base + sidx * STAGE_BYTES + 3 * PLANE_STRIDE);
-        const float* Mst = (const float*)(stage_base + sidx * STAGE_BYTES + 4 * PLANE_STRIDE);
-        const float* Ps = (const float*)(stage_base + sidx * STAGE_BYTES + PX_OFF);
-        const float* Xs = (const float*)(stage_base + sidx * STAGE_BYTES + PX_OFF + PX_BYTES);
-        float* Uk = U + (j % 3) * RY * RX;
-        float* Dk = Dr + (j % 3) * RY * RX;
+        bool ok = true;
+        if (lane == 0) ok = mbar_wait(&bars[SL], (uint32_t)((j / STAGES) & 1));
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (!ok) abort_flag = 1;
+        const unsigned char* st = stage_base + SL * STAGE_BYTES;
+        const float* R = (const float*)st;
+        const float* W = (const float*)(st + PLANE_STRIDE);
+        const float* S = (const float*)(st + 2 * PLANE_STRIDE);
+        const float* Dst = (const float*)(st + 3 * PLANE_STRIDE);
+        const float* Mst = (const float*)(st + 4 * PLANE_STRIDE);
+        const float* Ps = (const float*)(st + PX_OFF);
+        const float* Xs = (const float*)(st + PX_OFF + PX_BYTES);
+        float* Uk = U + SL * RY * RX;
+        float* Dk = Dr + SL * RY * RX;
         const bool plane_in = k >= 0 && k < a.nz;
-        // interior cells: s, r, u and the pointwise p, x updates for owned planes
-        {
-            const int bx = ix + 4, by = iy + 1;
-            const float sv = W[by * BXW + bx] + beta * S[by * BXW + bx];
-            const float rv_old = R[by * BXW + bx];
+        if (ok) {
+            // interior cells: s, r, u and the pointwise p, x updates for owned planes
+            const float sv = W[ib] + beta * S[ib];
+            const float rv_old = R[ib];
             const float rv = rv_old - alpha * sv;
             const bool in = col_in && plane_in;
-            const float mi = HET ? Mst[by * BXW + bx] : a.invd;
+            const float mi = HET ? Mst[ib] : a.invd;
             const float uv = in ? mi * rv : 0.0f;
-            Uk[by * RX + bx - 3] = uv;
-            if (HET) Dk[by * RX + bx - 3] = Dst[by * BXW + bx];
+            Uk[iu] = uv;
+            if (HET) Dk[iu] = Dst[ib];
             if (in && k >= z0 && k < z1) {
-                const int c = gx + sy * gy + sz * k;
-                const float pv = mi * rv_old + beta * Ps[iy * TX + ix];
+                const int c = cxy + sz * k;
+                const float pv = mi * rv_old + beta * Ps[ip];
                 a.p[c] = pv;
-                a.x[c] = Xs[iy * TX + ix] + alpha * pv;
+                a.x[c] = Xs[ip] + alpha * pv;
                 a.s_out[c] = sv;
                 a.r_out[c] = rv;
                 acc_g += rv * uv;
                 acc_r += rv * rv;
             }
-        }
-        // halo ring of the u region
-        if (tid < HALO_CELLS) {
-            int bx, by;
-            if (tid < RX) { bx = 3 + tid; by = 0; }
-            else if (tid < 2 * RX) { bx = 3 + tid - RX; by = RY - 1; }
-            else if (tid < 2 * RX + TY) { bx = 3; by = 1 + tid - 2 * RX; }
-            else { bx = 3 + RX - 1; by = 1 + tid - 2 * RX - TY; }
-            const int hx = x0 - 4 + bx, hy = y0 - 1 + by;
-            const bool in = plane_in && hx >= 0 && hx < a.nx && hy >= 0 && hy < a.ny;
-            const float sv = W[by * BXW + bx] + beta * S[by * BXW + bx];
-            const float rv = R[by * BXW + bx] - alpha * sv;
-            const float mi = HET ? Mst[by * BXW + bx] : a.invd;
-            Uk[by * RX + bx - 3] = in ? mi * rv : 0.0f;
-            if (HET) Dk[by * RX + bx - 3] = Dst[by * BXW + bx];
-        }
-        __syncthreads();
-        // refill this stage with the plane STAGES ahead
-        if (tid == 0 && j + STAGES < np) issue(j + STAGES);
-        // w = A u for the plane behind (k - 1), owned when j >= 2
-        if (j >= 2) {
-            const int kb = k - 1;
-            const float* Um = U + ((j - 2) % 3) * RY * RX;  // plane k - 2
-            const float* Uc = U + ((j - 1) % 3) * RY * RX;  // plane k - 1
-            const int bx = ix + 1, by = iy + 1;               // in u-region coordinates
-            if (col_in && kb < z1) {
-                const float uc = Uc[by * RX + bx];
-                float wv;
-                if (HET) {
-                    const float* Dm = Dr + ((j - 2) % 3) * RY * RX;
-                    const float* Dc = Dr + ((j - 1) % 3) * RY * RX;
-                    const float dc = Dc[by * RX + bx];
-                    float acc = face_coef(dc, Dc[by * RX + bx - 1], gx > 0) * (uc - Uc[by * RX + bx - 1]);
-                    acc += face_coef(dc, Dc[by * RX + bx + 1], gx < a.nx - 1) * (uc - Uc[by * RX + bx + 1]);
-                    acc += face_coef(dc, Dc[(by - 1) * RX + bx], gy > 0) * (uc - Uc[(by - 1) * RX + bx]);
-                    acc += face_coef(dc, Dc[(by + 1) * RX + bx], gy < a.ny - 1) * (uc - Uc[(by + 1) * RX + bx]);
-                    acc += face_coef(dc, Dm[by * RX + bx], kb > 0) * (uc - Um[by * RX + bx]);
-                    acc += face_coef(dc, Dk[by * RX + bx], kb < a.nz - 1) * (uc - Uk[by * RX + bx]);
-                    wv = a.onepb * uc + a.op_alpha * acc;
-                } else {
-                    const float nb = Uc[by * RX + bx - 1] + Uc[by * RX + bx + 1] + Uc[(by - 1) * RX + bx] +
-                                     Uc[(by + 1) * RX + bx] + Um[by * RX + bx] + Uk[by * RX + bx];
-                    wv = (a.onepb + 6.0f * a.op_alpha) * uc - a.op_alpha * nb;
-                }
-                a.w_out[gx + sy * gy + sz * kb] = wv;
-                acc_d += wv * uc;
+            // halo ring of the u region
+            if (tid < HALO_CELLS) {
+                const float hsv = W[hb] + beta * S[hb];
+                const float hrv = R[hb] - alpha * hsv;
+                const float hmi = HET ? Mst[hb] : a.invd;
+                Uk[hu] = (hcol && plane_in) ? hmi * hrv : 0.0f;
+                if (HET) Dk[hu] = Dst[hb];
             }
         }
-        // no barrier here: the next plane's post-wait barrier already orders
-        // this w-phase before any write to the u ring or any stage refill
+        __syncthreads();
+        if (abort_flag) return false;
+        // refill this stage with the plane STAGES ahead (every warp is done with it)
+        if (tid == 0 && j + STAGES < np) issue(j + STAGES);
+        // w = A u for the plane behind (k - 1), owned when j >= 2
+        if (j >= 2 && col_in && k - 1 < z1) {
+            const int kb = k - 1;
+            const float* Um = U + SM * RY * RX;
+            const float* Uc = U + SC * RY * RX;
+            const float uc = Uc[iu];
+            float wv;
+            if (HET) {
+                const float* Dm = Dr + SM * RY * RX;
+                const float* Dc = Dr + SC * RY * RX;
+                const float dc = Dc[iu];
+                float acc = face_coef(dc, Dc[iu - 1], gx > 0) * (uc - Uc[iu - 1]);
+                acc += face_coef(dc, Dc[iu + 1], gx < a.nx - 1) * (uc - Uc[iu + 1]);
+                acc += face_coef(dc, Dc[iu - RX], gy > 0) * (uc - Uc[iu - RX]);
+                acc += face_coef(dc, Dc[iu + RX], gy < a.ny - 1) * (uc - Uc[iu + RX]);
+                acc += face_coef(dc, Dm[iu], kb > 0) * (uc - Um[iu]);
+                acc += face_coef(dc, Dk[iu], kb < a.nz - 1) * (uc - Uk[iu]);
+                wv = a.onepb * uc + a.op_alpha * acc;
+            } else {
+                const float nb = Uc[iu - 1] + Uc[iu + 1] + Uc[iu - RX] + Uc[iu + RX] + Um[iu] + Uk[iu];
+                wv = (a.onepb + 6.0f * a.op_alpha) * uc - a.op_alpha * nb;
+            }
+            a.w_out[cxy + sz * kb] = wv;
+            acc_d += wv * uc;
+        }
+        return true;
+    };
+    static_assert(STAGES == RING, "the plane loop is unrolled by the stage / ring count");
+    for (int j = 0; j < np; j += 4) {
+        if (!plane(std::integral_constant<int, 0>{}, j)) break;
+        if (j + 1 < np && !plane(std::integral_constant<int, 1>{}, j + 1)) break;
+        if (j + 2 < np && !plane(std::integral_constant<int, 2>{}, j + 2)) break;
+        if (j + 3 < np && !plane(std::integral_constant<int, 3>{}, j + 3)) break;
     }
     if (abort_flag) {
         if (tid == 0) {
             a.flags[2] = 1;
             a.flags[0] = 3;
+            // let copies still in flight land before the block leaves
+            for (int q = 0; q <= last_issued; ++q) mbar_wait(&bars[q % STAGES], (uint32_t)((q / STAGES) & 1));
         }
         return;
     }

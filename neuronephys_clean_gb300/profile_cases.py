@@ -1,0 +1,82 @@
+"""Small, self-contained GPU cases for kernel profiling (ncu captures).
+
+    python -m neuronephys_clean_gb300.profile_cases hh1m     # 2 steps, 1M neurons, 128^3 grid
+    python -m neuronephys_clean_gb300.profile_cases cg128    # 3 PCG iterations, 128^3, constant D
+    python -m neuronephys_clean_gb300.profile_cases cghet    # 3 PCG iterations, 128^3, lognormal D
+    python -m neuronephys_clean_gb300.profile_cases conv128  # 3x3x3 convs (16->16, 48->16) + wgrad at 128^3
+
+Each case holds a few GB at most and launches a handful of kernels, so that
+an ncu capture of it ends by itself; every case also runs without ncu.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+import neuronephys_clean_gb300 as nn
+
+
+def hh1m(ctx):
+    c = nn.default_config(1_000_000)
+    c.seed, c.max_delay, c.grid, c.timescale = 1, 20, 128, 100
+    c.par_D, c.par_rtol, c.par_max_iter = 1.0, 1e-6, 8
+    s = nn.Simulation(ctx, c)
+    sp = nn.default_net_spec(nn.NN_NET_GAUSS)
+    sp.k, sp.dmax = 10, 20
+    s.generate_network(sp)
+    s.init_state(-65.0, 6.0, 12.0)
+    s.set_field("V", np.random.default_rng(0).uniform(-70, -30, 1_000_000).astype(np.float32))
+    s.step(2)
+
+
+def _pcg(ctx, D=None):
+    n = 128
+    dD = None if D is None else ctx.to_device(D.ravel())
+    pc = nn.PCG(ctx, n, n, n, 16.384, 0.0, dD)
+    b = ctx.to_device(np.random.default_rng(1).random(n ** 3).astype(np.float32))
+    x = ctx.to_device(np.zeros(n ** 3, np.float32))
+    try:
+        pc.solve(b, x, rtol=1e-6, max_iter=3)
+    except nn.NNError as e:
+        if e.status != nn.NN_ERR_NOT_CONVERGED:
+            raise
+
+
+def cg128(ctx):
+    _pcg(ctx)
+
+
+def cghet(ctx):
+    from neuronephys_clean_gb300 import fields
+    _pcg(ctx, fields.lognormal_diffusivity((128, 128, 128), 1.0, 8.0, seed=1))
+
+
+def conv128(ctx):
+    shape = (128, 128, 128)
+    rng = np.random.default_rng(2)
+    for cin, cout in [(16, 16), (48, 16)]:
+        a = nn.Activation(ctx, shape, cin)
+        a.pack(ctx.to_device(rng.standard_normal((cin,) + shape).astype(np.float32)))
+        w = ctx.to_device((rng.standard_normal((27, cin, cout)) * 0.05).astype(np.float32))
+        wp = nn.conv3d_pack_weights(ctx, w, cin, cout)
+        y = nn.Activation(ctx, shape, cout)
+        nn.conv3d_forward(ctx, a, wp, y, relu=True)
+        dw = ctx.to_device(np.zeros((27, cin, cout), np.float32))
+        nn.conv3d_wgrad(ctx, a, y, dw)
+
+
+CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128}
+
+
+def main(argv: list[str]) -> None:
+    names = argv or list(CASES)
+    ctx = nn.Context(0)
+    for name in names:
+        CASES[name](ctx)
+        ctx.synchronize()
+        print(f"{name} done", flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
