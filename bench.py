@@ -53,15 +53,18 @@ WORKLOADS = {
                i_lo=5.0, i_hi=15.0, grid=32, timescale=100, par_D=1.0, par_decay=0.0, total_steps=10000),
 }
 
-# Algorithmic bytes per unit:
+# Algorithmic bytes per unit of work (what one launch must move at minimum):
 HH_BYTES_PER_NEURON_STEP = 60      # R: V,m,h,n,ge,gi,I (28 B) + ring (E,I) slot (8 B); W: 6 state floats (24 B)
 PCG_BYTES_PER_CELL_ITER = 40       # k_cg_iter R: r,w,s,p,x; W: r,w,s,p,x -> 10 floats per cell
 PCG_HET_BYTES_PER_CELL_ITER = 48   # k_cg_iter<HET>: + D and 1/diag reads
 PUSH_BYTES_PER_EVENT = 13          # 4 B target + 4 B weight + 1 B delay + 4 B ring read-modify-write
 
-# DRAM bytes per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
-# per unit of work; filled from the committed ncu summaries in profiles/.
-NCU_TRAFFIC_PER_UNIT = {"hh_step": None, "pcg_iteration": None}
+# DRAM bytes per unit of work from one ncu capture of the kernel
+# (dram__bytes_read.sum + dram__bytes_write.sum per launch / units per launch).
+NCU_TRAFFIC_PER_UNIT = {
+    "hh_step": 36.03,        # 36.03 MB read + 0 MB written per 1M-neuron launch (writes stay in L2)
+    "pcg_iteration": 20.2,   # 41.99 MB read + 0.45 MB written per 128^3 launch (the rest hits L2)
+}
 
 
 def measured_peaks() -> tuple[float, str]:

@@ -42,8 +42,8 @@ constexpr int RX = TX + 2, RY = TY + 2;      // u region (tile + halo)
 constexpr int PLANE_BYTES = BXW * BYW * 4;   // 1600
 constexpr int PLANE_STRIDE = 1664;           // 128-byte multiple
 constexpr int PX_BYTES = TX * TY * 4;        // p, x interior boxes (owned planes only)
-constexpr int STAGES = 4;
-constexpr int RING = 4;                      // u-ring slots: planes k-3 .. k
+constexpr int STAGES = 3;
+constexpr int RING = 3;                      // u-ring slots: planes k-2 .. k
 constexpr int U_BYTES = RING * RY * RX * 4;  // one ring over the u region
 
 template <bool HET>
@@ -103,6 +103,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
         if (done) return true;
     }
     return false;
+}
+
+// Abort path: wait (bounded) for the copies of planes first .. last to land.
+__device__ __noinline__ void drain_planes(uint64_t* bars, int first, int last, int stages)
+{
+    for (int q = first; q <= last; ++q) mbar_wait(&bars[q % stages], (uint32_t)((q / stages) & 1));
 }
 
 __device__ __forceinline__ void tma_load_plane(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
@@ -291,9 +297,7 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
     __syncthreads();
     // plane j (z = z0 - 1 + j) into stage j % STAGES: r, w, s with halo, and
     // for owned planes p, x of the tile
-    int last_issued = -1;  // tid 0: the last plane whose copies were issued
     auto issue = [&](int j) {
-        last_issued = j;
         unsigned char* st = stage_base + (j % STAGES) * STAGE_BYTES;
         uint64_t* bar = &bars[j % STAGES];
         const int kz = z0 - 1 + j;
@@ -339,21 +343,24 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
     }
     float acc_g = 0.0f, acc_r = 0.0f, acc_d = 0.0f;
 
-    // One plane j; SL = j % 4 names both its stage buffer and its u-ring slot,
-    // so every shared-memory offset below is a compile-time constant.  Each
-    // warp waits for the landed plane itself; the one block barrier per plane
-    // sits between writing u (all warps) and reading its neighbours.  With
-    // four ring slots the next plane's u writes never touch the three slots a
-    // slower warp may still be reading for w.
-    const int lane = tid & 31;
-    auto plane = [&](auto sl_c, int j) {
+    // One plane j; SL = j % 3 names both its stage buffer and its u-ring slot,
+    // so every shared-memory offset below is a compile-time constant.
+    auto plane = [&](auto sl_c, int j) -> bool {
         constexpr int SL = decltype(sl_c)::value;
-        constexpr int SM = (SL + 2) % RING, SC = (SL + 3) % RING;  // ring slots of planes k - 2 and k - 1
+        constexpr int SM = (SL + 1) % RING, SC = (SL + 2) % RING;  // ring slots of planes k - 2 and k - 1
         const int k = z0 - 1 + j;
-        bool ok = true;
-        if (lane == 0) ok = mbar_wait(&bars[SL], (uint32_t)((j / STAGES) & 1));
-        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-        if (!ok) abort_flag = 1;
+        // one thread polls the barrier (spinning threads would take issue
+        // slots from the working warps); the block barrier then publishes the
+        // landed plane to everyone and orders the previous plane's w-phase
+        // before this plane's writes to the u ring
+        if (tid == 0 && !mbar_wait(&bars[SL], (uint32_t)((j / STAGES) & 1))) {
+            // let the copies still in flight (planes j .. j + STAGES - 1) land
+            // before the block leaves
+            drain_planes(bars, j, min(np - 1, j + STAGES - 1), STAGES);
+            abort_flag = 1;
+        }
+        __syncthreads();
+        if (abort_flag) return false;
         const unsigned char* st = stage_base + SL * STAGE_BYTES;
         const float* R = (const float*)st;
         const float* W = (const float*)(st + PLANE_STRIDE);
@@ -365,8 +372,8 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
         float* Uk = U + SL * RY * RX;
         float* Dk = Dr + SL * RY * RX;
         const bool plane_in = k >= 0 && k < a.nz;
-        if (ok) {
-            // interior cells: s, r, u and the pointwise p, x updates for owned planes
+        // interior cells: s, r, u and the pointwise p, x updates for owned planes
+        {
             const float sv = W[ib] + beta * S[ib];
             const float rv_old = R[ib];
             const float rv = rv_old - alpha * sv;
@@ -385,18 +392,17 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
                 acc_g += rv * uv;
                 acc_r += rv * rv;
             }
-            // halo ring of the u region
-            if (tid < HALO_CELLS) {
-                const float hsv = W[hb] + beta * S[hb];
-                const float hrv = R[hb] - alpha * hsv;
-                const float hmi = HET ? Mst[hb] : a.invd;
-                Uk[hu] = (hcol && plane_in) ? hmi * hrv : 0.0f;
-                if (HET) Dk[hu] = Dst[hb];
-            }
+        }
+        // halo ring of the u region
+        if (tid < HALO_CELLS) {
+            const float hsv = W[hb] + beta * S[hb];
+            const float hrv = R[hb] - alpha * hsv;
+            const float hmi = HET ? Mst[hb] : a.invd;
+            Uk[hu] = (hcol && plane_in) ? hmi * hrv : 0.0f;
+            if (HET) Dk[hu] = Dst[hb];
         }
         __syncthreads();
-        if (abort_flag) return false;
-        // refill this stage with the plane STAGES ahead (every warp is done with it)
+        // refill this stage with the plane STAGES ahead
         if (tid == 0 && j + STAGES < np) issue(j + STAGES);
         // w = A u for the plane behind (k - 1), owned when j >= 2
         if (j >= 2 && col_in && k - 1 < z1) {
@@ -425,19 +431,16 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
         }
         return true;
     };
-    static_assert(STAGES == RING, "the plane loop is unrolled by the stage / ring count");
-    for (int j = 0; j < np; j += 4) {
+    static_assert(STAGES == 3 && RING == 3, "the plane loop is unrolled by the 3 stages / 3 ring slots");
+    for (int j = 0; j < np; j += 3) {
         if (!plane(std::integral_constant<int, 0>{}, j)) break;
         if (j + 1 < np && !plane(std::integral_constant<int, 1>{}, j + 1)) break;
         if (j + 2 < np && !plane(std::integral_constant<int, 2>{}, j + 2)) break;
-        if (j + 3 < np && !plane(std::integral_constant<int, 3>{}, j + 3)) break;
     }
     if (abort_flag) {
         if (tid == 0) {
             a.flags[2] = 1;
             a.flags[0] = 3;
-            // let copies still in flight land before the block leaves
-            for (int q = 0; q <= last_issued; ++q) mbar_wait(&bars[q % STAGES], (uint32_t)((q / STAGES) & 1));
         }
         return;
     }

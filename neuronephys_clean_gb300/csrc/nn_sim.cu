@@ -59,6 +59,8 @@ struct nn_sim {
     int32_t* vox = nullptr;
     float* src = nullptr;
     float* u = nullptr;
+    float* u_prev = nullptr;       // previous solve's solution (initial-guess extrapolation)
+    bool have_prev = false;
     float* b = nullptr;
     nn_pcg* pcg = nullptr;
     nn_solve_stats stats{};
@@ -376,12 +378,18 @@ __global__ void k_list_bitmap(const int* list, int count, uint32_t* bitmap, cons
         atomicOr(bm + (list[q] >> 5), 1u << (list[q] & 31));
 }
 
-// paracrine: b = u + src ; src = 0
-__global__ void k_par_rhs(const float* u, float* src, float* b, int64_t G)
+// paracrine: b = u + src ; src = 0 ; with u_prev: initial guess u <- 2u - u_prev
+// (linear extrapolation in time of the slowly evolving field), u_prev <- u
+__global__ void k_par_rhs(float* u, float* src, float* b, float* u_prev, int extrapolate, int64_t G)
 {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < G; q += (int64_t)gridDim.x * blockDim.x) {
-        b[q] = u[q] + src[q];
+        const float uq = u[q];
+        b[q] = uq + src[q];
         src[q] = 0.0f;
+        if (u_prev) {
+            if (extrapolate) u[q] = 2.0f * uq - u_prev[q];
+            u_prev[q] = uq;
+        }
     }
 }
 
@@ -629,6 +637,7 @@ extern "C" void nn_sim_config_default(nn_sim_config* c, int n)
     c->par_decay = 0.0f;
     c->par_rtol = 1e-6;
     c->par_max_iter = 2000;
+    c->par_extrapolate = 0;
 }
 
 extern "C" void nn_net_spec_default(nn_net_spec* sp, int kind)
@@ -747,6 +756,7 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
         st = nn_alloc(ctx, &s->vox, NP);
         if (st == NN_OK) st = nn_alloc(ctx, &s->src, (size_t)s->G);
         if (st == NN_OK) st = nn_alloc(ctx, &s->u, (size_t)s->G);
+        if (st == NN_OK && cfg->par_extrapolate) st = nn_alloc(ctx, &s->u_prev, (size_t)s->G);
         if (st == NN_OK) st = nn_alloc(ctx, &s->b, (size_t)s->G);
         if (st == NN_OK) {
             const double dt_s = (double)cfg->timescale * cfg->hp.dt * 1e-3;
@@ -801,7 +811,7 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     for (int q = 0; q < NN_F_COUNT; ++q) nn_release(s->f[q]);
     nn_release(s->ring); nn_release(s->bitmap); nn_release(s->list); nn_release(s->counts); nn_release(s->step);
     nn_release(s->total); nn_release(s->rcount); nn_release(s->raster); nn_release(s->err);
-    nn_release(s->is_inh); nn_release(s->vox); nn_release(s->src); nn_release(s->u); nn_release(s->b);
+    nn_release(s->is_inh); nn_release(s->vox); nn_release(s->src); nn_release(s->u); nn_release(s->u_prev); nn_release(s->b);
     free_network(s);
     if (s->pcg) nn_pcg_destroy(s->pcg);
     for (auto e : s->ev_a) cudaEventDestroy(e);
@@ -1247,7 +1257,9 @@ static nn_status paracrine_solve(nn_sim* s)
 {
     nn_ctx* ctx = s->ctx;
     cudaStream_t cs = ctx->stream;
-    k_par_rhs<<<nn_grid_for(ctx, s->G, 256, 8), 256, 0, cs>>>(s->u, s->src, s->b, s->G);
+    k_par_rhs<<<nn_grid_for(ctx, s->G, 256, 8), 256, 0, cs>>>(s->u, s->src, s->b, s->u_prev, s->have_prev ? 1 : 0,
+                                                               s->G);
+    s->have_prev = s->u_prev != nullptr;
     NN_CHECK_LAUNCH(ctx, "k_par_rhs");
     int it = 0, conv = 0;
     double rel = 0.0;
@@ -1421,6 +1433,7 @@ extern "C" nn_status nn_sim_set_density(nn_sim* s, const float* h_u)
     nn_ctx* ctx = s->ctx;
     NN_CUDA(ctx, cudaMemcpyAsync(s->u, h_u, sizeof(float) * (size_t)s->G, cudaMemcpyHostToDevice, ctx->stream));
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    s->have_prev = false;
     return NN_OK;
 }
 
