@@ -43,6 +43,9 @@ WORKLOADS = {
     "c3": dict(workload="hh_10M_block200_k100_d40_grid192", n=10_000_000, kind="block", k=100, n_regions=200,
                size_sigma=1.0, density_sigma=1.0, w_mu=-1.0, w_sigma=1.0, dmax=40, inh=0.2, i_lo=6.0, i_hi=12.0,
                grid=192, timescale=100, par_D=1.0, par_decay=0.0, total_steps=500),
+    "c4": dict(workload="batch256_er_1k-64k_grids32-64", kind="batch", n_inst=256, size_lo=1000, size_hi=64000,
+               p_lo=0.005, p_hi=0.05, gna_lo=0.8, gna_hi=1.2, drive_lo=4.0, drive_hi=16.0, w_max=0.5, inh=0.2,
+               grid_lo=32, grid_hi=64, timescale=100, par_D=1.0, par_decay=0.0, total_steps=2000),
     "c5": dict(workload="cg_256cube_lognormalD_s1_l8_uptake0.1", kind="cg", grid=256, sigma=1.0, corr=8.0,
                D0=1.0, uptake=0.1, dt_s=1e-3, neurons=20000, rate=2.0,
                # iterations of the FP64 oracle PCG to 1e-6 on this seeded instance
@@ -392,6 +395,104 @@ def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | Non
             "push_pull_crossover_fraction": cross}
 
 
+def batch_layout(wl: dict, seed: int = 4):
+    """Seeded instance sizes (log-uniform), ER p, gNa scale, drive and grid
+    sides (32 at 1k neurons to 64 at 64k, growing as size^(1/6))."""
+    rng = np.random.default_rng(seed)
+    B = wl["n_inst"]
+    sizes = np.exp(rng.uniform(np.log(wl["size_lo"]), np.log(wl["size_hi"]), B)).astype(np.int64)
+    p = rng.uniform(wl["p_lo"], wl["p_hi"], B)
+    gna = rng.uniform(wl["gna_lo"], wl["gna_hi"], B).astype(np.float32)
+    drive = rng.uniform(wl["drive_lo"], wl["drive_hi"], B).astype(np.float32)
+    sides = np.clip(np.rint(wl["grid_lo"] * (sizes / wl["size_lo"]) ** (1 / 6)), wl["grid_lo"], wl["grid_hi"])
+    return sizes, p, gna, drive, sides.astype(np.int32)
+
+
+def run_batch(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
+    """A batch of independent networks in one simulation: one neuron-update
+    launch per step for all instances, per-instance paracrine grids solved by
+    the batched PCG, launch shape chosen by the autotuner."""
+    import neuronephys_clean_gb300 as nn
+    ctx = nn.Context(local_rank)
+    sizes, p, gna, drive, sides = batch_layout(wl)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    n = int(off[-1])
+    c = nn.default_config(n)
+    c.seed, c.grid, c.timescale, c.par_D, c.par_decay = 1, 0, wl["timescale"], wl["par_D"], wl["par_decay"]
+    c.par_rtol, c.par_max_iter, c.raster_capacity = 1e-6, 5000, 0
+    sim = nn.Simulation(ctx, c)
+    sim.set_instances(off, sides)
+    t0 = time.perf_counter()
+    nnz = sim.generate_batch_er(p, w_max=wl["w_max"], inh_fraction=wl["inh"])
+    t_gen = time.perf_counter() - t0
+    sim.init_state(-65.0, 0.0, 0.0)
+    sim.set_field("GNA_SCALE", np.repeat(gna, sizes))
+    sim.set_field("IDRIVE", np.repeat(drive, sizes))
+    sim.step(args.settle)
+    tpb, npt, tune_ms = sim.autotune(20)
+    P = wl["total_steps"]
+    sim.set_kernel_timing(True)
+    for _ in range(args.warmup):
+        sim.step(P)
+    ctx.synchronize()
+    launches0 = ctx.kernel_launches
+    _, spikes_a = sim.counters()
+    clocks = ClockSampler(local_rank)
+    barrier(dist)
+    clocks.start()
+    ctx.time_begin()
+    for _ in range(args.steps):
+        sim.step(P)
+    ms = ctx.time_end()
+    clock_info = clocks.stop()
+    barrier(dist)
+    launches = ctx.kernel_launches - launches0
+    _, spikes_b = sim.counters()
+    kt = sim.kernel_times()
+    value, tmax = aggregate(float(n) * P * args.steps, ms / 1e3, dist)
+    iters = sim.instance_iterations()
+    hbm_peak, peak_kind = measured_peaks()
+    hh_ach = n * HH_BYTES_PER_NEURON_STEP / (kt.hh_step_ms * 1e-3) / 1e9 if kt.hh_step_ms > 0 else None
+    # end to end: state from / to pinned host memory around each bench step
+    pin_in = nn.PinnedArray((6, n), np.float32)
+    pin_out = nn.PinnedArray((6, n), np.float32)
+    for q, k in enumerate(("V", "M", "H", "N", "GE", "GI")):
+        pin_in.array[q] = sim.get_field(k)
+    t1 = time.perf_counter()
+    for _ in range(max(1, args.e2e_steps)):
+        sim.run_host(pin_in.array, P, pin_out.array)
+    e2e_s = time.perf_counter() - t1
+    e2e_val, _ = aggregate(float(n) * P * max(1, args.e2e_steps), e2e_s, dist)
+    pin_in.free()
+    pin_out.free()
+    if rank != 0:
+        return None
+    line = {
+        "metric": "neuron-steps/s", "value": value, "unit": "neuron-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded counter-based generators)",
+        "config": {"workload": wl["workload"], "instances": int(wl["n_inst"]), "neurons": n, "synapses": int(nnz),
+                   "timesteps_per_step": P, "grid_cells": int(sim.field_cells()),
+                   "autotuned": {"threads_per_block": tpb, "neurons_per_thread": npt, "trial_ms_per_step": tune_ms},
+                   "network_generation_s": t_gen, "l2": "inputs larger than L2"},
+        "spikes_in_timed_region": spikes_b - spikes_a,
+        "cg": {"instances": int(wl["n_inst"]), "iterations_last_solve_max": int(iters.max()),
+               "iterations_last_solve_median": float(np.median(iters)), "solve_ms": kt.solve_ms},
+        "roofline": {"bound": "hbm", "kernel": "k_hh_step", "achieved": hh_ach, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": hh_ach / hbm_peak if hh_ach else None,
+                     "traffic": NCU_TRAFFIC_PER_UNIT["hh_step"] * n, "algorithmic_bytes": n * HH_BYTES_PER_NEURON_STEP,
+                     "launch_ms": kt.hh_step_ms, "peak_source": peak_kind},
+        "gpu_launches": int(launches),
+        "clocks": clock_info,
+        "e2e": {"value": e2e_val, "unit": "neuron-steps/s", "h2d_bytes_per_step": 6 * 4 * n,
+                "d2h_bytes_per_step": 6 * 4 * n + 8 * 2},
+    }
+    sim.close()
+    ctx.close()
+    return line
+
+
 def cg_problem(wl: dict):
     from neuronephys_clean_gb300 import fields
     g = wl["grid"]
@@ -634,7 +735,8 @@ def main() -> None:
     if args.delivery_sweep:
         line = run_delivery_sweep(args, wl, rank, local_rank)
     else:
-        line = (run_cg if wl.get("kind") == "cg" else run_ours)(args, wl, dist, rank, local_rank)
+        runner = {"cg": run_cg, "batch": run_batch}.get(wl.get("kind"), run_ours)
+        line = runner(args, wl, dist, rank, local_rank)
     if line is not None:
         print(json.dumps(line), flush=True)
 

@@ -265,9 +265,26 @@ typedef struct nn_net_spec {
     int n_regions;         /* BLOCK: regions of lognormal size */
     double region_size_sigma, density_sigma;
     int block_dmax;        /* BLOCK: delays 1..block_dmax by centroid distance */
+    const double* inst_p;  /* ER on a batch (nn_sim_set_instances): one p per instance, else NULL */
 } nn_net_spec;
 NN_API void nn_net_spec_default(nn_net_spec* sp, int kind);
 NN_API nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* spec);
+/* No counterpart in the reference.  A batch of independent networks in one
+ * simulation (one launch per step for all of them): instance b owns neurons
+ * h_offsets[b] .. h_offsets[b+1]-1 (h_offsets[0] = 0, h_offsets[n_inst] = n).
+ * h_grid_sides (nullable) gives each instance its own cubic paracrine grid
+ * (the simulation must be created with grid = 0); the fields are solved by
+ * the batched PCG, each instance to par_rtol.  Call before generating the
+ * network (ER then draws within instances, nn_net_spec.inst_p giving each its
+ * p) and before nn_sim_init_state (positions and voxels per instance). */
+NN_API nn_status nn_sim_set_instances(nn_sim* s, int n_inst, const int* h_offsets, const int* h_grid_sides);
+/* No counterpart in the reference.  Launch-shape autotuner of the neuron
+ * update: times trial_steps steps of every (threads per block 64/128/256,
+ * neurons per thread 1/2/4) candidate on the simulation's own network and
+ * state, keeps the fastest and restores the state the trials touched. */
+NN_API nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, int* best_npt, float* best_ms);
+/* Per-instance solver iteration counts of the last paracrine solve (n_inst entries). */
+NN_API nn_status nn_sim_instance_iterations(nn_sim* s, int* h_iters);
 NN_API nn_status nn_sim_network_size(nn_sim* s, int64_t* nnz);
 /* Download the device network (any pointer may be NULL). */
 NN_API nn_status nn_sim_get_network(nn_sim* s, int64_t* h_row_ptr, int32_t* h_col, float* h_weight,
@@ -314,6 +331,10 @@ NN_API nn_status nn_sim_get_raster(nn_sim* s, int64_t cap, int32_t* h_step, int3
 /* Paracrine density (grid^3 floats, x fastest) and last solve statistics. */
 NN_API nn_status nn_sim_get_density(nn_sim* s, float* h_u);
 NN_API nn_status nn_sim_set_density(nn_sim* s, const float* h_u);
+/* Cells of the paracrine field (grid^3, or the sum over a batch's grids) and
+ * the field cell of every neuron's deposits (n entries). */
+NN_API nn_status nn_sim_field_cells(nn_sim* s, int64_t* cells);
+NN_API nn_status nn_sim_get_vox(nn_sim* s, int32_t* h_vox);
 typedef struct nn_solve_stats { int iterations; double relres; int solves; int converged; } nn_solve_stats;
 NN_API nn_status nn_sim_solve_stats(nn_sim* s, nn_solve_stats* st);
 /* Kernel timing: when enabled, CUDA events bracket every neuron-update and
@@ -351,6 +372,20 @@ NN_API nn_status nn_pcg_solve(nn_pcg* pc, const float* d_b, float* d_x, double r
  * the last solve. */
 NN_API nn_status nn_pcg_set_kernel_timing(nn_pcg* pc, int enable);
 NN_API nn_status nn_pcg_kernel_time(nn_pcg* pc, float* ms, int* iters);
+
+/* No counterpart in the reference.  Batched Jacobi-PCG for the per-instance
+ * paracrine fields of a batch of networks: n_inst independent cubic grids of
+ * sides h_sides[b] (cells concatenated in instance order, x fastest), operator
+ * (1 + beta) I + alpha_unit * side_b^2 * L (alpha_unit = dt * D on the unit
+ * cube), each instance solved to its own relative residual rtol; converged
+ * instances stop costing work.  h_iters (nullable): n_inst iteration counts;
+ * *unconverged: instances that stopped short of rtol. */
+typedef struct nn_bpcg nn_bpcg;
+NN_API nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides, double alpha_unit, double beta,
+                                nn_bpcg** out);
+NN_API nn_status nn_bpcg_destroy(nn_bpcg* bp);
+NN_API nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter, int* h_iters,
+                               int* max_iters, int* unconverged);
 
 /* No counterpart in the reference.  The same solve as nn_pcg_create +
  * nn_pcg_solve + nn_pcg_destroy for callers that may not allocate device

@@ -475,6 +475,35 @@ class Simulation:
     def step(self, nsteps: int = 1) -> None:
         _check(lib().nn_sim_step(self.handle, nsteps), self.ctx, "step")
 
+    def set_instances(self, offsets, grid_sides=None) -> None:
+        """A batch of independent networks (see nn_sim_set_instances)."""
+        off = np.ascontiguousarray(offsets, np.int32)
+        gs = None if grid_sides is None else np.ascontiguousarray(grid_sides, np.int32)
+        _check(lib().nn_sim_set_instances(self.handle, len(off) - 1, _ptr(off), None if gs is None else _ptr(gs)),
+               self.ctx, "sim_set_instances")
+        self.n_inst = len(off) - 1
+        self._inst = (off, gs)
+
+    def generate_batch_er(self, p_per_instance, w_max: float = 0.5, inh_fraction: float = 0.2) -> int:
+        """Block-diagonal Erdos-Renyi network, one p per instance."""
+        spec = default_net_spec(NN_NET_ER)
+        self._inst_p = np.ascontiguousarray(p_per_instance, np.float64)
+        spec.inst_p = self._inst_p.ctypes.data
+        spec.w_max, spec.inh_fraction = w_max, inh_fraction
+        return self.generate_network(spec)
+
+    def autotune(self, trial_steps: int = 20) -> tuple[int, int, float]:
+        """(threads per block, neurons per thread, ms per step) chosen for the neuron update."""
+        tpb, npt, ms = C.c_int(), C.c_int(), C.c_float()
+        _check(lib().nn_sim_autotune(self.handle, trial_steps, C.byref(tpb), C.byref(npt), C.byref(ms)), self.ctx,
+               "sim_autotune")
+        return tpb.value, npt.value, ms.value
+
+    def instance_iterations(self) -> np.ndarray:
+        out = np.empty(self.n_inst, np.int32)
+        _check(lib().nn_sim_instance_iterations(self.handle, _ptr(out)), self.ctx, "sim_instance_iterations")
+        return out
+
     def deliver_spikes(self, d_list: "DeviceArray", count: int, mode: int = NN_DELIVERY_PUSH) -> None:
         _check(lib().nn_sim_deliver_spikes(self.handle, d_list.ptr, count, mode), self.ctx, "sim_deliver_spikes")
 
@@ -498,10 +527,21 @@ class Simulation:
         m = min(cap, cnt.value)
         return st[:m].copy(), ne[:m].copy()
 
+    def field_cells(self) -> int:
+        c = C.c_int64()
+        _check(lib().nn_sim_field_cells(self.handle, C.byref(c)), self.ctx, "field_cells")
+        return int(c.value)
+
     def density(self) -> np.ndarray:
-        g = self.config.grid
-        out = np.empty(g * g * g, np.float32)
+        out = np.empty(self.field_cells(), np.float32)
         _check(lib().nn_sim_get_density(self.handle, _ptr(out)), self.ctx, "density")
+        return out
+
+    get_density = density
+
+    def get_vox(self) -> np.ndarray:
+        out = np.empty(self.n, np.int32)
+        _check(lib().nn_sim_get_vox(self.handle, _ptr(out)), self.ctx, "get_vox")
         return out
 
     def set_density(self, u: np.ndarray) -> None:
@@ -520,6 +560,36 @@ class Simulation:
         s = SolveStats()
         _check(lib().nn_sim_solve_stats(self.handle, C.byref(s)), self.ctx)
         return s
+
+
+class BatchedPCG:
+    """Jacobi-PCG over many independent cubic grids, each to its own rtol."""
+
+    def __init__(self, ctx: Context, sides, alpha_unit: float, beta: float):
+        self.ctx = ctx
+        self.sides = np.ascontiguousarray(sides, np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sides.astype(np.int64) ** 3)])
+        self.handle = C.c_void_p()
+        _check(lib().nn_bpcg_create(ctx.handle, len(self.sides), _ptr(self.sides), alpha_unit, beta,
+                                    C.byref(self.handle)), ctx, "nn_bpcg_create")
+
+    def solve(self, b: DeviceArray, x: DeviceArray, rtol: float = 1e-6, max_iter: int = 10000):
+        its = np.empty(len(self.sides), np.int32)
+        mx, bad = C.c_int(), C.c_int()
+        _check(lib().nn_bpcg_solve(self.handle, b.ptr, x.ptr, rtol, max_iter, _ptr(its), C.byref(mx), C.byref(bad)),
+               self.ctx, "bpcg_solve")
+        return its, bad.value
+
+    def close(self):
+        if self.handle:
+            lib().nn_bpcg_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PCG:

@@ -49,7 +49,7 @@ class NetSpec(C.Structure):
                 ("sigma", c_double), ("w_mu", c_double), ("w_sigma", c_double), ("dmax", c_int),
                 ("inh_fraction", c_double), ("inh_random", c_int), ("n_regions", c_int),
                 ("region_size_sigma", c_double), ("density_sigma", c_double),
-                ("block_dmax", c_int)]
+                ("block_dmax", c_int), ("inst_p", c_void_p)]
 
 
 class SolveStats(C.Structure):
@@ -132,6 +132,14 @@ _SIGS = {
     "nn_pcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
     "nn_sim_deliver_spikes": (c_int, [c_void_p, c_void_p, c_int, c_int]),
+    "nn_sim_set_instances": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "nn_sim_field_cells": (c_int, [c_void_p, P(c_int64)]),
+    "nn_sim_get_vox": (c_int, [c_void_p, c_void_p]),
+    "nn_sim_autotune": (c_int, [c_void_p, c_int, P(c_int), P(c_int), P(c_float)]),
+    "nn_sim_instance_iterations": (c_int, [c_void_p, c_void_p]),
+    "nn_bpcg_create": (c_int, [c_void_p, c_int, c_void_p, c_double, c_double, P(c_void_p)]),
+    "nn_bpcg_destroy": (c_int, [c_void_p]),
+    "nn_bpcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, c_void_p, P(c_int), P(c_int)]),
     "nn_net_file_write": (c_int, [C.c_char_p, c_int64, c_int64, c_void_p, c_void_p]),
     "nn_net_file_read": (c_int, [C.c_char_p, P(c_int64), P(c_int64), c_void_p, c_void_p]),
     "nn_net_subsample": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, P(c_int64)]),

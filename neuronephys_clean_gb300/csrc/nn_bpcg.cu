@@ -1,0 +1,412 @@
+// Batched Jacobi-PCG: many independent cubic 7-point backward-Euler systems
+// (one per network instance of a batch, each with its own side g_b and
+// alpha_b = dt D g_b^2) solved together, each to its own relative residual.
+//
+// The instances' cells are concatenated (instance b at cell offset off_b,
+// x fastest).  A thread block covers 256 consecutive cells of one instance,
+// so every reduction is per instance: a block writes its FP64 partials, and
+// the last block of an instance to arrive (a per-instance ticket) sums them in
+// fixed order and forms that instance's scalars.  Per iteration two kernels
+// run (the structure of the two-kernel PCG: direction + operator, then
+// update), and blocks of converged instances return at once, so the batch
+// iterates until its slowest instance converges while the others stop
+// costing work.  The host reads one counter of unconverged instances per
+// chunk of iterations.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "nn_internal.cuh"
+
+namespace {
+constexpr int BT = 256;
+
+struct Batch {
+    int n_inst;
+    const int* side;         // [n_inst]
+    const int64_t* off;      // [n_inst + 1] cell offsets
+    const float* alpha;      // [n_inst]
+    const float* invd;       // [n_inst] 1 / (1 + beta + 6 alpha)
+    float onepb;             // 1 + beta
+    const int* blk_inst;     // block -> instance
+    const int* blk_first;    // [n_inst + 1] first block of each instance
+    double* scal;            // [n_inst][S_COUNT]
+    double* partials;        // [3][nblocks]
+    unsigned int* ticket;    // [n_inst]
+    int* flags;              // [n_inst] 0 running, 1 converged, 2 stopped (non-finite)
+    int* iters;              // [n_inst]
+    int* running;            // [1] unconverged instances
+    double rtol2;
+};
+
+enum { S_RZ = 0, S_PAP, S_RR, S_BB, S_ALPHA, S_BETA, S_COUNT };
+
+__device__ __forceinline__ void coords(int64_t c, int g, int& i, int& j, int& k)
+{
+    i = (int)(c % g);
+    const int64_t t = c / g;
+    j = (int)(t % g);
+    k = (int)(t / g);
+}
+
+// (A v)_c on the instance's cube (zero outside)
+template <class V>
+__device__ __forceinline__ float apply_cell(float onepb, float al, int g, int64_t c, V v)
+{
+    int i, j, k;
+    coords(c, g, i, j, k);
+    const int64_t sy = g, sz = (int64_t)g * g;
+    float nb = 0.0f;
+    nb += i > 0 ? v(c - 1) : 0.0f;
+    nb += i < g - 1 ? v(c + 1) : 0.0f;
+    nb += j > 0 ? v(c - sy) : 0.0f;
+    nb += j < g - 1 ? v(c + sy) : 0.0f;
+    nb += k > 0 ? v(c - sz) : 0.0f;
+    nb += k < g - 1 ? v(c + sz) : 0.0f;
+    return (onepb + 6.0f * al) * v(c) - al * nb;
+}
+
+// block partial sums (FP32 within a warp, FP64 across warps); the last block
+// of instance b to arrive sums the instance's partials in block order
+__device__ bool instance_reduce(const Batch& B, int b, int nsum, const float* v, double* out)
+{
+    __shared__ double ws[3][BT / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nblocks = gridDim.x;
+    for (int q = 0; q < nsum; ++q) {
+        float s = v[q];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) ws[q][w] = (double)s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < nsum; ++q) {
+            double s = 0.0;
+            for (int u = 0; u < BT / 32; ++u) s += ws[q][u];
+            B.partials[(size_t)q * nblocks + blockIdx.x] = s;
+        }
+        __threadfence();
+        const unsigned nb = (unsigned)(B.blk_first[b + 1] - B.blk_first[b]);
+        last = atomicAdd(&B.ticket[b], 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    const int f0 = B.blk_first[b], f1 = B.blk_first[b + 1];
+    for (int q = 0; q < nsum; ++q) {
+        const volatile double* pp = B.partials + (size_t)q * nblocks;
+        double s = 0.0;
+        for (int k = f0 + threadIdx.x; k < f1; k += BT) s += pp[k];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        __syncthreads();
+        if (lane == 0) ws[q][w] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int u = 0; u < BT / 32; ++u) t += ws[q][u];
+            out[q] = t;
+        }
+    }
+    if (threadIdx.x == 0) B.ticket[b] = 0;
+    __syncthreads();
+    return true;
+}
+
+// r = b - A x, p = z = M r; partials (r, z), (b, b), (r, r)
+__global__ void __launch_bounds__(BT) k_bpcg_init(Batch B, const float* rhs, const float* x, float* r, float* p)
+{
+    const int b = B.blk_inst[blockIdx.x];
+    const int g = B.side[b];
+    const int64_t base = B.off[b], cells = B.off[b + 1] - base;
+    const int64_t c = (int64_t)(blockIdx.x - B.blk_first[b]) * BT + threadIdx.x;
+    float rz = 0.0f, bb = 0.0f, rr = 0.0f;
+    if (c < cells) {
+        const float* xb = x + base;
+        const float ax = apply_cell(B.onepb, B.alpha[b], g, c, [&](int64_t q) { return xb[q]; });
+        const float bv = rhs[base + c];
+        const float rv = bv - ax;
+        const float zv = B.invd[b] * rv;
+        r[base + c] = rv;
+        p[base + c] = zv;
+        rz = rv * zv;
+        bb = bv * bv;
+        rr = rv * rv;
+    }
+    float v[3] = {rz, bb, rr};
+    double out[3];
+    if (instance_reduce(B, b, 3, v, out) && threadIdx.x == 0) {
+        double* s = B.scal + (size_t)b * S_COUNT;
+        s[S_RZ] = out[0];
+        s[S_BB] = out[1];
+        s[S_RR] = out[2];
+        s[S_BETA] = 0.0;
+        B.iters[b] = 0;
+        const bool done = out[2] <= B.rtol2 * out[1];
+        B.flags[b] = done ? 1 : 0;
+        if (!done) atomicAdd(B.running, 1);
+    }
+}
+
+// p = z + beta p_old (z = M r; the first iteration has beta = 0 and p_old = z),
+// Ap = A p; partial (p, Ap) -> alpha = rz / pAp
+__global__ void __launch_bounds__(BT) k_bpcg_dir_apply(Batch B, const float* r, const float* p_old, float* p_new,
+                                                       float* Ap)
+{
+    const int b = B.blk_inst[blockIdx.x];
+    if (B.flags[b]) return;
+    const int g = B.side[b];
+    const int64_t base = B.off[b], cells = B.off[b + 1] - base;
+    const int64_t c = (int64_t)(blockIdx.x - B.blk_first[b]) * BT + threadIdx.x;
+    const double* s = B.scal + (size_t)b * S_COUNT;
+    const float beta = (float)s[S_BETA], md = B.invd[b];
+    float pap = 0.0f;
+    if (c < cells) {
+        const float* rb = r + base;
+        const float* pb = p_old + base;
+        auto pv = [&](int64_t q) { return md * rb[q] + beta * pb[q]; };
+        const float pc = pv(c);
+        p_new[base + c] = pc;
+        const float ap = apply_cell(B.onepb, B.alpha[b], g, c, pv);
+        Ap[base + c] = ap;
+        pap = pc * ap;
+    }
+    float v[1] = {pap};
+    double out[1];
+    if (instance_reduce(B, b, 1, v, out) && threadIdx.x == 0) {
+        double* sw = B.scal + (size_t)b * S_COUNT;
+        sw[S_PAP] = out[0];
+        sw[S_ALPHA] = out[0] != 0.0 ? sw[S_RZ] / out[0] : 0.0;
+    }
+}
+
+// x += alpha p, r -= alpha Ap; partials (r, z), (r, r) -> beta, convergence
+__global__ void __launch_bounds__(BT) k_bpcg_update(Batch B, float* x, float* r, const float* p, const float* Ap,
+                                                    int max_iter)
+{
+    const int b = B.blk_inst[blockIdx.x];
+    if (B.flags[b]) return;
+    const int64_t base = B.off[b], cells = B.off[b + 1] - base;
+    const int64_t c = (int64_t)(blockIdx.x - B.blk_first[b]) * BT + threadIdx.x;
+    const double* s = B.scal + (size_t)b * S_COUNT;
+    const float alpha = (float)s[S_ALPHA];
+    float rz = 0.0f, rr = 0.0f;
+    if (c < cells) {
+        const int64_t q = base + c;
+        x[q] += alpha * p[q];
+        const float rv = r[q] - alpha * Ap[q];
+        r[q] = rv;
+        rz = rv * (B.invd[b] * rv);
+        rr = rv * rv;
+    }
+    float v[2] = {rz, rr};
+    double out[2];
+    if (instance_reduce(B, b, 2, v, out) && threadIdx.x == 0) {
+        double* sw = B.scal + (size_t)b * S_COUNT;
+        const int it = B.iters[b] + 1;
+        B.iters[b] = it;
+        sw[S_BETA] = sw[S_RZ] != 0.0 ? out[0] / sw[S_RZ] : 0.0;
+        sw[S_RZ] = out[0];
+        sw[S_RR] = out[1];
+        int f = 0;
+        if (out[1] <= B.rtol2 * sw[S_BB]) f = 1;
+        else if (!std::isfinite(out[1])) f = 2;
+        else if (it >= max_iter) f = 3;
+        if (f) {
+            B.flags[b] = f;
+            atomicSub(B.running, 1);
+        }
+    }
+}
+}  // namespace
+
+struct nn_bpcg {
+    nn_ctx* ctx = nullptr;
+    int n_inst = 0;
+    int64_t G = 0;
+    int nblocks = 0;
+    std::vector<int> h_side;
+    std::vector<int64_t> h_off;
+    int *side = nullptr, *blk_inst = nullptr, *blk_first = nullptr, *flags = nullptr, *iters = nullptr,
+        *running = nullptr;
+    int64_t* off = nullptr;
+    float *alpha = nullptr, *invd = nullptr;
+    float onepb = 1.0f;
+    double* scal = nullptr;
+    double* partials = nullptr;
+    unsigned int* ticket = nullptr;
+    float *r = nullptr, *p0 = nullptr, *p1 = nullptr, *Ap = nullptr;
+    // timing of the last solve (events around the iteration chunks)
+    bool timing = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_ms = 0.0f;
+    int last_iters = 0;
+};
+
+extern "C" nn_status nn_bpcg_destroy(nn_bpcg* bp)
+{
+    if (!bp) return NN_OK;
+    if (bp->ctx) cudaStreamSynchronize(bp->ctx->stream);
+    for (void* q : {(void*)bp->side, (void*)bp->blk_inst, (void*)bp->blk_first, (void*)bp->flags, (void*)bp->iters,
+                    (void*)bp->running, (void*)bp->off, (void*)bp->alpha, (void*)bp->invd, (void*)bp->scal,
+                    (void*)bp->partials, (void*)bp->ticket, (void*)bp->r, (void*)bp->p0, (void*)bp->p1, (void*)bp->Ap})
+        if (q) cudaFree(q);
+    if (bp->ev0) cudaEventDestroy(bp->ev0);
+    if (bp->ev1) cudaEventDestroy(bp->ev1);
+    nn_ctx* ctx = bp->ctx;
+    delete bp;
+    if (ctx) nn_ctx_release(ctx);
+    return NN_OK;
+}
+
+// sides[b] >= 1; alpha_b = alpha_unit * side_b^2 (alpha_unit = dt D on the unit cube)
+extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides, double alpha_unit, double beta,
+                                    nn_bpcg** out)
+{
+    if (!ctx || !h_sides || !out) return NN_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (n_inst < 1) return nn_fail(ctx, NN_ERR_INVALID_ARG, "batched PCG: no instances");
+    nn_bpcg* bp = new nn_bpcg();
+    bp->ctx = ctx;
+    nn_ctx_retain(ctx);
+    bp->n_inst = n_inst;
+    bp->h_side.assign(h_sides, h_sides + n_inst);
+    bp->h_off.assign((size_t)n_inst + 1, 0);
+    std::vector<float> al(n_inst), iv(n_inst);
+    std::vector<int> first((size_t)n_inst + 1, 0), binst;
+    for (int b = 0; b < n_inst; ++b) {
+        const int g = h_sides[b];
+        if (g < 1) {
+            nn_bpcg_destroy(bp);
+            return nn_fail(ctx, NN_ERR_INVALID_ARG, "batched PCG: instance %d has side %d", b, g);
+        }
+        const int64_t cells = (int64_t)g * g * g;
+        bp->h_off[(size_t)b + 1] = bp->h_off[(size_t)b] + cells;
+        al[b] = (float)(alpha_unit * g * g);
+        iv[b] = (float)(1.0 / (1.0 + beta + 6.0 * alpha_unit * g * g));
+        const int nb = (int)((cells + BT - 1) / BT);
+        first[(size_t)b + 1] = first[(size_t)b] + nb;
+        for (int q = 0; q < nb; ++q) binst.push_back(b);
+    }
+    bp->G = bp->h_off.back();
+    bp->nblocks = first.back();
+    bp->onepb = (float)(1.0 + beta);
+    nn_status st = NN_OK;
+    const size_t G = (size_t)bp->G;
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->side, (size_t)n_inst);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->off, (size_t)n_inst + 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->alpha, (size_t)n_inst);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->invd, (size_t)n_inst);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->blk_inst, (size_t)bp->nblocks);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->blk_first, (size_t)n_inst + 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->flags, (size_t)n_inst);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->iters, (size_t)n_inst);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->running, 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->scal, (size_t)n_inst * S_COUNT);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->partials, (size_t)3 * bp->nblocks);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->ticket, (size_t)n_inst);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->r, G);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->p0, G);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->p1, G);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->Ap, G);
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpy(bp->side, h_sides, sizeof(int) * n_inst, cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, cudaMemcpy(bp->off, bp->h_off.data(), sizeof(int64_t) * (n_inst + 1), cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpy(bp->alpha, al.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpy(bp->invd, iv.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, cudaMemcpy(bp->blk_inst, binst.data(), sizeof(int) * binst.size(), cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, cudaMemcpy(bp->blk_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemset(bp->ticket, 0, sizeof(unsigned int) * n_inst), "memset");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&bp->ev0), "event");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&bp->ev1), "event");
+    if (st != NN_OK) {
+        nn_bpcg_destroy(bp);
+        return st;
+    }
+    *out = bp;
+    return NN_OK;
+}
+
+int64_t nn_bpcg_cells(const nn_bpcg* bp) { return bp->G; }
+const int64_t* nn_bpcg_offsets(const nn_bpcg* bp) { return bp->h_off.data(); }
+void nn_bpcg_set_timing(nn_bpcg* bp, bool on) { bp->timing = on; }
+void nn_bpcg_last_timing(const nn_bpcg* bp, float* ms, int* iters)
+{
+    *ms = bp->last_ms;
+    *iters = bp->last_iters;
+}
+
+static Batch batch_args(nn_bpcg* bp, double rtol)
+{
+    Batch B;
+    B.n_inst = bp->n_inst;
+    B.side = bp->side;
+    B.off = bp->off;
+    B.alpha = bp->alpha;
+    B.invd = bp->invd;
+    B.onepb = bp->onepb;
+    B.blk_inst = bp->blk_inst;
+    B.blk_first = bp->blk_first;
+    B.scal = bp->scal;
+    B.partials = bp->partials;
+    B.ticket = bp->ticket;
+    B.flags = bp->flags;
+    B.iters = bp->iters;
+    B.running = bp->running;
+    B.rtol2 = rtol * rtol;
+    return B;
+}
+
+// Solve every instance (x holds the initial guesses).  *unconverged: the
+// instances that stopped before reaching rtol (0 on success); iters
+// (nullable, n_inst entries): per-instance iteration counts; *max_iters: the
+// batch's iteration count.
+extern "C" nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter,
+                                   int* h_iters, int* max_iters, int* unconverged)
+{
+    if (!bp || !d_b || !d_x || !(rtol > 0.0) || max_iter < 0) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = bp->ctx;
+    cudaStream_t cs = ctx->stream;
+    Batch B = batch_args(bp, rtol);
+    NN_CUDA(ctx, cudaMemsetAsync(bp->running, 0, sizeof(int), cs));
+    NN_CUDA(ctx, cudaMemsetAsync(bp->ticket, 0, sizeof(unsigned int) * bp->n_inst, cs));
+    if (bp->timing) NN_CUDA(ctx, cudaEventRecord(bp->ev0, cs));
+    k_bpcg_init<<<bp->nblocks, BT, 0, cs>>>(B, d_b, d_x, bp->r, bp->p0);
+    NN_CHECK_LAUNCH(ctx, "k_bpcg_init");
+    int running = 0, it = 0;
+    const int chunk = 16;
+    while (true) {
+        NN_CUDA(ctx, cudaMemcpyAsync(&running, bp->running, sizeof(int), cudaMemcpyDeviceToHost, cs));
+        NN_CUDA(ctx, cudaStreamSynchronize(cs));
+        if (running == 0 || it >= max_iter) break;
+        for (int q = 0; q < chunk && it < max_iter; ++q, ++it) {
+            // p0 holds z = M r at the start (beta = 0), then the directions alternate
+            const float* p_old = (it & 1) ? bp->p1 : bp->p0;
+            float* p_new = (it & 1) ? bp->p0 : bp->p1;
+            k_bpcg_dir_apply<<<bp->nblocks, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap);
+            NN_CHECK_LAUNCH(ctx, "k_bpcg_dir_apply");
+            k_bpcg_update<<<bp->nblocks, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter);
+            NN_CHECK_LAUNCH(ctx, "k_bpcg_update");
+        }
+    }
+    if (bp->timing) {
+        NN_CUDA(ctx, cudaEventRecord(bp->ev1, cs));
+        NN_CUDA(ctx, cudaEventSynchronize(bp->ev1));
+        NN_CUDA(ctx, cudaEventElapsedTime(&bp->last_ms, bp->ev0, bp->ev1));
+    }
+    std::vector<int> its(bp->n_inst), fl(bp->n_inst);
+    NN_CUDA(ctx, cudaMemcpy(its.data(), bp->iters, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, cudaMemcpy(fl.data(), bp->flags, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
+    int mx = 0, bad = 0;
+    for (int b = 0; b < bp->n_inst; ++b) {
+        mx = std::max(mx, its[(size_t)b]);
+        bad += fl[(size_t)b] != 1;
+    }
+    if (h_iters) std::copy(its.begin(), its.end(), h_iters);
+    if (max_iters) *max_iters = mx;
+    if (unconverged) *unconverged = bad;
+    bp->last_iters = mx;
+    return NN_OK;
+}

@@ -147,6 +147,12 @@ nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol,
 void nn_pcg_info(const nn_pcg* pc, nn_ctx** ctx, int* nx, int* ny, int* nz, const float** invd, float* invd_const,
                  const float** D);
 
+// batched PCG (nn_bpcg.cu)
+int64_t nn_bpcg_cells(const nn_bpcg* bp);
+const int64_t* nn_bpcg_offsets(const nn_bpcg* bp);
+void nn_bpcg_set_timing(nn_bpcg* bp, bool on);
+void nn_bpcg_last_timing(const nn_bpcg* bp, float* ms, int* iters);
+
 struct nn_cg_plan;
 nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, const float* D,
                             const float* invdv, nn_cg_plan** out);

@@ -63,6 +63,15 @@ struct nn_sim {
     bool have_prev = false;
     float* b = nullptr;
     nn_pcg* pcg = nullptr;
+    // batch of independent networks: instance b owns neurons inst_off[b] ..
+    // inst_off[b+1]-1 and (with a field) its own cubic grid of side inst_grid[b]
+    int n_inst = 0;
+    std::vector<int> h_inst_off, h_inst_grid;
+    int* inst_off = nullptr;       // device [n_inst + 1]
+    int* inst_grid = nullptr;      // device [n_inst]
+    int64_t* inst_goff = nullptr;  // device [n_inst + 1] cell offsets
+    nn_bpcg* bpcg = nullptr;
+    std::vector<int> inst_iters;
     nn_solve_stats stats{};
     // host mirrors
     int64_t host_step = 0;
@@ -406,20 +415,68 @@ __global__ void k_fill_f(float* p, int64_t n, float v)
 }
 
 // ER: edge i -> j (j != i) iff philox word < thr; counts per row.
-__global__ void k_er_count(int n, uint32_t thr, uint64_t seed, int64_t* cnt)
+// Instance of neuron i (binary search over the instance offsets; one instance
+// when inst_off is null).
+__device__ __forceinline__ int instance_of(const int* inst_off, int n_inst, int i)
+{
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst_off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Erdos-Renyi rows by counter-based draws.  With instances (a batch), row i
+// of instance b draws only among the instance's neurons, with the instance's
+// threshold and the stream key seed + b over local indices, so each block of
+// the block-diagonal network equals the single network of that size and seed.
+struct ErRows {
+    int n;
+    uint32_t thr;
+    uint64_t seed;
+    const int* inst_off;   // null: one network
+    const uint32_t* inst_thr;
+    int n_inst;
+};
+
+__device__ __forceinline__ void er_row(const ErRows& g, int i, int& li, int& base, int& size, uint32_t& thr,
+                                       uint64_t& key)
+{
+    if (g.inst_off) {
+        const int b = instance_of(g.inst_off, g.n_inst, i);
+        base = g.inst_off[b];
+        size = g.inst_off[b + 1] - base;
+        li = i - base;
+        thr = g.inst_thr[b];
+        key = g.seed + (uint64_t)b;
+    } else {
+        base = 0;
+        size = g.n;
+        li = i;
+        thr = g.thr;
+        key = g.seed;
+    }
+}
+
+__global__ void k_er_count(ErRows g, int64_t* cnt)
 {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    const int nb = (n + 3) >> 2;
-    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < g.n; i += nw) {
+        int li, base, size;
+        uint32_t thr;
+        uint64_t key;
+        er_row(g, i, li, base, size, thr, key);
+        const int nb = (size + 3) >> 2;
         int c = 0;
         for (int jb = lane; jb < nb; jb += 32) {
-            const nn_u4 r = nn_philox(seed, (uint32_t)i, (uint32_t)jb, 0u, NN_P_ER);
+            const nn_u4 r = nn_philox(key, (uint32_t)li, (uint32_t)jb, 0u, NN_P_ER);
             const uint32_t w[4] = {r.x, r.y, r.z, r.w};
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int j = 4 * jb + q;
-                c += (j < n && j != i && w[q] < thr) ? 1 : 0;
+                c += (j < size && j != li && w[q] < thr) ? 1 : 0;
             }
         }
         c = __reduce_add_sync(0xffffffffu, c);
@@ -427,25 +484,28 @@ __global__ void k_er_count(int n, uint32_t thr, uint64_t seed, int64_t* cnt)
     }
 }
 
-__global__ void k_er_fill(int n, uint32_t thr, uint64_t seed, float wmax, const int64_t* row_ptr, int32_t* col,
-                          float* weight, uint8_t* delay)
+__global__ void k_er_fill(ErRows g, float wmax, const int64_t* row_ptr, int32_t* col, float* weight, uint8_t* delay)
 {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    const int nb = (n + 3) >> 2;
-    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < g.n; i += nw) {
+        int li, base, size;
+        uint32_t thr;
+        uint64_t key;
+        er_row(g, i, li, base, size, thr, key);
+        const int nb = (size + 3) >> 2;
         int64_t pos = row_ptr[i];
         int e_run = 0;
         for (int jb0 = 0; jb0 < nb; jb0 += 32) {
             const int jb = jb0 + lane;
             uint32_t m = 0;
             if (jb < nb) {
-                const nn_u4 r = nn_philox(seed, (uint32_t)i, (uint32_t)jb, 0u, NN_P_ER);
+                const nn_u4 r = nn_philox(key, (uint32_t)li, (uint32_t)jb, 0u, NN_P_ER);
                 const uint32_t w[4] = {r.x, r.y, r.z, r.w};
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int j = 4 * jb + q;
-                    if (j < n && j != i && w[q] < thr) m |= 1u << q;
+                    if (j < size && j != li && w[q] < thr) m |= 1u << q;
                 }
             }
             const int c = __popc(m);
@@ -459,8 +519,8 @@ __global__ void k_er_fill(int n, uint32_t thr, uint64_t seed, float wmax, const 
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 if (m & (1u << q)) {
-                    const nn_u4 rw = nn_philox(seed, (uint32_t)i, (uint32_t)e, 0u, NN_P_WEIGHT);
-                    col[pos + e] = 4 * jb + q;
+                    const nn_u4 rw = nn_philox(key, (uint32_t)li, (uint32_t)e, 0u, NN_P_WEIGHT);
+                    col[pos + e] = base + 4 * jb + q;
                     weight[pos + e] = __fmul_rn(wmax, nn_u01f(rw.x));
                     delay[pos + e] = 1;
                     ++e;
@@ -581,6 +641,35 @@ __global__ void k_init_state(StepArgs a, float v0, float m0, float h0, float n0,
     }
 }
 
+// Batch: each instance on its own jittered lattice in the unit cube (local
+// index, stream key seed + b), and voxels of its own grid (cell offset goff).
+__global__ void k_inst_positions(int n, const int* inst_off, int n_inst, uint64_t seed, float* x, float* y, float* z)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int b = instance_of(inst_off, n_inst, i);
+        const int li = i - inst_off[b];
+        const int L = nn_lattice_side(inst_off[b + 1] - inst_off[b]);
+        const nn_u4 rp = nn_philox(seed + (uint64_t)b, (uint32_t)li, 0u, 0u, NN_P_POS);
+        const int cx = li % L, cy = (li / L) % L, cz = li / (L * L);
+        x[i] = __fdiv_rn(__fadd_rn((float)cx, nn_u01f(rp.x)), (float)L);
+        y[i] = __fdiv_rn(__fadd_rn((float)cy, nn_u01f(rp.y)), (float)L);
+        z[i] = __fdiv_rn(__fadd_rn((float)cz, nn_u01f(rp.z)), (float)L);
+    }
+}
+
+__global__ void k_inst_vox(const float* x, const float* y, const float* z, int n, const int* inst_off, int n_inst,
+                           const int* inst_grid, const int64_t* inst_goff, int32_t* vox)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int b = instance_of(inst_off, n_inst, i);
+        const int grid = inst_grid[b];
+        int ix = (int)__fmul_rn(x[i], (float)grid), iy = (int)__fmul_rn(y[i], (float)grid),
+            iz = (int)__fmul_rn(z[i], (float)grid);
+        ix = min(max(ix, 0), grid - 1); iy = min(max(iy, 0), grid - 1); iz = min(max(iz, 0), grid - 1);
+        vox[i] = (int32_t)(inst_goff[b] + ix + (int64_t)grid * (iy + (int64_t)grid * iz));
+    }
+}
+
 __global__ void k_vox(const float* x, const float* y, const float* z, int n, int grid, int32_t* vox)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -660,6 +749,9 @@ extern "C" void nn_net_spec_default(nn_net_spec* sp, int kind)
     sp->block_dmax = 40;
 }
 
+// a paracrine field exists: one grid, or one grid per instance of a batch
+static bool has_field(const nn_sim* s) { return s->grid > 0 || s->bpcg != nullptr; }
+
 static StepArgs step_args(nn_sim* s, int q)
 {
     StepArgs a;
@@ -667,7 +759,7 @@ static StepArgs step_args(nn_sim* s, int q)
     a.ge = s->f[NN_F_GE]; a.gi = s->f[NN_F_GI];
     a.idrive = s->f[NN_F_IDRIVE];
     a.gna_scale = s->gna_set ? s->f[NN_F_GNA_SCALE] : nullptr;  // all ones unless set
-    a.upar = (s->cfg.hp.g_par != 0.0f && s->grid > 0) ? s->f[NN_F_UPAR] : nullptr;
+    a.upar = (s->cfg.hp.g_par != 0.0f && has_field(s)) ? s->f[NN_F_UPAR] : nullptr;
     a.ring = reinterpret_cast<float*>(s->ring);
     a.bitmap = s->bitmap;
     a.list = s->list;
@@ -685,7 +777,7 @@ static StepArgs step_args(nn_sim* s, int q)
     a.raster = s->raster;
     a.rcap = s->cfg.raster_capacity;
     a.vox = s->vox;
-    a.src = s->grid > 0 ? s->src : nullptr;
+    a.src = has_field(s) ? s->src : nullptr;
     a.err = s->err;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
     a.zero_ring = push;
@@ -814,6 +906,8 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     nn_release(s->is_inh); nn_release(s->vox); nn_release(s->src); nn_release(s->u); nn_release(s->u_prev); nn_release(s->b);
     free_network(s);
     if (s->pcg) nn_pcg_destroy(s->pcg);
+    if (s->bpcg) nn_bpcg_destroy(s->bpcg);
+    nn_release(s->inst_off); nn_release(s->inst_grid); nn_release(s->inst_goff);
     for (auto e : s->ev_a) cudaEventDestroy(e);
     for (auto e : s->ev_b) cudaEventDestroy(e);
     for (auto e : s->ev_c) cudaEventDestroy(e);
@@ -960,6 +1054,89 @@ static void block_tables(int n, const nn_net_spec* sp, uint64_t seed, std::vecto
     }
 }
 
+static void free_instances(nn_sim* s)
+{
+    nn_release(s->inst_off);
+    nn_release(s->inst_grid);
+    nn_release(s->inst_goff);
+    if (s->bpcg) {
+        nn_bpcg_destroy(s->bpcg);
+        s->bpcg = nullptr;
+        nn_release(s->vox);
+        nn_release(s->src);
+        nn_release(s->u);
+        nn_release(s->b);
+        s->G = 0;
+    }
+    s->n_inst = 0;
+    s->h_inst_off.clear();
+    s->h_inst_grid.clear();
+}
+
+extern "C" nn_status nn_sim_set_instances(nn_sim* s, int n_inst, const int* h_offsets, const int* h_grid_sides)
+{
+    if (!s || n_inst < 1 || !h_offsets) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    if (h_offsets[0] != 0 || h_offsets[n_inst] != s->n)
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "instance offsets must run from 0 to n = %d", s->n);
+    for (int b = 0; b < n_inst; ++b)
+        if (h_offsets[b + 1] <= h_offsets[b])
+            return nn_fail(ctx, NN_ERR_INVALID_ARG, "instance %d is empty", b);
+    if (h_grid_sides) {
+        if (s->grid > 0)
+            return nn_fail(ctx, NN_ERR_INVALID_ARG, "per-instance grids need a simulation created with grid = 0");
+        for (int b = 0; b < n_inst; ++b)
+            if (h_grid_sides[b] < 1) return nn_fail(ctx, NN_ERR_INVALID_ARG, "instance %d: grid side < 1", b);
+    }
+    drop_graph(s);
+    free_instances(s);
+    s->n_inst = n_inst;
+    s->h_inst_off.assign(h_offsets, h_offsets + n_inst + 1);
+    NN_TRY(nn_alloc(ctx, &s->inst_off, (size_t)n_inst + 1));
+    NN_CUDA(ctx, cudaMemcpy(s->inst_off, h_offsets, sizeof(int) * (n_inst + 1), cudaMemcpyHostToDevice));
+    if (h_grid_sides) {
+        s->h_inst_grid.assign(h_grid_sides, h_grid_sides + n_inst);
+        const double dt_s = (double)s->cfg.timescale * s->cfg.hp.dt * 1e-3;
+        NN_TRY(nn_bpcg_create(ctx, n_inst, h_grid_sides, dt_s * s->cfg.par_D, dt_s * s->cfg.par_decay, &s->bpcg));
+        s->G = nn_bpcg_cells(s->bpcg);
+        NN_TRY(nn_alloc(ctx, &s->inst_grid, (size_t)n_inst));
+        NN_TRY(nn_alloc(ctx, &s->inst_goff, (size_t)n_inst + 1));
+        NN_CUDA(ctx, cudaMemcpy(s->inst_grid, h_grid_sides, sizeof(int) * n_inst, cudaMemcpyHostToDevice));
+        NN_CUDA(ctx, cudaMemcpy(s->inst_goff, nn_bpcg_offsets(s->bpcg), sizeof(int64_t) * (n_inst + 1),
+                                cudaMemcpyHostToDevice));
+        NN_TRY(nn_alloc(ctx, &s->vox, (size_t)s->n_pad));
+        NN_TRY(nn_alloc(ctx, &s->src, (size_t)s->G));
+        NN_TRY(nn_alloc(ctx, &s->u, (size_t)s->G));
+        NN_TRY(nn_alloc(ctx, &s->b, (size_t)s->G));
+        NN_CUDA(ctx, cudaMemset(s->vox, 0, sizeof(int32_t) * s->n_pad));
+        NN_CUDA(ctx, cudaMemset(s->src, 0, sizeof(float) * s->G));
+        NN_CUDA(ctx, cudaMemset(s->u, 0, sizeof(float) * s->G));
+    }
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_get_vox(nn_sim* s, int32_t* h_vox)
+{
+    if (!s || !h_vox || !s->vox) return NN_ERR_INVALID_ARG;
+    NN_CUDA(s->ctx, cudaStreamSynchronize(s->ctx->stream));
+    NN_CUDA(s->ctx, cudaMemcpy(h_vox, s->vox, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost));
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_field_cells(nn_sim* s, int64_t* cells)
+{
+    if (!s || !cells) return NN_ERR_INVALID_ARG;
+    *cells = has_field(s) ? s->G : 0;
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_instance_iterations(nn_sim* s, int* h_iters)
+{
+    if (!s || !h_iters || s->n_inst < 1) return NN_ERR_INVALID_ARG;
+    for (int b = 0; b < s->n_inst; ++b) h_iters[b] = b < (int)s->inst_iters.size() ? s->inst_iters[(size_t)b] : 0;
+    return NN_OK;
+}
+
 extern "C" nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* sp)
 {
     if (!s || !sp) return NN_ERR_INVALID_ARG;
@@ -976,7 +1153,24 @@ extern "C" nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* sp)
         int64_t* cnt = nullptr;
         NN_TRY(nn_alloc(ctx, &cnt, (size_t)n + 1));
         NN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * ((size_t)n + 1), cs));
-        k_er_count<<<nn_grid_for(ctx, (int64_t)n * 32, 256, 16), 256, 0, cs>>>(n, thr, seed, cnt);
+        ErRows g{n, thr, seed, nullptr, nullptr, 0};
+        uint32_t* d_thr = nullptr;
+        if (s->n_inst > 0 && sp->inst_p) {
+            // a batch: the instances' own probabilities
+            std::vector<uint32_t> th((size_t)s->n_inst);
+            for (int b = 0; b < s->n_inst; ++b) {
+                if (!(sp->inst_p[b] >= 0.0 && sp->inst_p[b] <= 1.0))
+                    return nn_fail(ctx, NN_ERR_INVALID_ARG, "instance %d: ER p outside [0,1]", b);
+                const double t = std::floor(sp->inst_p[b] * 4294967296.0);
+                th[(size_t)b] = t >= 4294967295.0 ? 0xffffffffu : (uint32_t)t;
+            }
+            NN_TRY(nn_alloc(ctx, &d_thr, th.size()));
+            NN_CUDA(ctx, cudaMemcpyAsync(d_thr, th.data(), sizeof(uint32_t) * th.size(), cudaMemcpyHostToDevice, cs));
+            g.inst_off = s->inst_off;
+            g.inst_thr = d_thr;
+            g.n_inst = s->n_inst;
+        }
+        k_er_count<<<nn_grid_for(ctx, (int64_t)n * 32, 256, 16), 256, 0, cs>>>(g, cnt);
         NN_CHECK_LAUNCH(ctx, "k_er_count");
         NN_TRY(nn_scan_exclusive_i64(ctx, cnt, s->row_ptr, (int64_t)n + 1));
         cudaFree(cnt);
@@ -986,9 +1180,11 @@ extern "C" nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* sp)
         NN_TRY(nn_alloc(ctx, &s->col, E));
         NN_TRY(nn_alloc(ctx, &s->weight, E));
         NN_TRY(nn_alloc(ctx, &s->delay, E));
-        k_er_fill<<<nn_grid_for(ctx, (int64_t)n * 32, 256, 16), 256, 0, cs>>>(n, thr, seed, sp->w_max, s->row_ptr, s->col,
+        k_er_fill<<<nn_grid_for(ctx, (int64_t)n * 32, 256, 16), 256, 0, cs>>>(g, sp->w_max, s->row_ptr, s->col,
                                                                                s->weight, s->delay);
         NN_CHECK_LAUNCH(ctx, "k_er_fill");
+        NN_CUDA(ctx, cudaStreamSynchronize(cs));
+        if (d_thr) cudaFree(d_thr);
     } else if (sp->kind == NN_NET_GAUSS || sp->kind == NN_NET_BLOCK) {
         if (sp->k < 0 || (int64_t)n * sp->k >= ((int64_t)1 << 32))
             return nn_fail(ctx, NN_ERR_INVALID_ARG, "out-degree k out of range");
@@ -1118,6 +1314,11 @@ extern "C" nn_status nn_sim_set_field(nn_sim* s, int field, const float* h)
         s->gna_set = true;
         drop_graph(s);  // the captured kernels' arguments change
     }
+    if ((field == NN_F_X || field == NN_F_Y || field == NN_F_Z) && s->bpcg) {
+        k_inst_vox<<<nn_grid_for(ctx, s->n, 256, 16), 256, 0, ctx->stream>>>(
+            s->f[NN_F_X], s->f[NN_F_Y], s->f[NN_F_Z], s->n, s->inst_off, s->n_inst, s->inst_grid, s->inst_goff, s->vox);
+        NN_CHECK_LAUNCH(ctx, "k_inst_vox");
+    }
     if ((field == NN_F_X || field == NN_F_Y || field == NN_F_Z) && s->grid > 0) {
         k_vox<<<nn_grid_for(ctx, s->n, 256, 16), 256, 0, ctx->stream>>>(s->f[NN_F_X], s->f[NN_F_Y], s->f[NN_F_Z], s->n,
                                                                          s->grid, s->vox);
@@ -1161,6 +1362,17 @@ extern "C" nn_status nn_sim_init_state(nn_sim* s, float v0, float i_lo, float i_
         a, v0, (float)(am / (am + bm)), (float)(ah / (ah + bh)), (float)(an / (an + bn)), i_lo, i_hi, s->f[NN_F_X],
         s->f[NN_F_Y], s->f[NN_F_Z], s->f[NN_F_GNA_SCALE], L, s->grid, s->grid > 0 ? s->vox : nullptr);
     NN_CHECK_LAUNCH(ctx, "k_init_state");
+    if (s->n_inst > 0) {
+        k_inst_positions<<<nn_grid_for(ctx, s->n, 256, 16), 256, 0, ctx->stream>>>(
+            s->n, s->inst_off, s->n_inst, s->cfg.seed, s->f[NN_F_X], s->f[NN_F_Y], s->f[NN_F_Z]);
+        NN_CHECK_LAUNCH(ctx, "k_inst_positions");
+        if (s->bpcg) {
+            k_inst_vox<<<nn_grid_for(ctx, s->n, 256, 16), 256, 0, ctx->stream>>>(
+                s->f[NN_F_X], s->f[NN_F_Y], s->f[NN_F_Z], s->n, s->inst_off, s->n_inst, s->inst_grid, s->inst_goff,
+                s->vox);
+            NN_CHECK_LAUNCH(ctx, "k_inst_vox");
+        }
+    }
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return NN_OK;
 }
@@ -1209,7 +1421,7 @@ extern "C" nn_status nn_sim_set_kernel_timing(nn_sim* s, int enable)
 {
     if (!s) return NN_ERR_INVALID_ARG;
     nn_ctx* ctx = s->ctx;
-    const int P = s->grid > 0 ? s->cfg.timescale : 50;
+    const int P = has_field(s) ? s->cfg.timescale : 50;
     drop_graph(s);
     s->timing = enable != 0;
     if (s->timing && (int)s->ev_a.size() < P) {
@@ -1225,6 +1437,7 @@ extern "C" nn_status nn_sim_set_kernel_timing(nn_sim* s, int enable)
     }
     s->ev_valid.assign(s->ev_a.size(), 0);
     if (s->pcg) nn_pcg_set_timing(s->pcg, s->timing);
+    if (s->bpcg) nn_bpcg_set_timing(s->bpcg, s->timing);
     return NN_OK;
 }
 
@@ -1250,6 +1463,7 @@ extern "C" nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out)
     out->solve_ms = 0.0f;
     out->solve_iterations = 0;
     if (s->pcg) nn_pcg_last_timing(s->pcg, &out->solve_ms, &out->solve_iterations);
+    if (s->bpcg) nn_bpcg_last_timing(s->bpcg, &out->solve_ms, &out->solve_iterations);
     return NN_OK;
 }
 
@@ -1263,7 +1477,15 @@ static nn_status paracrine_solve(nn_sim* s)
     NN_CHECK_LAUNCH(ctx, "k_par_rhs");
     int it = 0, conv = 0;
     double rel = 0.0;
-    NN_TRY(nn_pcg_run_best(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, &it, &rel, &conv));
+    if (s->bpcg) {
+        int unconv = 0;
+        s->inst_iters.assign((size_t)s->n_inst, 0);
+        NN_TRY(nn_bpcg_solve(s->bpcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, s->inst_iters.data(), &it,
+                             &unconv));
+        conv = unconv == 0;
+    } else {
+        NN_TRY(nn_pcg_run_best(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, &it, &rel, &conv));
+    }
     s->stats.iterations = it;
     s->stats.relres = rel;
     s->stats.converged = conv;
@@ -1276,7 +1498,7 @@ static nn_status paracrine_solve(nn_sim* s)
 }
 
 // Steps per captured graph: one paracrine period, or 50 steps without a field.
-static int period_steps(const nn_sim* s) { return s->grid > 0 ? s->cfg.timescale : 50; }
+static int period_steps(const nn_sim* s) { return has_field(s) ? s->cfg.timescale : 50; }
 
 static nn_status ensure_graph(nn_sim* s)
 {
@@ -1307,6 +1529,90 @@ static nn_status ensure_graph(nn_sim* s)
     return NN_OK;
 }
 
+// Launch-shape autotuner for the neuron update: time trial steps of every
+// (threads per block, neurons per thread) candidate on this simulation's own
+// network and state, keep the fastest, and restore the state the trials
+// changed (neuron fields, delay ring, spike counters and lists, bitmap,
+// deposits).  The step counter is restored too, so the trials leave no trace.
+extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, int* best_npt, float* best_ms)
+{
+    if (!s || trial_steps < 1) return NN_ERR_INVALID_ARG;
+    if (!s->row_ptr) return nn_fail(s->ctx, NN_ERR_INVALID_ARG, "nn_sim_autotune: no network set");
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    const size_t NP = (size_t)s->n_pad;
+    // snapshot
+    struct Buf { void* dst; const void* src; size_t bytes; };
+    std::vector<Buf> keep;
+    auto save = [&](const void* p, size_t bytes) -> nn_status {
+        if (!p || !bytes) return NN_OK;
+        unsigned char* d = nullptr;
+        NN_TRY(nn_alloc(ctx, &d, bytes));
+        keep.push_back({d, p, bytes});
+        NN_CUDA(ctx, cudaMemcpyAsync(d, p, bytes, cudaMemcpyDeviceToDevice, cs));
+        return NN_OK;
+    };
+    nn_status st = NN_OK;
+    for (int q = 0; q < NN_F_COUNT && st == NN_OK; ++q) st = save(s->f[q], NP * sizeof(float));
+    if (st == NN_OK) st = save(s->ring, (size_t)s->D * NP * sizeof(float2));
+    if (st == NN_OK) st = save(s->bitmap, s->bitmap ? (size_t)s->D * s->words * sizeof(uint32_t) : 0);
+    if (st == NN_OK) st = save(s->list, 2 * NP * sizeof(int));
+    if (st == NN_OK) st = save(s->counts, 2 * sizeof(int));
+    if (st == NN_OK) st = save(s->step, sizeof(unsigned long long));
+    if (st == NN_OK) st = save(s->total, sizeof(unsigned long long));
+    if (st == NN_OK) st = save(s->rcount, sizeof(unsigned long long));
+    if (st == NN_OK) st = save(s->src, has_field(s) ? (size_t)s->G * sizeof(float) : 0);
+    const int old_tpb = s->tpb, old_npt = s->npt;
+    const bool old_timing = s->timing;
+    s->timing = false;
+    float best = 1e30f;
+    int btpb = old_tpb, bnpt = old_npt;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&e0), "event");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&e1), "event");
+    for (int npt : {1, 2, 4}) {
+        for (int tpb : {64, 128, 256}) {
+            if (st != NN_OK) break;
+            s->tpb = tpb;
+            s->npt = npt;
+            // restore, warm once, then time
+            for (const Buf& b : keep)
+                if (st == NN_OK)
+                    st = nn_cuda_check(ctx, cudaMemcpyAsync((void*)b.src, b.dst, b.bytes, cudaMemcpyDeviceToDevice, cs),
+                                       "restore");
+            if (st == NN_OK) st = enqueue_step(s, 0, -1);
+            if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e0, cs), "event");
+            for (int q = 0; q < trial_steps && st == NN_OK; ++q) st = enqueue_step(s, 0, -1);
+            if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e1, cs), "event");
+            float ms = 0.0f;
+            if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventSynchronize(e1), "event");
+            if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventElapsedTime(&ms, e0, e1), "event");
+            ms /= trial_steps;
+            if (st == NN_OK && ms < best) {
+                best = ms;
+                btpb = tpb;
+                bnpt = npt;
+            }
+        }
+    }
+    for (const Buf& b : keep) {
+        if (st == NN_OK)
+            st = nn_cuda_check(ctx, cudaMemcpyAsync((void*)b.src, b.dst, b.bytes, cudaMemcpyDeviceToDevice, cs), "restore");
+    }
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(cs), "nn_sim_autotune");
+    for (const Buf& b : keep) cudaFree(b.dst);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    s->timing = old_timing;
+    s->tpb = st == NN_OK ? btpb : old_tpb;
+    s->npt = st == NN_OK ? bnpt : old_npt;
+    drop_graph(s);
+    if (best_tpb) *best_tpb = s->tpb;
+    if (best_npt) *best_npt = s->npt;
+    if (best_ms) *best_ms = best;
+    return st;
+}
+
 extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
 {
     if (!s || nsteps < 0) return NN_ERR_INVALID_ARG;
@@ -1328,7 +1634,7 @@ extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
             s->host_step += 1;
             left -= 1;
         }
-        if (s->grid > 0 && (s->host_step % s->cfg.timescale) == 0) NN_TRY(paracrine_solve(s));
+        if (has_field(s) && (s->host_step % s->cfg.timescale) == 0) NN_TRY(paracrine_solve(s));
     }
     return NN_OK;
 }
@@ -1420,7 +1726,7 @@ extern "C" nn_status nn_sim_get_raster(nn_sim* s, int64_t cap, int32_t* h_step, 
 
 extern "C" nn_status nn_sim_get_density(nn_sim* s, float* h_u)
 {
-    if (!s || !h_u || s->grid <= 0) return NN_ERR_INVALID_ARG;
+    if (!s || !h_u || !has_field(s)) return NN_ERR_INVALID_ARG;
     nn_ctx* ctx = s->ctx;
     NN_CUDA(ctx, cudaMemcpyAsync(h_u, s->u, sizeof(float) * (size_t)s->G, cudaMemcpyDeviceToHost, ctx->stream));
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1429,7 +1735,7 @@ extern "C" nn_status nn_sim_get_density(nn_sim* s, float* h_u)
 
 extern "C" nn_status nn_sim_set_density(nn_sim* s, const float* h_u)
 {
-    if (!s || !h_u || s->grid <= 0) return NN_ERR_INVALID_ARG;
+    if (!s || !h_u || !has_field(s)) return NN_ERR_INVALID_ARG;
     nn_ctx* ctx = s->ctx;
     NN_CUDA(ctx, cudaMemcpyAsync(s->u, h_u, sizeof(float) * (size_t)s->G, cudaMemcpyHostToDevice, ctx->stream));
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

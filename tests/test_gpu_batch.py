@@ -1,0 +1,115 @@
+"""Batched mode: many independent networks in one simulation (block-diagonal
+ER with one p per instance, per-instance paracrine grids solved by the
+batched PCG), and the launch-shape autotuner.
+
+Tolerances: generated networks bit-exact against the oracle's single-network
+generator per instance; batched PCG solutions within 1e-5 (relative 2-norm)
+of FP64 CG per instance, iteration counts within 3 of the single-grid
+solver's; the simulated raster of the batch equal to the FP64 oracle's for
+the concatenated network (margin-aware, as the single-network test); the
+autotuned simulation bit-identical to an untuned twin (pull delivery)."""
+import numpy as np
+import pytest
+
+import neuronephys_clean_gb300 as nn
+from tolerance import assert_rasters_match
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [300, 800, 1500, 400, 1000]
+GRIDS = [8, 12, 16, 8, 12]
+P = [0.05, 0.02, 0.01, 0.04, 0.015]
+
+
+def batch_sim(ctx, seed=11, delivery=0, grids=True, raster=100000):
+    n = sum(SIZES)
+    c = nn.default_config(n)
+    c.seed, c.delivery, c.raster_capacity, c.grid, c.timescale = seed, delivery, raster, 0, 100
+    s = nn.Simulation(ctx, c)
+    off = np.concatenate([[0], np.cumsum(SIZES)])
+    s.set_instances(off, GRIDS if grids else None)
+    s.generate_batch_er(P, w_max=0.5, inh_fraction=0.2)
+    s.init_state(-65.0, 5.0, 15.0)
+    return s, off
+
+
+def test_block_diagonal_er_matches_single_networks(ctx, orc):
+    s, off = batch_sim(ctx, grids=False)
+    rp, col, w, d, _ = s.get_network()
+    for b, (n_b, p_b) in enumerate(zip(SIZES, P)):
+        ref = orc.gen_er(n_b, p_b, 0.5, 11 + b)
+        lo, hi = rp[off[b]], rp[off[b + 1]]
+        assert np.array_equal(rp[off[b]:off[b + 1] + 1] - lo, ref.row_ptr)
+        assert np.array_equal(col[lo:hi] - off[b], ref.col)
+        assert np.array_equal(w[lo:hi], ref.weight)
+        assert np.all(d[lo:hi] == 1)
+
+
+def test_batched_pcg_matches_single_solves(ctx, orc):
+    sides = [16, 24, 20, 32, 12]
+    alpha_unit, beta = 4e-3, 1e-4
+    bp = nn.BatchedPCG(ctx, sides, alpha_unit, beta)
+    rng = np.random.default_rng(0)
+    G = int(bp.offsets[-1])
+    b = np.zeros(G, np.float32)
+    b[rng.integers(0, G, 500)] += 1.0
+    b += 0.01 * rng.random(G).astype(np.float32)
+    db, dx = ctx.to_device(b), ctx.to_device(np.zeros(G, np.float32))
+    its, bad = bp.solve(db, dx, 1e-6, 5000)
+    assert bad == 0
+    x = dx.numpy()
+    for k, g in enumerate(sides):
+        lo, hi = bp.offsets[k], bp.offsets[k + 1]
+        al = alpha_unit * g * g
+        ref, _, _ = orc.pcg7(b[lo:hi], np.zeros(hi - lo), (g, g, g), al, beta, rtol=1e-12)
+        assert np.linalg.norm(x[lo:hi] - ref) <= 1e-5 * np.linalg.norm(ref), k
+        single = nn.PCG(ctx, g, g, g, al, beta)
+        xs = ctx.to_device(np.zeros(hi - lo, np.float32))
+        it1, _ = single.solve(ctx.to_device(b[lo:hi]), xs, 1e-6, 5000)
+        assert abs(int(its[k]) - it1) <= 3, (k, its[k], it1)
+
+
+def test_batch_simulation_matches_oracle(ctx, orc):
+    s, off = batch_sim(ctx)
+    rp, col, w, d, inh = s.get_network()
+    state = np.stack([s.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")])
+    o = orc.Sim(orc.CSR(rp, col, w, d), inh, s.get_field("IDRIVE"), 11, 2, state)
+    ref = {}
+    for t in range(100):
+        for j in o.step():
+            ref[(t, int(j))] = o.margins[(t, int(j))]
+    s.step(100)
+    st, ne = s.raster()
+    assert len(ref) > 50
+    assert_rasters_match(set(zip(st.tolist(), ne.tolist())), ref)
+    # one batched solve after 100 steps: each instance's field from its deposits
+    u = s.get_density()
+    vox = s.get_vox()
+    G = sum(g ** 3 for g in GRIDS)
+    src = np.zeros(G)
+    for (t, j) in ref:
+        src[vox[j]] += 1.0
+    goff = np.concatenate([[0], np.cumsum(np.array(GRIDS) ** 3)])
+    dt_s = 100 * s.config.hp.dt * 1e-3
+    iters = s.instance_iterations()
+    for b, g in enumerate(GRIDS):
+        lo, hi = goff[b], goff[b + 1]
+        refu, _, _ = orc.pcg7(src[lo:hi], np.zeros(hi - lo), (g, g, g), dt_s * g * g, 0.0, rtol=1e-12)
+        if np.linalg.norm(refu) > 0:
+            assert np.linalg.norm(u[lo:hi] - refu) <= 1e-4 * np.linalg.norm(refu), b
+            assert iters[b] > 0
+
+
+def test_autotune_keeps_state_and_results(ctx):
+    a, _ = batch_sim(ctx, seed=3, delivery=1, grids=False, raster=0)
+    b, _ = batch_sim(ctx, seed=3, delivery=1, grids=False, raster=0)
+    a.step(37)
+    b.step(37)
+    tpb, npt, ms = a.autotune(trial_steps=5)
+    assert tpb in (64, 128, 256) and npt in (1, 2, 4) and ms > 0
+    assert a.counters() == b.counters()
+    a.step(120)
+    b.step(120)
+    for k in ("V", "M", "H", "N", "GE", "GI"):
+        assert np.array_equal(a.get_field(k), b.get_field(k)), k
+    assert a.counters() == b.counters()
