@@ -543,4 +543,16 @@ NN_API nn_status nn_positions_file_read(const char* path, int64_t* n, float* h_x
 NN_API nn_status nn_positions_subsample(nn_ctx* ctx, const float* d_x, const float* d_y, const float* d_z,
                                         int64_t n, int N, float* d_ox, float* d_oy, float* d_oz);
 
+
+/* NormalNetwork(morphology, stddev, n_stddevs).Generate(N)
+ * (src_wholebrain/network_factory.cu:95-138) on the device: neuron i couples
+ * to every j within n_stddevs * stddev with probability
+ * exp(-|x_i - x_j|^2 / (2 stddev^2)); counter-based draws per pair (the
+ * reference draws from its unseeded engine in kd-tree order: same
+ * distribution, other edges).  d_offsets (n + 1) is always written; with
+ * d_indices non-NULL and capacity >= *nnz the targets are written too. */
+NN_API nn_status nn_net_local_gaussian(nn_ctx* ctx, int n, const float* d_x, const float* d_y, const float* d_z,
+                                       float stddev, int n_stddevs, uint64_t seed, int* d_offsets, int* d_indices,
+                                       int64_t capacity, int64_t* nnz);
+
 #endif

@@ -949,3 +949,70 @@ class FileMorphology:
                                             o[2].ptr), ctx, "nn_positions_subsample")
         self.positions = np.stack([v.numpy() for v in o], axis=1)
         return True
+
+
+# ------------------------------------------------------- whole-brain step --
+
+class NormalNetwork:
+    """NormalNetwork (src_wholebrain/network_factory.cuh:73-91): local
+    Gaussian-ball connectivity over device positions, built on the device."""
+
+    def __init__(self, x: DeviceArray, y: DeviceArray, z: DeviceArray, stddev: float, n_stddevs: int = 2,
+                 seed: int = 0):
+        self.x, self.y, self.z = x, y, z
+        self.stddev, self.n_stddevs, self.seed = stddev, n_stddevs, seed
+
+    def to_adjacency_list(self, ctx: Context, tcount: DeviceArray | None = None) -> AdjacencyList:
+        n = self.x.shape[0]
+        off = DeviceArray(ctx, (n + 1,), np.int32)
+        nnz = C.c_int64()
+        args = (ctx.handle, n, self.x.ptr, self.y.ptr, self.z.ptr, self.stddev, self.n_stddevs, self.seed, off.ptr)
+        _check(lib().nn_net_local_gaussian(*args, None, 0, C.byref(nnz)), ctx, "NormalNetwork count")
+        idx = DeviceArray(ctx, (max(nnz.value, 1),), np.int32)
+        _check(lib().nn_net_local_gaussian(*args, idx.ptr, nnz.value, C.byref(nnz)), ctx, "NormalNetwork fill")
+        if tcount is not None:
+            _check(lib().nn_net_tcount(ctx.handle, idx.ptr, nnz.value, n, tcount.ptr), ctx, "Tcount")
+        self.nnz = nnz.value
+        return AdjacencyList(idx, off)
+
+
+class MouseCortex:
+    """MouseCortex (src_wholebrain/mouse_cortex.cu:8-120): the whole-brain
+    HH model with white-matter AMPA / GABA couplings (uniform random, 0.9 and
+    0.1 of ncouple out-edges) and optional gray-matter local GABA coupling
+    (Gaussian ball of stddev over the positions).  simulate() is
+    MouseCortex::Simulate: the couplings in the reference's order (gray GABA,
+    white GABA, white AMPA), then one leapfrog step."""
+
+    def __init__(self, ctx: Context, n: int, positions=None, ncouple: int = 1000, use_gray: bool = True,
+                 stddev: float = 0.045, seed: int = 0):
+        self.ctx, self.n = ctx, n
+        self.ephys = HHEphys(ctx, n, variant=1, seed=seed)
+        v = self.ephys.vars
+        ix = {name: v[SIM_PARAMS.index(name)] for name in SIM_PARAMS}
+        e_net, i_net = UniformRandomNetwork(int(0.9 * ncouple)), UniformRandomNetwork(int(0.1 * ncouple))
+        e_net.generate(n)
+        i_net.generate(n)
+        self.e_list = e_net.to_adjacency_list(ctx, ix["ECOUNT"])
+        self.i_list = i_net.to_adjacency_list(ctx, ix["ICOUNT"])
+        self.white_ampa = AtomicCoupling(ctx, n)
+        self.white_gaba = AtomicCoupling(ctx, n)
+        self.gray_gaba = None
+        if use_gray:
+            if positions is None:
+                positions = np.random.default_rng(seed).uniform(-1.0, 1.0, (n, 3)).astype(np.float32)
+            self.pos = [ctx.to_device(np.ascontiguousarray(positions[:, a], np.float32)) for a in range(3)]
+            self.loc_net = NormalNetwork(*self.pos, stddev=stddev, seed=seed)
+            self.loc_list = self.loc_net.to_adjacency_list(ctx, ix["LOCAL_COUNT"])
+            self.gray_gaba = AtomicCoupling(ctx, n)
+        self._ix = ix
+
+    def simulate(self) -> int:
+        ix = self._ix
+        n_firing = 0
+        if self.gray_gaba is not None:
+            n_firing = self.gray_gaba(self.loc_list, ix["LOCAL_IN"], ix["LOCAL_OUTPUT"])
+        n_firing = self.white_gaba(self.i_list, ix["IIN"], ix["IOUTPUT"])
+        n_firing = self.white_ampa(self.e_list, ix["EIN"], ix["EOUTPUT"])
+        self.ephys.simulate_ephys()
+        return n_firing

@@ -147,6 +147,8 @@ _SIGS = {
     "nn_positions_file_read": (c_int, [C.c_char_p, P(c_int64), c_void_p, c_void_p, c_void_p]),
     "nn_positions_subsample": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p,
                                        c_void_p]),
+    "nn_net_local_gaussian": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_float, c_int, c_uint64,
+                                      c_void_p, c_void_p, c_int64, P(c_int64)]),
     "nn_electrodes_create": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_void_p)]),
     "nn_electrodes_destroy": (c_int, [c_void_p]),
     "nn_electrodes_measure": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

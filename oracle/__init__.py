@@ -64,6 +64,8 @@ _SIGS = {
     "orc_csr_to_csc": (None, [P(OrcCSR), V, V, V, V, V]),
     "orc_gen_er": (None, [C.c_int, C.c_double, C.c_float, C.c_uint64, P(OrcCSR)]),
     "orc_gauss_table": (None, [C.c_double, V]),
+    "orc_local_gaussian": (C.c_int64, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_uint64,
+                                       C.c_void_p, C.c_void_p, C.c_int64]),
     "orc_gen_block": (None, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
                              C.c_uint64, C.c_void_p]),
     "orc_gen_gauss": (None, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_uint64,
@@ -245,6 +247,17 @@ def gen_block(n: int, k: int, R: int, size_sigma: float, density_sigma: float, d
     s = OrcCSR(n, 0, rp.ctypes.data, col.ctypes.data, w.ctypes.data, d.ctypes.data)
     lib().orc_gen_block(n, k, R, size_sigma, density_sigma, dmax, mu, sg, seed, C.byref(s))
     return CSR(rp, col, w, d)
+
+
+def local_gaussian(x, y, z, stddev: float, n_stddevs: int, seed: int):
+    """(offsets, indices) of the local Gaussian-ball network."""
+    x, y, z = (np.ascontiguousarray(v, np.float32) for v in (x, y, z))
+    n = len(x)
+    off = np.zeros(n + 1, np.int32)
+    nnz = lib().orc_local_gaussian(n, ptr(x), ptr(y), ptr(z), stddev, n_stddevs, seed, ptr(off), None, 0)
+    idx = np.zeros(max(nnz, 1), np.int32)
+    lib().orc_local_gaussian(n, ptr(x), ptr(y), ptr(z), stddev, n_stddevs, seed, ptr(off), ptr(idx), nnz)
+    return off, idx[:nnz]
 
 
 def gauss_table(sigma_sites: float) -> np.ndarray:

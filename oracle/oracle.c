@@ -704,6 +704,86 @@ void orc_gen_block(int n, int k, int R, double size_sigma, double density_sigma,
     free(start); free(size); free(cum); free(pdelay);
 }
 
+/* Local Gaussian-ball network (the library's GPU restatement of NormalNetwork,
+ * src_wholebrain/network_factory.cu:95-138, with counter-based draws): cells
+ * of side n_stddevs * stddev over the bounding box, members ascending, rows
+ * visiting the 27 neighbouring cells (dz, dy, dx = -1..1) in order; pair
+ * (i, j) accepted when d2 <= r2 (FP32, no contraction) and
+ * u53(Philox(seed; i, j, 0, 10)) < exp(-d2 / (2 stddev^2)) (FP64).
+ * offsets: n + 1 ints; indices: capacity ints (NULL: count only).  Returns nnz. */
+int64_t orc_local_gaussian(int n, const float* x, const float* y, const float* z, float stddev, int n_stddevs,
+                           uint64_t seed, int* offsets, int* indices, int64_t capacity)
+{
+    float lo[3] = {x[0], y[0], z[0]}, hi[3] = {x[0], y[0], z[0]};
+    for (int i = 0; i < n; ++i) {
+        const float v[3] = {x[i], y[i], z[i]};
+        for (int a = 0; a < 3; ++a) {
+            if (v[a] < lo[a]) lo[a] = v[a];
+            if (v[a] > hi[a]) hi[a] = v[a];
+        }
+    }
+    const float h = stddev * (float)n_stddevs;
+    const float inv_h = 1.0f / h;
+    int g[3];
+    for (int a = 0; a < 3; ++a) {
+        g[a] = (int)ceil((hi[a] - lo[a]) / h);
+        if (g[a] < 1) g[a] = 1;
+    }
+    const int64_t ncells = (int64_t)g[0] * g[1] * g[2];
+    int* cell = (int*)malloc(sizeof(int) * n);
+    int* cc = (int*)malloc(sizeof(int) * 3 * n);
+    int64_t* start = (int64_t*)calloc((size_t)ncells + 1, sizeof(int64_t));
+    int* members = (int*)malloc(sizeof(int) * n);
+    for (int i = 0; i < n; ++i) {
+        const float p[3] = {x[i], y[i], z[i]};
+        int c[3];
+        for (int a = 0; a < 3; ++a) {
+            int q = (int)((p[a] - lo[a]) * inv_h);
+            if (q < 0) q = 0;
+            if (q > g[a] - 1) q = g[a] - 1;
+            c[a] = q;
+            cc[3 * i + a] = q;
+        }
+        cell[i] = c[0] + g[0] * (c[1] + g[1] * c[2]);
+        start[cell[i] + 1] += 1;
+    }
+    for (int64_t c = 0; c < ncells; ++c) start[c + 1] += start[c];
+    int64_t* fillp = (int64_t*)malloc(sizeof(int64_t) * (size_t)ncells);
+    for (int64_t c = 0; c < ncells; ++c) fillp[c] = start[c];
+    for (int i = 0; i < n; ++i) members[fillp[cell[i]]++] = i;  /* ascending within a cell */
+    const float r2 = h * h;
+    const double inv_2var = 1.0 / (2.0 * (double)stddev * (double)stddev);
+    int64_t total = 0;
+    offsets[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int ax = cc[3 * i] + dx, ay = cc[3 * i + 1] + dy, az = cc[3 * i + 2] + dz;
+                    if (ax < 0 || ay < 0 || az < 0 || ax >= g[0] || ay >= g[1] || az >= g[2]) continue;
+                    const int64_t c = ax + (int64_t)g[0] * (ay + (int64_t)g[1] * az);
+                    for (int64_t q = start[c]; q < start[c + 1]; ++q) {
+                        const int j = members[q];
+                        if (j == i) continue;
+                        const float ddx = x[i] - x[j], ddy = y[i] - y[j], ddz = z[i] - z[j];
+                        const float d2 = (ddx * ddx + ddy * ddy) + ddz * ddz;
+                        if (!(d2 <= r2)) continue;
+                        uint32_t r[4];
+                        philox(seed, (uint32_t)i, (uint32_t)j, 0u, 10u, r);
+                        const double u = ((double)(r[0] >> 5) * 67108864.0 + (double)(r[1] >> 6)) *
+                                         (1.0 / 9007199254740992.0);
+                        if (u < exp(-(double)d2 * inv_2var)) {
+                            if (indices && total < capacity) indices[total] = j;
+                            ++total;
+                        }
+                    }
+                }
+        offsets[i + 1] = (int)total;
+    }
+    free(cell); free(cc); free(start); free(members); free(fillp);
+    return total;
+}
+
 int orc_sim_step(orc_sim* s, uint64_t step, int32_t* spikes)
 {
     const int n = s->n, D = s->D;

@@ -157,6 +157,8 @@ void orc_gen_er(int n, double p, float wmax, uint64_t seed, orc_csr* out);
  * lattice offsets from a discretised Gaussian table (sigma in lattice units),
  * lognormal(mu, s) weights, delay 1 + floor(u * dmax). */
 void orc_gauss_table(double sigma_sites, int16_t* table4096);
+int64_t orc_local_gaussian(int n, const float* x, const float* y, const float* z, float stddev, int n_stddevs,
+                           uint64_t seed, int* offsets, int* indices, int64_t capacity);
 void orc_block_tables(int n, int R, double size_sigma, double density_sigma, int dmax, uint64_t seed,
                       int* start, int* size, uint32_t* cum, uint8_t* pdelay);
 void orc_gen_block(int n, int k, int R, double size_sigma, double density_sigma, int dmax, double w_mu,
