@@ -44,7 +44,7 @@ WORKLOADS = {
                size_sigma=1.0, density_sigma=1.0, w_mu=-1.0, w_sigma=1.0, dmax=40, inh=0.2, i_lo=6.0, i_hi=12.0,
                grid=192, timescale=100, par_D=1.0, par_decay=0.0, total_steps=500),
     "c4": dict(workload="batch256_er_1k-64k_grids32-64", kind="batch", n_inst=256, size_lo=1000, size_hi=64000,
-               p_lo=0.005, p_hi=0.05, gna_lo=0.8, gna_hi=1.2, drive_lo=4.0, drive_hi=16.0, w_max=0.5, inh=0.2,
+               p_lo=0.005, p_hi=0.05, gna_lo=0.8, gna_hi=1.2, drive_lo=4.0, drive_hi=16.0, w_total=2.5, inh=0.2,
                grid_lo=32, grid_hi=64, timescale=100, par_D=1.0, par_decay=0.0, total_steps=2000),
     "c5": dict(workload="cg_256cube_lognormalD_s1_l8_uptake0.1", kind="cg", grid=256, sigma=1.0, corr=8.0,
                D0=1.0, uptake=0.1, dt_s=1e-3, neurons=20000, rate=2.0,
@@ -423,7 +423,12 @@ def run_batch(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     sim = nn.Simulation(ctx, c)
     sim.set_instances(off, sides)
     t0 = time.perf_counter()
-    nnz = sim.generate_batch_er(p, w_max=wl["w_max"], inh_fraction=wl["inh"])
+    # weight ceiling per instance: the expected total synaptic weight onto a
+    # neuron (in-degree p * size times mean weight w_max / 2) stays that of the
+    # 1k-neuron configuration (10 inputs, weights U[0, 0.5]: 2.5 nS), so large
+    # dense instances are not driven into an unstable conductance regime
+    w_inst = (wl["w_total"] * 2.0 / (p * sizes)).astype(np.float32)
+    nnz = sim.generate_batch_er(p, w_max=w_inst, inh_fraction=wl["inh"])
     t_gen = time.perf_counter() - t0
     sim.init_state(-65.0, 0.0, 0.0)
     sim.set_field("GNA_SCALE", np.repeat(gna, sizes))
@@ -474,6 +479,7 @@ def run_batch(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "data": "synthetic (seeded counter-based generators)",
         "config": {"workload": wl["workload"], "instances": int(wl["n_inst"]), "neurons": n, "synapses": int(nnz),
                    "timesteps_per_step": P, "grid_cells": int(sim.field_cells()),
+                   "weights": "U[0, w_b], w_b = 2 * 2.5 nS / (p_b * size_b) per instance",
                    "autotuned": {"threads_per_block": tpb, "neurons_per_thread": npt, "trial_ms_per_step": tune_ms},
                    "network_generation_s": t_gen, "l2": "inputs larger than L2"},
         "spikes_in_timed_region": spikes_b - spikes_a,

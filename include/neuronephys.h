@@ -266,6 +266,7 @@ typedef struct nn_net_spec {
     double region_size_sigma, density_sigma;
     int block_dmax;        /* BLOCK: delays 1..block_dmax by centroid distance */
     const double* inst_p;  /* ER on a batch (nn_sim_set_instances): one p per instance, else NULL */
+    const float* inst_w_max; /* ER on a batch: one w_max per instance (NULL: w_max for all) */
 } nn_net_spec;
 NN_API void nn_net_spec_default(nn_net_spec* sp, int kind);
 NN_API nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* spec);

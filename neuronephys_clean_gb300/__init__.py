@@ -484,11 +484,16 @@ class Simulation:
         self.n_inst = len(off) - 1
         self._inst = (off, gs)
 
-    def generate_batch_er(self, p_per_instance, w_max: float = 0.5, inh_fraction: float = 0.2) -> int:
-        """Block-diagonal Erdos-Renyi network, one p per instance."""
+    def generate_batch_er(self, p_per_instance, w_max=0.5, inh_fraction: float = 0.2) -> int:
+        """Block-diagonal Erdos-Renyi network, one p (and optionally one
+        w_max) per instance."""
         spec = default_net_spec(NN_NET_ER)
         self._inst_p = np.ascontiguousarray(p_per_instance, np.float64)
         spec.inst_p = self._inst_p.ctypes.data
+        if np.ndim(w_max):
+            self._inst_w = np.ascontiguousarray(w_max, np.float32)
+            spec.inst_w_max = self._inst_w.ctypes.data
+            w_max = 0.0
         spec.w_max, spec.inh_fraction = w_max, inh_fraction
         return self.generate_network(spec)
 

@@ -49,7 +49,7 @@ class NetSpec(C.Structure):
                 ("sigma", c_double), ("w_mu", c_double), ("w_sigma", c_double), ("dmax", c_int),
                 ("inh_fraction", c_double), ("inh_random", c_int), ("n_regions", c_int),
                 ("region_size_sigma", c_double), ("density_sigma", c_double),
-                ("block_dmax", c_int), ("inst_p", c_void_p)]
+                ("block_dmax", c_int), ("inst_p", c_void_p), ("inst_w_max", c_void_p)]
 
 
 class SolveStats(C.Structure):

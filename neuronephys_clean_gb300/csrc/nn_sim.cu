@@ -437,6 +437,7 @@ struct ErRows {
     uint64_t seed;
     const int* inst_off;   // null: one network
     const uint32_t* inst_thr;
+    const float* inst_wmax;  // null: the network's w_max
     int n_inst;
 };
 
@@ -484,7 +485,8 @@ __global__ void k_er_count(ErRows g, int64_t* cnt)
     }
 }
 
-__global__ void k_er_fill(ErRows g, float wmax, const int64_t* row_ptr, int32_t* col, float* weight, uint8_t* delay)
+__global__ void k_er_fill(ErRows g, float wmax_all, const int64_t* row_ptr, int32_t* col, float* weight,
+                          uint8_t* delay)
 {
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -493,6 +495,7 @@ __global__ void k_er_fill(ErRows g, float wmax, const int64_t* row_ptr, int32_t*
         uint32_t thr;
         uint64_t key;
         er_row(g, i, li, base, size, thr, key);
+        const float wmax = g.inst_wmax ? g.inst_wmax[instance_of(g.inst_off, g.n_inst, i)] : wmax_all;
         const int nb = (size + 3) >> 2;
         int64_t pos = row_ptr[i];
         int e_run = 0;
@@ -1153,8 +1156,9 @@ extern "C" nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* sp)
         int64_t* cnt = nullptr;
         NN_TRY(nn_alloc(ctx, &cnt, (size_t)n + 1));
         NN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int64_t) * ((size_t)n + 1), cs));
-        ErRows g{n, thr, seed, nullptr, nullptr, 0};
+        ErRows g{n, thr, seed, nullptr, nullptr, nullptr, 0};
         uint32_t* d_thr = nullptr;
+        float* d_wmax = nullptr;
         if (s->n_inst > 0 && sp->inst_p) {
             // a batch: the instances' own probabilities
             std::vector<uint32_t> th((size_t)s->n_inst);
@@ -1169,6 +1173,12 @@ extern "C" nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* sp)
             g.inst_off = s->inst_off;
             g.inst_thr = d_thr;
             g.n_inst = s->n_inst;
+            if (sp->inst_w_max) {
+                NN_TRY(nn_alloc(ctx, &d_wmax, (size_t)s->n_inst));
+                NN_CUDA(ctx, cudaMemcpyAsync(d_wmax, sp->inst_w_max, sizeof(float) * s->n_inst, cudaMemcpyHostToDevice,
+                                             cs));
+                g.inst_wmax = d_wmax;
+            }
         }
         k_er_count<<<nn_grid_for(ctx, (int64_t)n * 32, 256, 16), 256, 0, cs>>>(g, cnt);
         NN_CHECK_LAUNCH(ctx, "k_er_count");
@@ -1185,6 +1195,7 @@ extern "C" nn_status nn_sim_generate_network(nn_sim* s, const nn_net_spec* sp)
         NN_CHECK_LAUNCH(ctx, "k_er_fill");
         NN_CUDA(ctx, cudaStreamSynchronize(cs));
         if (d_thr) cudaFree(d_thr);
+        if (d_wmax) cudaFree(d_wmax);
     } else if (sp->kind == NN_NET_GAUSS || sp->kind == NN_NET_BLOCK) {
         if (sp->k < 0 || (int64_t)n * sp->k >= ((int64_t)1 << 32))
             return nn_fail(ctx, NN_ERR_INVALID_ARG, "out-degree k out of range");

@@ -30,6 +30,8 @@ def batch_sim(ctx, seed=11, delivery=0, grids=True, raster=100000):
     s.set_instances(off, GRIDS if grids else None)
     s.generate_batch_er(P, w_max=0.5, inh_fraction=0.2)
     s.init_state(-65.0, 5.0, 15.0)
+    # potentials spread over [-65, -35] mV so spikes (and deposits) start at once
+    s.set_field("V", np.random.default_rng(seed).uniform(-65, -35, n).astype(np.float32))
     return s, off
 
 
@@ -98,6 +100,21 @@ def test_batch_simulation_matches_oracle(ctx, orc):
         if np.linalg.norm(refu) > 0:
             assert np.linalg.norm(u[lo:hi] - refu) <= 1e-4 * np.linalg.norm(refu), b
             assert iters[b] > 0
+
+
+def test_per_instance_weight_ceiling(ctx):
+    n = sum(SIZES)
+    c = nn.default_config(n)
+    c.seed, c.grid = 2, 0
+    s = nn.Simulation(ctx, c)
+    off = np.concatenate([[0], np.cumsum(SIZES)])
+    s.set_instances(off)
+    wmax = np.array([0.1, 0.2, 0.3, 0.4, 0.5], np.float32)
+    s.generate_batch_er(P, w_max=wmax)
+    rp, col, w, _, _ = s.get_network()
+    for b in range(len(SIZES)):
+        wb = w[rp[off[b]]:rp[off[b + 1]]]
+        assert wb.max() <= wmax[b] and wb.max() > 0.5 * wmax[b]
 
 
 def test_autotune_keeps_state_and_results(ctx):
