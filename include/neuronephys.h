@@ -231,6 +231,8 @@ typedef struct nn_sim_config {
     int par_max_iter;
     int threads_per_block; /* 0 = autotuned default */
     int neurons_per_thread;/* 1, 2 or 4; 0 = autotuned default */
+    int par_overlap;       /* 1 (default): when the field does not feed back (g_par == 0), each period's
+                              field solve runs on its own stream, overlapping the next period's steps */
     int par_extrapolate;   /* 1: initial guess 2 u_n - u_(n-1) from the second solve on; 0 (default): u_n.
                               Helps when the sources change slowly; with spike deposits that are new every
                               period it costs iterations (95 -> 103 on the 1M-neuron workload). */

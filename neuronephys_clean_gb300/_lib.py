@@ -41,7 +41,7 @@ class SimConfig(C.Structure):
                 ("delivery", c_int), ("raster_capacity", c_int64), ("grid", c_int),
                 ("timescale", c_int), ("par_D", c_float), ("par_decay", c_float),
                 ("par_rtol", c_double), ("par_max_iter", c_int), ("threads_per_block", c_int),
-                ("neurons_per_thread", c_int), ("par_extrapolate", c_int)]
+                ("neurons_per_thread", c_int), ("par_overlap", c_int), ("par_extrapolate", c_int)]
 
 
 class NetSpec(C.Structure):

@@ -309,16 +309,16 @@ extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides,
     if (st == NN_OK) st = nn_alloc(ctx, &bp->p0, G);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->p1, G);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->Ap, G);
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpy(bp->side, h_sides, sizeof(int) * n_inst, cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->side, h_sides, sizeof(int) * n_inst, cudaMemcpyHostToDevice), "copy");
     if (st == NN_OK)
-        st = nn_cuda_check(ctx, cudaMemcpy(bp->off, bp->h_off.data(), sizeof(int64_t) * (n_inst + 1), cudaMemcpyHostToDevice), "copy");
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpy(bp->alpha, al.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpy(bp->invd, iv.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->off, bp->h_off.data(), sizeof(int64_t) * (n_inst + 1), cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->alpha, al.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->invd, iv.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
     if (st == NN_OK)
-        st = nn_cuda_check(ctx, cudaMemcpy(bp->blk_inst, binst.data(), sizeof(int) * binst.size(), cudaMemcpyHostToDevice), "copy");
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->blk_inst, binst.data(), sizeof(int) * binst.size(), cudaMemcpyHostToDevice), "copy");
     if (st == NN_OK)
-        st = nn_cuda_check(ctx, cudaMemcpy(bp->blk_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice), "copy");
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemset(bp->ticket, 0, sizeof(unsigned int) * n_inst), "memset");
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->blk_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, bp->ticket, sizeof(unsigned int) * n_inst), "memset");
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&bp->ev0), "event");
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&bp->ev1), "event");
     if (st != NN_OK) {
@@ -397,8 +397,8 @@ extern "C" nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, do
         NN_CUDA(ctx, cudaEventElapsedTime(&bp->last_ms, bp->ev0, bp->ev1));
     }
     std::vector<int> its(bp->n_inst), fl(bp->n_inst);
-    NN_CUDA(ctx, cudaMemcpy(its.data(), bp->iters, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
-    NN_CUDA(ctx, cudaMemcpy(fl.data(), bp->flags, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, nn_copy_sync(ctx, its.data(), bp->iters, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, nn_copy_sync(ctx, fl.data(), bp->flags, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
     int mx = 0, bad = 0;
     for (int b = 0; b < bp->n_inst; ++b) {
         mx = std::max(mx, its[(size_t)b]);

@@ -514,6 +514,17 @@ struct nn_cg_plan {
     std::vector<cudaEvent_t> ev_a, ev_b;
     float last_ms = 0.0f;
     int last_iters = 0;
+    // asynchronous solve in progress (nn_cg_async_*)
+    struct {
+        bool active = false;
+        float* x = nullptr;
+        CUtensorMap map_x;
+        double rtol = 0.0;
+        int max_iter = 0;
+        int enqueued = 0;
+        cudaStream_t cs = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+    } as;
 };
 
 void nn_cg_plan_destroy(nn_cg_plan* pl)
@@ -532,6 +543,8 @@ void nn_cg_plan_destroy(nn_cg_plan* pl)
     nn_release(pl->flags);
     for (auto e : pl->ev_a) cudaEventDestroy(e);
     for (auto e : pl->ev_b) cudaEventDestroy(e);
+    if (pl->as.e0) cudaEventDestroy(pl->as.e0);
+    if (pl->as.e1) cudaEventDestroy(pl->as.e1);
     nn_ctx* ctx = pl->ctx;
     delete pl;
     nn_ctx_release(ctx);
@@ -654,6 +667,106 @@ static CgArgs cg_args(nn_cg_plan* pl, float* x, double rtol, int max_iter, int p
     a.rtol2 = rtol * rtol;
     a.max_iter = max_iter;
     return a;
+}
+
+// init kernels (r0, w0, scalars) on stream cs
+static nn_status enqueue_init(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, int max_iter, cudaStream_t cs)
+{
+    nn_ctx* ctx = pl->ctx;
+    NN_CUDA(ctx, cudaMemsetAsync(pl->ticket, 0, sizeof(unsigned int), cs));  // clean after an aborted solve
+    CgArgs a0 = cg_args(pl, d_x, rtol, max_iter, 0);
+    if (pl->D) {
+        k_cg_init_r<true><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, d_b, d_x, pl->r[0]);
+        NN_CHECK_LAUNCH(ctx, "k_cg_init_r");
+        k_cg_init_w<true><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, pl->r[0], pl->w[0], pl->s[0]);
+    } else {
+        k_cg_init_r<false><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, d_b, d_x, pl->r[0]);
+        NN_CHECK_LAUNCH(ctx, "k_cg_init_r");
+        k_cg_init_w<false><<<pl->init_blocks, CG_THREADS, 0, cs>>>(a0, pl->r[0], pl->w[0], pl->s[0]);
+    }
+    NN_CHECK_LAUNCH(ctx, "k_cg_init_w");
+    return NN_OK;
+}
+
+// iterations it0 .. it0 + n - 1 (each a no-op once the device flag is set)
+static nn_status enqueue_iters(nn_cg_plan* pl, float* d_x, const CUtensorMap& map_x, double rtol, int max_iter, int it0,
+                               int n, cudaStream_t cs)
+{
+    nn_ctx* ctx = pl->ctx;
+    for (int it = it0; it < it0 + n; ++it) {
+        const int pin = it & 1, pout = pin ^ 1;
+        CgArgs a = cg_args(pl, d_x, rtol, max_iter, pout);
+        if (pl->D)
+            k_cg_iter<true><<<pl->tiles, CG_THREADS, Layout<true>::SMEM_BYTES, cs>>>(
+                pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], pl->map_d, pl->map_m, pl->map_p, map_x, a);
+        else
+            k_cg_iter<false><<<pl->tiles, CG_THREADS, Layout<false>::SMEM_BYTES, cs>>>(
+                pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], pl->map_p, pl->map_p, pl->map_p, map_x, a);
+        NN_CHECK_LAUNCH(ctx, "k_cg_iter");
+    }
+    return NN_OK;
+}
+
+// Asynchronous solve on stream cs: the init and n iterations are enqueued
+// with no host read; nn_cg_async_more adds iterations; nn_cg_async_finish
+// waits for the stream, completes the solve if n was not enough and reports.
+nn_status nn_cg_async_begin(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, int max_iter, int n,
+                            cudaStream_t cs)
+{
+    nn_ctx* ctx = pl->ctx;
+    if (((uintptr_t)d_x & 15) || !make_map(&pl->as.map_x, d_x, pl->nx, pl->ny, pl->nz, false))
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_cg_async_begin: x must be a 16-byte aligned device vector");
+    if (!pl->as.e0) NN_CUDA(ctx, cudaEventCreate(&pl->as.e0));
+    if (!pl->as.e1) NN_CUDA(ctx, cudaEventCreate(&pl->as.e1));
+    pl->as.active = true;
+    pl->as.x = d_x;
+    pl->as.rtol = rtol;
+    pl->as.max_iter = max_iter;
+    pl->as.cs = cs;
+    pl->as.enqueued = 0;
+    if (pl->timing) NN_CUDA(ctx, cudaEventRecord(pl->as.e0, cs));
+    NN_TRY(enqueue_init(pl, d_b, d_x, rtol, max_iter, cs));
+    return nn_cg_async_more(pl, n);
+}
+
+nn_status nn_cg_async_more(nn_cg_plan* pl, int n)
+{
+    if (!pl->as.active) return NN_ERR_INVALID_ARG;
+    n = std::min(n, pl->as.max_iter - pl->as.enqueued);
+    if (n <= 0) return NN_OK;
+    NN_TRY(enqueue_iters(pl, pl->as.x, pl->as.map_x, pl->as.rtol, pl->as.max_iter, pl->as.enqueued, n, pl->as.cs));
+    pl->as.enqueued += n;
+    if (pl->timing) NN_CUDA(pl->ctx, cudaEventRecord(pl->as.e1, pl->as.cs));
+    return NN_OK;
+}
+
+nn_status nn_cg_async_finish(nn_cg_plan* pl, int* iters, double* relres, int* converged)
+{
+    nn_ctx* ctx = pl->ctx;
+    if (!pl->as.active) return NN_ERR_INVALID_ARG;
+    cudaStream_t cs = pl->as.cs;
+    int h_flags[4] = {0, 0, 0, 0};
+    while (true) {
+        NN_CUDA(ctx, cudaMemcpyAsync(h_flags, pl->flags, sizeof h_flags, cudaMemcpyDeviceToHost, cs));
+        NN_CUDA(ctx, cudaStreamSynchronize(cs));
+        if (h_flags[0] || pl->as.enqueued >= pl->as.max_iter) break;
+        NN_TRY(nn_cg_async_more(pl, 16));
+    }
+    double h_scal[C_COUNT];
+    NN_CUDA(ctx, cudaMemcpyAsync(h_scal, pl->scal, sizeof h_scal, cudaMemcpyDeviceToHost, cs));
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    pl->as.active = false;
+    if (h_flags[2]) return nn_fail(ctx, NN_ERR_TIMEOUT, "k_cg_iter: a TMA pipeline wait timed out");
+    if (pl->timing) {
+        float ms = 0.0f;
+        NN_CUDA(ctx, cudaEventElapsedTime(&ms, pl->as.e0, pl->as.e1));
+        pl->last_ms = ms;
+        pl->last_iters = h_flags[1];
+    }
+    if (iters) *iters = h_flags[1];
+    if (relres) *relres = h_scal[C_BB] > 0 ? std::sqrt(h_scal[C_RR] / h_scal[C_BB]) : 0.0;
+    if (converged) *converged = h_flags[0] == 1;
+    return NN_OK;
 }
 
 // Solve A x = b (x holds the initial guess).  Iterations are enqueued in

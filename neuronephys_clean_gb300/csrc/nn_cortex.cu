@@ -197,7 +197,7 @@ extern "C" nn_status nn_net_local_gaussian(nn_ctx* ctx, int n, const float* d_x,
     }
     // offsets (int, as the reference's AdjacencyList)
     std::vector<int> hcnt((size_t)n), hoff((size_t)n + 1, 0);
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpy(hcnt.data(), cnt, sizeof(int) * n, cudaMemcpyDeviceToHost), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_copy_sync(ctx, hcnt.data(), cnt, sizeof(int) * n, cudaMemcpyDeviceToHost), "copy");
     int64_t total = 0;
     for (int i = 0; i < n && st == NN_OK; ++i) {
         total += hcnt[(size_t)i];
@@ -205,7 +205,7 @@ extern "C" nn_status nn_net_local_gaussian(nn_ctx* ctx, int n, const float* d_x,
         hoff[(size_t)i + 1] = (int)total;
     }
     if (st == NN_OK)
-        st = nn_cuda_check(ctx, cudaMemcpy(d_offsets, hoff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice), "copy");
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, d_offsets, hoff.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice), "copy");
     *nnz = total;
     if (st == NN_OK && d_indices) {
         if (capacity < total) {

@@ -72,6 +72,16 @@ void nn_release(T*& p)
     p = nullptr;
 }
 
+// The context stream is non-blocking: legacy-stream copies and memsets are
+// not ordered with its kernels.  These go through the context stream.
+inline cudaError_t nn_copy_sync(nn_ctx* ctx, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind)
+{
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e;
+}
+inline cudaError_t nn_zero_async(nn_ctx* ctx, void* p, size_t bytes) { return cudaMemsetAsync(p, 0, bytes, ctx->stream); }
+
 inline int nn_grid_for(const nn_ctx* ctx, int64_t work, int threads, int per_sm = 8)
 {
     int64_t b = (work + threads - 1) / threads;
@@ -160,6 +170,14 @@ void nn_cg_plan_destroy(nn_cg_plan* pl);
 nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
                     double* relres, int* converged);
 void nn_cg_set_timing(nn_cg_plan* pl, bool on);
+nn_status nn_cg_async_begin(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, int max_iter, int n,
+                            cudaStream_t cs);
+nn_status nn_cg_async_more(nn_cg_plan* pl, int n);
+nn_status nn_cg_async_finish(nn_cg_plan* pl, int* iters, double* relres, int* converged);
+nn_status nn_pcg_async_begin(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int n,
+                             cudaStream_t cs);
+nn_status nn_pcg_async_finish(nn_pcg* pc, int* iters, double* relres, int* converged);
+bool nn_pcg_async_supported(const nn_pcg* pc);
 void nn_cg_last_timing(const nn_cg_plan* pl, float* ms, int* iters);
 double nn_host_inv_phi(double p);
 void nn_host_gauss_table(double sigma_sites, int16_t* table4096);

@@ -506,6 +506,23 @@ extern "C" nn_status nn_pcg_kernel_time(nn_pcg* pc, float* ms, int* iters)
     return NN_OK;
 }
 
+// Asynchronous solve on a stream (single-kernel path only; UNSUPPORTED
+// otherwise): n iterations enqueued now, the rest and the outcome at finish.
+nn_status nn_pcg_async_begin(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int n,
+                             cudaStream_t cs)
+{
+    if (!pc->fast) return NN_ERR_UNSUPPORTED;
+    return nn_cg_async_begin(pc->fast, d_b, d_x, rtol, max_iter, n, cs);
+}
+
+nn_status nn_pcg_async_finish(nn_pcg* pc, int* iters, double* relres, int* converged)
+{
+    if (!pc->fast) return NN_ERR_UNSUPPORTED;
+    return nn_cg_async_finish(pc->fast, iters, relres, converged);
+}
+
+bool nn_pcg_async_supported(const nn_pcg* pc) { return pc->fast != nullptr; }
+
 // The single-kernel TMA iteration when the grid allows it, else two kernels.
 nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
                           double* relres, int* converged)

@@ -161,11 +161,11 @@ extern "C" nn_status nn_electrodes_create(nn_ctx* ctx, const int* h_indices, con
     if (st == NN_OK) st = nn_alloc(ctx, &e->avg, (size_t)n_regions);
     if (st == NN_OK) st = nn_alloc(ctx, &e->nfiring, (size_t)n_regions);
     if (st == NN_OK)
-        st = nn_cuda_check(ctx, cudaMemcpy(e->idx, h_indices, sizeof(int) * nidx, cudaMemcpyHostToDevice), "copy");
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, e->idx, h_indices, sizeof(int) * nidx, cudaMemcpyHostToDevice), "copy");
     if (st == NN_OK)
-        st = nn_cuda_check(ctx, cudaMemcpy(e->off, h_offsets, sizeof(int) * (n_regions + 1), cudaMemcpyHostToDevice),
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, e->off, h_offsets, sizeof(int) * (n_regions + 1), cudaMemcpyHostToDevice),
                            "copy");
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemset(e->nfiring, 0, sizeof(int) * n_regions), "memset");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, e->nfiring, sizeof(int) * n_regions), "memset");
     if (st != NN_OK) {
         nn_electrodes_destroy(e);
         return st;
@@ -255,9 +255,9 @@ extern "C" nn_status nn_synchrony_create(nn_ctx* ctx, const int* h_region_inds, 
     if (st == NN_OK) st = nn_alloc(ctx, &s->vi, (size_t)n_inds);
     if (st == NN_OK) st = nn_alloc(ctx, &s->sub_sum, (size_t)n_sub);
     if (st == NN_OK)
-        st = nn_cuda_check(ctx, cudaMemcpy(s->idx, h_region_inds, sizeof(int) * n_inds, cudaMemcpyHostToDevice), "copy");
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemset(s->vi2, 0, sizeof(double) * n_inds), "memset");
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemset(s->vi, 0, sizeof(double) * n_inds), "memset");
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, s->idx, h_region_inds, sizeof(int) * n_inds, cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, s->vi2, sizeof(double) * n_inds), "memset");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, s->vi, sizeof(double) * n_inds), "memset");
     if (st != NN_OK) {
         nn_synchrony_destroy(s);
         return st;
@@ -310,8 +310,8 @@ extern "C" nn_status nn_synchrony_get(nn_synchrony* s, double* h_chi)
     nn_ctx* ctx = s->ctx;
     std::vector<double> vi2(s->n), vi(s->n);
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    NN_CUDA(ctx, cudaMemcpy(vi2.data(), s->vi2, sizeof(double) * s->n, cudaMemcpyDeviceToHost));
-    NN_CUDA(ctx, cudaMemcpy(vi.data(), s->vi, sizeof(double) * s->n, cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, nn_copy_sync(ctx, vi2.data(), s->vi2, sizeof(double) * s->n, cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, nn_copy_sync(ctx, vi.data(), s->vi, sizeof(double) * s->n, cudaMemcpyDeviceToHost));
     const double T = s->steps;
     if (T > 0)
         for (int i = 0; i < s->n; ++i) {
@@ -358,8 +358,8 @@ extern "C" nn_status nn_hebbian_create(nn_ctx* ctx, int window, float inc, int64
     if (st == NN_OK) st = nn_alloc(ctx, &h->row_left, (size_t)n_neurons);
     if (st == NN_OK) st = nn_alloc(ctx, &h->rows, (size_t)n_neurons);
     if (st == NN_OK) st = nn_alloc(ctx, &h->nrows, 1);
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemset(h->timers, 0, sizeof(int) * std::max<int64_t>(nconns, 1)), "memset");
-    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemset(h->row_left, 0, sizeof(int) * n_neurons), "memset");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, h->timers, sizeof(int) * std::max<int64_t>(nconns, 1)), "memset");
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, h->row_left, sizeof(int) * n_neurons), "memset");
     if (st != NN_OK) {
         nn_hebbian_destroy(h);
         return st;
@@ -412,6 +412,6 @@ extern "C" nn_status nn_hebbian_timers(nn_hebbian* h, int* h_timers)
 {
     if (!h || !h_timers) return NN_ERR_INVALID_ARG;
     NN_CUDA(h->ctx, cudaStreamSynchronize(h->ctx->stream));
-    NN_CUDA(h->ctx, cudaMemcpy(h_timers, h->timers, sizeof(int) * h->nconns, cudaMemcpyDeviceToHost));
+    NN_CUDA(h->ctx, nn_copy_sync(h->ctx, h_timers, h->timers, sizeof(int) * h->nconns, cudaMemcpyDeviceToHost));
     return NN_OK;
 }

@@ -72,6 +72,14 @@ struct nn_sim {
     int64_t* inst_goff = nullptr;  // device [n_inst + 1] cell offsets
     nn_bpcg* bpcg = nullptr;
     std::vector<int> inst_iters;
+    // overlapped field solve: with no feedback of the field into the neurons
+    // (g_par == 0) a period's solve runs on its own stream while the next
+    // period's steps run; the main stream waits for it only before the next
+    // right-hand side is formed
+    cudaStream_t par_stream = nullptr;
+    cudaEvent_t ev_rhs = nullptr, ev_solved = nullptr;
+    bool solve_pending = false;
+    int iter_estimate = 64;
     nn_solve_stats stats{};
     // host mirrors
     int64_t host_step = 0;
@@ -730,6 +738,7 @@ extern "C" void nn_sim_config_default(nn_sim_config* c, int n)
     c->par_rtol = 1e-6;
     c->par_max_iter = 2000;
     c->par_extrapolate = 0;
+    c->par_overlap = 1;
 }
 
 extern "C" void nn_net_spec_default(nn_net_spec* sp, int kind)
@@ -901,6 +910,7 @@ static void free_network(nn_sim* s)
 extern "C" nn_status nn_sim_destroy(nn_sim* s)
 {
     if (!s) return NN_OK;
+    if (s->par_stream) cudaStreamSynchronize(s->par_stream);
     if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
     drop_graph(s);
     for (int q = 0; q < NN_F_COUNT; ++q) nn_release(s->f[q]);
@@ -911,6 +921,9 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     if (s->pcg) nn_pcg_destroy(s->pcg);
     if (s->bpcg) nn_bpcg_destroy(s->bpcg);
     nn_release(s->inst_off); nn_release(s->inst_grid); nn_release(s->inst_goff);
+    if (s->par_stream) cudaStreamDestroy(s->par_stream);
+    if (s->ev_rhs) cudaEventDestroy(s->ev_rhs);
+    if (s->ev_solved) cudaEventDestroy(s->ev_solved);
     for (auto e : s->ev_a) cudaEventDestroy(e);
     for (auto e : s->ev_b) cudaEventDestroy(e);
     for (auto e : s->ev_c) cudaEventDestroy(e);
@@ -1096,7 +1109,7 @@ extern "C" nn_status nn_sim_set_instances(nn_sim* s, int n_inst, const int* h_of
     s->n_inst = n_inst;
     s->h_inst_off.assign(h_offsets, h_offsets + n_inst + 1);
     NN_TRY(nn_alloc(ctx, &s->inst_off, (size_t)n_inst + 1));
-    NN_CUDA(ctx, cudaMemcpy(s->inst_off, h_offsets, sizeof(int) * (n_inst + 1), cudaMemcpyHostToDevice));
+    NN_CUDA(ctx, nn_copy_sync(ctx, s->inst_off, h_offsets, sizeof(int) * (n_inst + 1), cudaMemcpyHostToDevice));
     if (h_grid_sides) {
         s->h_inst_grid.assign(h_grid_sides, h_grid_sides + n_inst);
         const double dt_s = (double)s->cfg.timescale * s->cfg.hp.dt * 1e-3;
@@ -1104,16 +1117,16 @@ extern "C" nn_status nn_sim_set_instances(nn_sim* s, int n_inst, const int* h_of
         s->G = nn_bpcg_cells(s->bpcg);
         NN_TRY(nn_alloc(ctx, &s->inst_grid, (size_t)n_inst));
         NN_TRY(nn_alloc(ctx, &s->inst_goff, (size_t)n_inst + 1));
-        NN_CUDA(ctx, cudaMemcpy(s->inst_grid, h_grid_sides, sizeof(int) * n_inst, cudaMemcpyHostToDevice));
-        NN_CUDA(ctx, cudaMemcpy(s->inst_goff, nn_bpcg_offsets(s->bpcg), sizeof(int64_t) * (n_inst + 1),
+        NN_CUDA(ctx, nn_copy_sync(ctx, s->inst_grid, h_grid_sides, sizeof(int) * n_inst, cudaMemcpyHostToDevice));
+        NN_CUDA(ctx, nn_copy_sync(ctx, s->inst_goff, nn_bpcg_offsets(s->bpcg), sizeof(int64_t) * (n_inst + 1),
                                 cudaMemcpyHostToDevice));
         NN_TRY(nn_alloc(ctx, &s->vox, (size_t)s->n_pad));
         NN_TRY(nn_alloc(ctx, &s->src, (size_t)s->G));
         NN_TRY(nn_alloc(ctx, &s->u, (size_t)s->G));
         NN_TRY(nn_alloc(ctx, &s->b, (size_t)s->G));
-        NN_CUDA(ctx, cudaMemset(s->vox, 0, sizeof(int32_t) * s->n_pad));
-        NN_CUDA(ctx, cudaMemset(s->src, 0, sizeof(float) * s->G));
-        NN_CUDA(ctx, cudaMemset(s->u, 0, sizeof(float) * s->G));
+        NN_CUDA(ctx, nn_zero_async(ctx, s->vox, sizeof(int32_t) * s->n_pad));
+        NN_CUDA(ctx, nn_zero_async(ctx, s->src, sizeof(float) * s->G));
+        NN_CUDA(ctx, nn_zero_async(ctx, s->u, sizeof(float) * s->G));
     }
     return NN_OK;
 }
@@ -1122,7 +1135,7 @@ extern "C" nn_status nn_sim_get_vox(nn_sim* s, int32_t* h_vox)
 {
     if (!s || !h_vox || !s->vox) return NN_ERR_INVALID_ARG;
     NN_CUDA(s->ctx, cudaStreamSynchronize(s->ctx->stream));
-    NN_CUDA(s->ctx, cudaMemcpy(h_vox, s->vox, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost));
+    NN_CUDA(s->ctx, nn_copy_sync(s->ctx, h_vox, s->vox, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost));
     return NN_OK;
 }
 
@@ -1478,14 +1491,56 @@ extern "C" nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out)
     return NN_OK;
 }
 
+static bool overlap_solve(const nn_sim* s)
+{
+    return s->cfg.par_overlap && s->cfg.hp.g_par == 0.0f && !s->bpcg && s->pcg && nn_pcg_async_supported(s->pcg);
+}
+
+// Complete an overlapped solve: wait for its stream, finish it if the
+// enqueued iterations were not enough, record its statistics.
+static nn_status finish_solve(nn_sim* s)
+{
+    if (!s->solve_pending) return NN_OK;
+    s->solve_pending = false;
+    int it = 0, conv = 0;
+    double rel = 0.0;
+    NN_TRY(nn_pcg_async_finish(s->pcg, &it, &rel, &conv));
+    s->stats.iterations = it;
+    s->stats.relres = rel;
+    s->stats.converged = conv;
+    s->iter_estimate = it + 8;
+    return NN_OK;
+}
+
 static nn_status paracrine_solve(nn_sim* s)
 {
     nn_ctx* ctx = s->ctx;
     cudaStream_t cs = ctx->stream;
+    const bool overlap = overlap_solve(s);
+    if (overlap) {
+        // the previous overlapped solve must be complete before b and u are reused
+        NN_TRY(finish_solve(s));
+        if (!s->par_stream) {
+            NN_CUDA(ctx, cudaStreamCreateWithFlags(&s->par_stream, cudaStreamNonBlocking));
+            NN_CUDA(ctx, cudaEventCreateWithFlags(&s->ev_rhs, cudaEventDisableTiming));
+            NN_CUDA(ctx, cudaEventCreateWithFlags(&s->ev_solved, cudaEventDisableTiming));
+        }
+        NN_CUDA(ctx, cudaStreamWaitEvent(cs, s->ev_solved, 0));
+    }
     k_par_rhs<<<nn_grid_for(ctx, s->G, 256, 8), 256, 0, cs>>>(s->u, s->src, s->b, s->u_prev, s->have_prev ? 1 : 0,
                                                                s->G);
     s->have_prev = s->u_prev != nullptr;
     NN_CHECK_LAUNCH(ctx, "k_par_rhs");
+    if (overlap) {
+        NN_CUDA(ctx, cudaEventRecord(s->ev_rhs, cs));
+        NN_CUDA(ctx, cudaStreamWaitEvent(s->par_stream, s->ev_rhs, 0));
+        NN_TRY(nn_pcg_async_begin(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, s->iter_estimate,
+                                  s->par_stream));
+        NN_CUDA(ctx, cudaEventRecord(s->ev_solved, s->par_stream));
+        s->solve_pending = true;
+        s->stats.solves += 1;
+        return NN_OK;
+    }
     int it = 0, conv = 0;
     double rel = 0.0;
     if (s->bpcg) {
@@ -1646,6 +1701,12 @@ extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
             left -= 1;
         }
         if (has_field(s) && (s->host_step % s->cfg.timescale) == 0) NN_TRY(paracrine_solve(s));
+    }
+    // the call's last overlapped solve completes before it returns, and the
+    // main stream is ordered after it
+    if (s->solve_pending) {
+        NN_TRY(finish_solve(s));
+        NN_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, s->ev_solved, 0));
     }
     return NN_OK;
 }

@@ -789,7 +789,7 @@ extern "C" nn_status nn_learned_train(nn_learned* lp, int steps, float lr, float
     }
     NN_TRY(check_err(u));
     double loss = 0.0;
-    NN_CUDA(ctx, cudaMemcpy(&loss, u->scal + 1, sizeof(double), cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, nn_copy_sync(ctx, &loss, u->scal + 1, sizeof(double), cudaMemcpyDeviceToHost));
     if (mean_loss) *mean_loss = steps ? (float)(loss / ((double)steps * u->G0)) : 0.0f;
     return NN_OK;
 }
@@ -870,9 +870,9 @@ extern "C" nn_status nn_learned_get_params(nn_learned* lp, float* h_out)
     int64_t off = 0;
     for (int l = 0; l < NL; ++l) {
         const auto& L = lp->net->L[l];
-        NN_CUDA(ctx, cudaMemcpy(h_out + off, L.w, sizeof(float) * L.nw, cudaMemcpyDeviceToHost));
+        NN_CUDA(ctx, nn_copy_sync(ctx, h_out + off, L.w, sizeof(float) * L.nw, cudaMemcpyDeviceToHost));
         off += L.nw;
-        NN_CUDA(ctx, cudaMemcpy(h_out + off, L.b, sizeof(float) * LCOUT[l], cudaMemcpyDeviceToHost));
+        NN_CUDA(ctx, nn_copy_sync(ctx, h_out + off, L.b, sizeof(float) * LCOUT[l], cudaMemcpyDeviceToHost));
         off += LCOUT[l];
     }
     return NN_OK;
@@ -886,9 +886,9 @@ extern "C" nn_status nn_learned_set_params(nn_learned* lp, const float* h_in)
     int64_t off = 0;
     for (int l = 0; l < NL; ++l) {
         auto& L = lp->net->L[l];
-        NN_CUDA(ctx, cudaMemcpy(L.w, h_in + off, sizeof(float) * L.nw, cudaMemcpyHostToDevice));
+        NN_CUDA(ctx, nn_copy_sync(ctx, L.w, h_in + off, sizeof(float) * L.nw, cudaMemcpyHostToDevice));
         off += L.nw;
-        NN_CUDA(ctx, cudaMemcpy(L.b, h_in + off, sizeof(float) * LCOUT[l], cudaMemcpyHostToDevice));
+        NN_CUDA(ctx, nn_copy_sync(ctx, L.b, h_in + off, sizeof(float) * LCOUT[l], cudaMemcpyHostToDevice));
         off += LCOUT[l];
         NN_TRY(unet_repack(lp->net, l));
     }
@@ -916,17 +916,17 @@ extern "C" nn_status nn_learned_net_gradient(nn_learned* lp, const float* d_rc, 
                   (uint4*)u->gOUT, u->g[0], u->scal + 1));
     NN_TRY(unet_backward(u));
     NN_TRY(check_err(u));
-    if (d_y) NN_CUDA(ctx, cudaMemcpy(d_y, u->y32, sizeof(float) * u->G0, cudaMemcpyDeviceToDevice));
+    if (d_y) NN_CUDA(ctx, nn_copy_sync(ctx, d_y, u->y32, sizeof(float) * u->G0, cudaMemcpyDeviceToDevice));
     double l2 = 0.0;
-    NN_CUDA(ctx, cudaMemcpy(&l2, u->scal + 1, sizeof(double), cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, nn_copy_sync(ctx, &l2, u->scal + 1, sizeof(double), cudaMemcpyDeviceToHost));
     if (loss) *loss = 0.5 * l2;
     if (h_grad) {
         int64_t off = 0;
         for (int l = 0; l < NL; ++l) {
             const auto& L = u->L[l];
-            NN_CUDA(ctx, cudaMemcpy(h_grad + off, L.gw, sizeof(float) * L.nw, cudaMemcpyDeviceToHost));
+            NN_CUDA(ctx, nn_copy_sync(ctx, h_grad + off, L.gw, sizeof(float) * L.nw, cudaMemcpyDeviceToHost));
             off += L.nw;
-            NN_CUDA(ctx, cudaMemcpy(h_grad + off, L.gb, sizeof(float) * LCOUT[l], cudaMemcpyDeviceToHost));
+            NN_CUDA(ctx, nn_copy_sync(ctx, h_grad + off, L.gb, sizeof(float) * LCOUT[l], cudaMemcpyDeviceToHost));
             off += LCOUT[l];
         }
     }
