@@ -329,29 +329,51 @@ struct PullArgs {
 
 // Pull: a warp per postsynaptic neuron sums its CSC column against the spike
 // bitmap of step t + 1 - delay and writes the complete input of step t + 1.
-// Deterministic: the column order and the warp reduction order are fixed.
+// Each lane takes four consecutive entries of a 128-entry window that starts
+// on a multiple of four (one 16-byte load of source words, one 4-byte load of
+// delays), so a column of up to 125 entries is a single pass; weights are read
+// only for entries whose source fired.  The slot of step t + 1 - d is
+// (s1 - d) mod D with s1 = (t + 1) mod D, in 32-bit arithmetic.
+// Deterministic: each lane adds its entries in column order, then the warp
+// tree reduction in a fixed order.
 __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
 {
-    const uint64_t t = *a.base + (uint64_t)a.q;
-    const int s1 = (int)((t + 1) % (uint64_t)a.D);
+    const uint64_t t1 = *a.base + (uint64_t)a.q + 1;
+    const int s1 = (int)(t1 % (uint64_t)a.D);
+    // delays longer than the elapsed steps reach back before step 0
+    const int dlim = t1 < (uint64_t)a.D ? (int)t1 : a.D;
     const int lane = threadIdx.x & 31;
     const int gw = blockIdx.x * (DELIV_THREADS / 32) + (threadIdx.x >> 5);
     const int nwarps = gridDim.x * (DELIV_THREADS / 32);
-    float* out = a.ring + (size_t)s1 * a.n_pad * 2;
+    float* out = a.ring + (size_t)(t1 % (uint64_t)a.D) * a.n_pad * 2;
     for (int k = gw; k < a.n; k += nwarps) {
         const int64_t beg = a.col_ptr[k], end = a.col_ptr[k + 1];
         float acc_e = 0.0f, acc_i = 0.0f;
-        for (int64_t e = beg + lane; e < end; e += 32) {
-            const int d = a.csc_d[e];
-            if ((uint64_t)d > t + 1) continue;
-            const uint64_t tau = t + 1 - (uint64_t)d;
-            const uint32_t s = a.csc_src[e];
-            const uint32_t sid = s & 0x7fffffffu;
-            const int hs = (int)(tau % (uint64_t)a.D);
-            const uint32_t word = a.bitmap[(size_t)hs * a.words + (sid >> 5)];
-            if ((word >> (sid & 31)) & 1u) {
-                if (s >> 31) acc_i += a.csc_w[e];
-                else acc_e += a.csc_w[e];
+        for (int64_t e0 = (beg & ~(int64_t)3) + 4 * lane; e0 < end; e0 += 128) {
+            const uint4 sv = *reinterpret_cast<const uint4*>(a.csc_src + e0);
+            const uint32_t dv = *reinterpret_cast<const uint32_t*>(a.csc_d + e0);
+            const uint32_t src[4] = {sv.x, sv.y, sv.z, sv.w};
+            uint32_t hit = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int d = (int)((dv >> (8 * j)) & 0xffu);
+                const int64_t e = e0 + j;
+                if (e >= beg && e < end && d <= dlim) {
+                    int hs = s1 - d;
+                    if (hs < 0) hs += a.D;
+                    const uint32_t sid = src[j] & 0x7fffffffu;
+                    const uint32_t word = a.bitmap[(size_t)hs * a.words + (sid >> 5)];
+                    hit |= ((word >> (sid & 31)) & 1u) << j;
+                }
+            }
+            if (hit) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if ((hit >> j) & 1u) {
+                        const float w = a.csc_w[e0 + j];
+                        if (src[j] >> 31) acc_i += w;
+                        else acc_e += w;
+                    }
             }
         }
         acc_e = nn_warp_sumf(acc_e);
@@ -941,10 +963,15 @@ static nn_status build_csc(nn_sim* s)
     uint32_t* edge_of = nullptr;
     NN_TRY(nn_alloc(ctx, &edge_of, (size_t)std::max<int64_t>(s->nnz, 1)));
     NN_TRY(nn_build_csc(ctx, s->n, s->nnz, s->row_ptr, s->col, s->col_ptr, edge_of));
-    const size_t E = (size_t)std::max<int64_t>(s->nnz, 1);
+    // the pull kernel reads whole groups of four entries: pad to a multiple
+    // of four (the padding is never summed)
+    const size_t E = ((size_t)std::max<int64_t>(s->nnz, 1) + 3) & ~(size_t)3;
     NN_TRY(nn_alloc(ctx, &s->csc_src, E));
     NN_TRY(nn_alloc(ctx, &s->csc_w, E));
     NN_TRY(nn_alloc(ctx, &s->csc_d, E));
+    NN_CUDA(ctx, nn_zero_async(ctx, s->csc_src, E * sizeof(uint32_t)));
+    NN_CUDA(ctx, nn_zero_async(ctx, s->csc_w, E * sizeof(float)));
+    NN_CUDA(ctx, nn_zero_async(ctx, s->csc_d, E));
     if (s->nnz > 0) {
         k_csc_gather<<<nn_grid_for(ctx, s->nnz, 256, 16), 256, 0, ctx->stream>>>(
             edge_of, s->nnz, s->row_ptr, s->n, s->weight, s->delay, s->is_inh, s->csc_src, s->csc_w, s->csc_d);
