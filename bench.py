@@ -582,6 +582,7 @@ def run_cg(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "e2e": {"value": 1e3 * statistics.mean(e2e_s), "unit": "ms", "h2d_bytes_per_step": 4 * G,
                 "d2h_bytes_per_step": 4 * G},
     }
+    line["multigrid"] = multigrid_cg(nn, ctx, pc, G, db, ms_solve, it_mean, args)
     if args.learned:
         line["learned"] = learned_cg(nn, ctx, pc, wl, shape, db, ms_solve, it_mean, args)
     if args.cpu_baseline:
@@ -589,6 +590,30 @@ def run_cg(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     pc.close()
     ctx.close()
     return line
+
+
+def multigrid_cg(nn, ctx, pc, G, db, plain_ms, plain_iters, args) -> dict:
+    """Flexible CG preconditioned by the geometric multigrid V-cycle on the
+    same problem, from x = 0 to the same relative residual."""
+    mg = nn.MultigridPCG(pc)
+    dx = ctx.empty((G,), np.float32)
+    for _ in range(max(1, args.warmup)):
+        dx.zero()
+        mg.solve(db, dx, 1e-6)
+    times, its, rel = [], [], 0.0
+    for _ in range(args.steps):
+        dx.zero()
+        ctx.time_begin()
+        it, rel = mg.solve(db, dx, 1e-6)
+        times.append(ctx.time_end())
+        its.append(it)
+    levels = mg.levels
+    mg.close()
+    ms = statistics.mean(times)
+    return {"ms_to_tol": ms, "iterations": statistics.mean(its), "relres": rel, "levels": levels,
+            "ms_per_iteration": ms / statistics.mean(its), "vs_plain_time": ms / plain_ms,
+            "vs_plain_iterations": statistics.mean(its) / plain_iters,
+            "solution_norm": float(np.linalg.norm(dx.numpy().astype(np.float64)))}
 
 
 def learned_cg(nn, ctx, pc, wl, shape, db, plain_ms, plain_iters, args) -> dict:

@@ -449,6 +449,23 @@ NN_API nn_status nn_conv3d_wgrad(nn_ctx* ctx, int nz, int ny, int nx, int cin, i
                                  const void* d_gy, float* d_dw, float* d_db);
 
 
+/* Geometric multigrid for the 7-point operator of an nn_pcg (no counterpart
+ * in the reference).  Cell-centred hierarchy (2x per axis while the sides stay
+ * even; levels = 0 picks the depth that leaves about 16^3 coarsest cells),
+ * 7-point coarse operators from the fine conductances, damped-Jacobi
+ * smoothing, trilinear prolongation.  nn_mg_apply runs one V-cycle (z = M r);
+ * nn_mg_solve runs flexible CG preconditioned by one V-cycle per iteration
+ * to the same relative residual as nn_pcg_solve (x holds the initial guess;
+ * NN_ERR_NOT_CONVERGED after max_iter iterations).  The nn_pcg (and its cell
+ * field) must outlive the nn_mg. */
+typedef struct nn_mg nn_mg;
+NN_API nn_status nn_mg_create(nn_pcg* pc, int levels, nn_mg** out);
+NN_API nn_status nn_mg_destroy(nn_mg* mg);
+NN_API nn_status nn_mg_levels(nn_mg* mg, int* levels);
+NN_API nn_status nn_mg_apply(nn_mg* mg, const float* d_r, float* d_z);
+NN_API nn_status nn_mg_solve(nn_mg* mg, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
+                             double* relres);
+
 /* Learned two-grid preconditioner for the 7-point operator of an nn_pcg
  * (grid sides multiples of 8): Jacobi smoothing on the fine grid and a
  * coarse-grid correction by a 3-level 3D conv U-Net (16/32/64 channels, BF16

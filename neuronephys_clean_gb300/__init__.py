@@ -24,7 +24,7 @@ from . import _lib as L
 from ._lib import HHParams, KernelTimes, LeapfrogParams, NetSpec, ParacrineRefParams, SimConfig, SolveStats
 
 __all__ = ["NNError", "Context", "DeviceArray", "HHEphys", "AtomicCoupling", "AdjacencyList",
-           "ChunkedAdjacencyList", "UniformRandomNetwork", "ParacrineModule", "Simulation", "PCG",
+           "ChunkedAdjacencyList", "UniformRandomNetwork", "ParacrineModule", "Simulation", "PCG", "MultigridPCG",
            "SimConfig", "HHParams", "NetSpec", "LeapfrogParams", "ParacrineRefParams",
            "lib", "NN_SIGNAL_COUNT", "NN_SIGNAL_OUTPUT", "FIELDS"]
 
@@ -629,6 +629,44 @@ class PCG:
     def close(self):
         if self.handle:
             lib().nn_pcg_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MultigridPCG:
+    """Flexible CG preconditioned by a geometric multigrid V-cycle on the
+    7-point operator of a PCG object (nn_mg_*).  The PCG object (and its
+    cell field) must stay alive while this one is used."""
+
+    def __init__(self, pcg: PCG, levels: int = 0):
+        self.ctx, self.pcg = pcg.ctx, pcg
+        self.handle = C.c_void_p()
+        _check(lib().nn_mg_create(pcg.handle, levels, C.byref(self.handle)), self.ctx, "nn_mg_create")
+
+    @property
+    def levels(self) -> int:
+        n = C.c_int(0)
+        _check(lib().nn_mg_levels(self.handle, C.byref(n)), self.ctx, "nn_mg_levels")
+        return n.value
+
+    def apply(self, r: DeviceArray, z: DeviceArray) -> None:
+        """z = M r (one V-cycle)."""
+        _check(lib().nn_mg_apply(self.handle, r.ptr, z.ptr), self.ctx, "nn_mg_apply")
+
+    def solve(self, b: DeviceArray, x: DeviceArray, rtol: float = 1e-6, max_iter: int = 1000) -> tuple[int, float]:
+        it, rel = C.c_int(0), C.c_double(0)
+        _check(lib().nn_mg_solve(self.handle, b.ptr, x.ptr, rtol, max_iter, C.byref(it), C.byref(rel)), self.ctx,
+               "nn_mg_solve")
+        return it.value, rel.value
+
+    def close(self):
+        if self.handle:
+            lib().nn_mg_destroy(self.handle)
             self.handle = C.c_void_p()
 
     def __del__(self):

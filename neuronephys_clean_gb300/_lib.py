@@ -161,6 +161,11 @@ _SIGS = {
     "nn_hebbian_destroy": (c_int, [c_void_p]),
     "nn_hebbian_update": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "nn_hebbian_timers": (c_int, [c_void_p, c_void_p]),
+    "nn_mg_create": (c_int, [c_void_p, c_int, P(c_void_p)]),
+    "nn_mg_destroy": (c_int, [c_void_p]),
+    "nn_mg_levels": (c_int, [c_void_p, P(c_int)]),
+    "nn_mg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "nn_mg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_learned_create": (c_int, [c_void_p, c_uint64, P(c_void_p)]),
     "nn_learned_destroy": (c_int, [c_void_p]),
     "nn_learned_add_pair": (c_int, [c_void_p, c_void_p, c_void_p]),

@@ -156,6 +156,8 @@ nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol,
 // when invd is null), the caller's cell field D (may be null)
 void nn_pcg_info(const nn_pcg* pc, nn_ctx** ctx, int* nx, int* ny, int* nz, const float** invd, float* invd_const,
                  const float** D);
+// The operator's coefficients: A = (1 + beta) I + alpha L_D.
+void nn_pcg_coefficients(const nn_pcg* pc, double* alpha, double* beta);
 
 // batched PCG (nn_bpcg.cu)
 int64_t nn_bpcg_cells(const nn_bpcg* bp);

@@ -492,6 +492,12 @@ void nn_pcg_info(const nn_pcg* pc, nn_ctx** ctx, int* nx, int* ny, int* nz, cons
     *D = pc->Dcell;
 }
 
+void nn_pcg_coefficients(const nn_pcg* pc, double* alpha, double* beta)
+{
+    *alpha = pc->alpha;
+    *beta = pc->beta;
+}
+
 extern "C" nn_status nn_pcg_set_kernel_timing(nn_pcg* pc, int enable)
 {
     if (!pc) return NN_ERR_INVALID_ARG;

@@ -4,6 +4,7 @@
     python -m neuronephys_clean_gb300.profile_cases cg128    # 3 PCG iterations, 128^3, constant D
     python -m neuronephys_clean_gb300.profile_cases cghet    # 3 PCG iterations, 128^3, lognormal D
     python -m neuronephys_clean_gb300.profile_cases conv128  # 3x3x3 convs (16->16, 48->16) + wgrad at 128^3
+    python -m neuronephys_clean_gb300.profile_cases mg256    # multigrid FCG solve to 1e-6, 256^3, lognormal D
 
 Each case holds a few GB at most and launches a handful of kernels, so that
 an ncu capture of it ends by itself; every case also runs without ncu.
@@ -66,7 +67,18 @@ def conv128(ctx):
         nn.conv3d_wgrad(ctx, a, y, dw)
 
 
-CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128}
+def mg256(ctx):
+    from neuronephys_clean_gb300 import fields
+    n = 256
+    D = ctx.to_device(fields.lognormal_diffusivity((n, n, n), 1.0, 8.0, seed=1).ravel())
+    b = ctx.to_device(fields.spike_sources((n, n, n), 20000, 2.0, seed=2))
+    pc = nn.PCG(ctx, n, n, n, 1e-3 * n * n, 1e-4, D)
+    mg = nn.MultigridPCG(pc)
+    x = ctx.to_device(np.zeros(n ** 3, np.float32))
+    mg.solve(b, x, rtol=1e-6)
+
+
+CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128, "mg256": mg256}
 
 
 def main(argv: list[str]) -> None:
