@@ -61,6 +61,7 @@ HH_BYTES_PER_NEURON_STEP = 60      # R: V,m,h,n,ge,gi,I (28 B) + ring (E,I) slot
 PCG_BYTES_PER_CELL_ITER = 40       # k_cg_iter R: r,w,s,p,x; W: r,w,s,p,x -> 10 floats per cell
 PCG_HET_BYTES_PER_CELL_ITER = 48   # k_cg_iter<HET>: + D and 1/diag reads
 PUSH_BYTES_PER_EVENT = 13          # 4 B target + 4 B weight + 1 B delay + 4 B ring read-modify-write
+PULL_CSC_BYTES_PER_SYNAPSE = 9     # full CSC sweep: 4 B source + 4 B weight + 1 B delay
 
 # DRAM bytes per unit of work from one ncu capture of the kernel
 # (dram__bytes_read.sum + dram__bytes_write.sum per launch / units per launch).
@@ -368,7 +369,13 @@ def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | Non
     wl = dict(wl, grid=0)
     sim = build_sim(nn, ctx, wl, delivery=nn.NN_DELIVERY_PULL)
     n, nnz = wl["n"], sim.nnz
-    rp = sim.get_network()[0]
+    rp, _, _, dly, _ = sim.get_network()
+    sliced, cols = sim.pull_info()
+    dmax = wl["dmax"]
+    # past the longest delay, so that the gather covers every delay slice
+    # (before step d a delay-d synapse reaches back before step 0)
+    sim.step(dmax + 1)
+    d1cum = np.concatenate([[0], np.cumsum(dly == 1)])  # delay-1 synapses before each CSR position
     hbm_peak, peak_kind = measured_peaks()
     rng = np.random.default_rng(5)
     rows = []
@@ -378,20 +385,38 @@ def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | Non
         events = int((rp[lst + 1] - rp[lst]).sum())
         dl = ctx.to_device(lst)
         res = {"fraction": frac, "spikes": cnt, "events": events}
+        # the list fires at the current step, so only its delay-1 synapses
+        # arrive in the gathered step: the weights the sliced pull reads
+        hits = int((d1cum[rp[lst + 1]] - d1cum[rp[lst]]).sum()) if sliced else 0
         for mode, name, reps in ((nn.NN_DELIVERY_PUSH, "push", 20), (nn.NN_DELIVERY_PULL, "pull", 5)):
             sim.deliver_spikes(dl, cnt, mode)
             ctx.time_begin()
             for _ in range(reps):
                 sim.deliver_spikes(dl, cnt, mode)
             ms = ctx.time_end() / reps
-            nbytes = events * PUSH_BYTES_PER_EVENT if mode == nn.NN_DELIVERY_PUSH else nnz * 9 + n * 8 + n // 8
+            if mode == nn.NN_DELIVERY_PUSH:
+                nbytes = events * PUSH_BYTES_PER_EVENT
+            elif sliced:
+                # entry words and column offsets + weights of arriving synapses
+                # + ring slot written + the D - 1 bitmap rows staged
+                nbytes = nnz * 6 + hits * 4 + n * 8 + dmax * (n // 8)
+            else:
+                nbytes = nnz * PULL_CSC_BYTES_PER_SYNAPSE + n * 8 + n // 8
             res[name] = {"ms": ms, "GBs": nbytes / (ms * 1e-3) / 1e9, "frac_of_peak": nbytes / (ms * 1e-3) / 1e9 / hbm_peak}
+            if mode == nn.NN_DELIVERY_PULL:
+                csc = nnz * PULL_CSC_BYTES_PER_SYNAPSE + n * 8 + n // 8
+                res[name]["bytes"] = nbytes
+                res[name]["GBs_csc_basis"] = csc / (ms * 1e-3) / 1e9
         rows.append(res)
     cross = next((r["fraction"] for r in rows if r["pull"]["ms"] < r["push"]["ms"]), None)
     sim.close()
     ctx.close()
     return {"metric": "spike delivery GB/s vs firing fraction", "workload": wl["workload"], "neurons": n,
-            "synapses": nnz, "peak_GBs": hbm_peak, "peak_source": peak_kind, "sweep": rows,
+            "synapses": nnz, "peak_GBs": hbm_peak, "peak_source": peak_kind,
+            "pull_kernel": (f"k_deliver_pull_sliced (shared-memory bitmap, {cols} columns per block; bytes: 6 per "
+                            "synapse + 4 per arriving synapse + 8 per neuron + the bitmap rows)")
+            if sliced else "k_deliver_pull (warp per column; bytes: the 9-byte CSC entry per synapse)",
+            "sweep": rows,
             "push_pull_crossover_fraction": cross}
 
 

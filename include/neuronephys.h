@@ -321,6 +321,11 @@ NN_API nn_status nn_sim_step(nn_sim* s, int nsteps);
  * here it serves callers with spikes from elsewhere and measurement of the
  * delivery path alone.  Asynchronous on the context stream. */
 NN_API nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int count, int mode);
+/* Pull delivery layout of a pull-mode simulation: *sliced = 1 when the
+ * shared-memory kernel over the delay-sliced CSC runs (bitmap of one step in
+ * shared memory; *cols = columns per block), 0 for the warp-per-column
+ * kernel.  No counterpart in the reference. */
+NN_API nn_status nn_sim_pull_info(nn_sim* s, int* sliced, int* cols);
 /* End-to-end call: copy the state (6*n floats: V,m,h,n,ge,gi planes) from
  * host memory, advance nsteps, copy the state back and return the number of
  * spikes emitted. */

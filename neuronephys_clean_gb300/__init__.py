@@ -512,6 +512,12 @@ class Simulation:
     def deliver_spikes(self, d_list: "DeviceArray", count: int, mode: int = NN_DELIVERY_PUSH) -> None:
         _check(lib().nn_sim_deliver_spikes(self.handle, d_list.ptr, count, mode), self.ctx, "sim_deliver_spikes")
 
+    def pull_info(self) -> tuple[bool, int]:
+        """(shared-memory sliced pull kernel in use, columns per block)."""
+        a, b = C.c_int(0), C.c_int(0)
+        _check(lib().nn_sim_pull_info(self.handle, C.byref(a), C.byref(b)), self.ctx, "sim_pull_info")
+        return bool(a.value), b.value
+
     def run_host(self, state_in: np.ndarray, nsteps: int, state_out: np.ndarray) -> int:
         sp = C.c_int64()
         _check(lib().nn_sim_run_host(self.handle, _ptr(state_in), nsteps, _ptr(state_out), C.byref(sp)), self.ctx,

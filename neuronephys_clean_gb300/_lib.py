@@ -132,6 +132,7 @@ _SIGS = {
     "nn_pcg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
     "nn_sim_deliver_spikes": (c_int, [c_void_p, c_void_p, c_int, c_int]),
+    "nn_sim_pull_info": (c_int, [c_void_p, P(c_int), P(c_int)]),
     "nn_sim_set_instances": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "nn_sim_field_cells": (c_int, [c_void_p, P(c_int64)]),
     "nn_sim_get_vox": (c_int, [c_void_p, c_void_p]),

@@ -47,6 +47,15 @@
 namespace {
 
 constexpr int MG_THREADS = 256;
+#ifndef NN_MG_VEC
+#define NN_MG_VEC 4  // cells per thread on the fine level (4 or 2) when the x side allows
+#endif
+#ifndef NN_MG_MIN_BLOCKS
+// resident blocks per SM the stencils are compiled for: 4 (64 registers) is
+// the fastest of 1, 3, 4, 5, 6 on the 256^3 solve (more spill, fewer leave
+// too few warps to cover the load latency)
+#define NN_MG_MIN_BLOCKS 4
+#endif
 constexpr int MG_MAX_LEVELS = 8;
 constexpr int MG_COARSE_CELLS = 4096;  // stop coarsening at this size
 
@@ -231,6 +240,7 @@ struct Op0 {
     }
     // field of the first smoothing sweep from zero: omega b / diag
     __device__ __forceinline__ FInvd first(const float* b, float omega) const { return FInvd{b, invd, invd_c, omega}; }
+
     // interior-face conductances (-x, +x, -y, +y, -z, +z) and the boundary
     // conductance of one cell (coarsening)
     __device__ __forceinline__ void faces(int c, int i, int j, int k, float w[6], float& wb) const
@@ -276,6 +286,7 @@ struct OpF {
         }
     }
     __device__ __forceinline__ FDiv first(const float* b, float omega) const { return FDiv{b, diag, omega}; }
+
     __device__ __forceinline__ void faces(int c, int i, int j, int k, float w[6], float& b) const
     {
         const int sy = nx, sz = nx * ny;
@@ -373,7 +384,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_smooth0(Op op, const float* b
 // Two sweeps from a zero guess in one pass: x1 = omega D^-1 b (recomputed at
 // the neighbours), y = x1 + omega D^-1 (b - A x1).
 template <int V, class Op>
-__global__ void __launch_bounds__(MG_THREADS) k_mg_pre2(Op op, const float* b, float omega, float* y,
+__global__ void __launch_bounds__(MG_THREADS, NN_MG_MIN_BLOCKS) k_mg_pre2(Op op, const float* b, float omega, float* y,
                                                         const int* flags)
 {
     if (flags && flags[F_DONE]) return;
@@ -398,7 +409,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_pre2(Op op, const float* b, f
 // y = x + omega D^-1 (b - A x).  DOTS (fine level, inside FCG): b is the
 // residual r; also (r, y) and (y, q) -> RZ and BETA = -(y, q) / PQ.
 template <int V, bool DOTS, class Op>
-__global__ void __launch_bounds__(MG_THREADS) k_mg_jacobi(Op op, const float* b, const float* x, float omega,
+__global__ void __launch_bounds__(MG_THREADS, NN_MG_MIN_BLOCKS) k_mg_jacobi(Op op, const float* b, const float* x, float omega,
                                                           float* y, const int* flags, const float* q, Red red)
 {
     if (flags && flags[F_DONE]) return;
@@ -566,7 +577,7 @@ __global__ void k_fcg_set(double* scal, int* flags, double rtol2, int max_iter)
 
 // r = b - A x; (b, b), (r, r); converged at once when (r, r) <= rtol2 (b, b)
 template <int V>
-__global__ void __launch_bounds__(MG_THREADS) k_fcg_init(Op0 op, const float* b, const float* x, float* r, Red red)
+__global__ void __launch_bounds__(MG_THREADS, NN_MG_MIN_BLOCKS) k_fcg_init(Op0 op, const float* b, const float* x, float* r, Red red)
 {
     const int gx = op.nx / V;
     float acc[2] = {0.0f, 0.0f};
@@ -619,7 +630,7 @@ __global__ void __launch_bounds__(MG_THREADS) k_fcg_first(const float* r, const 
 
 // p_new = z + beta p_old; q = A p_new; (p_new, q)
 template <int V>
-__global__ void __launch_bounds__(MG_THREADS) k_fcg_ap_dir(Op0 op, const float* z, const float* p_old, float* p_new,
+__global__ void __launch_bounds__(MG_THREADS, NN_MG_MIN_BLOCKS) k_fcg_ap_dir(Op0 op, const float* z, const float* p_old, float* p_new,
                                                            float* q, Red red)
 {
     if (red.flags[F_DONE]) return;
@@ -832,6 +843,7 @@ nn_status vcycle(nn_mg* mg, int l, const float* b, float* out, const int* flags,
 {
     if (l == 0) {
         if (mg->vec0 == 4) return vlevel<4>(mg, 0, mg->op0, b, out, flags, dots_q);
+        if (mg->vec0 == 2) return vlevel<2>(mg, 0, mg->op0, b, out, flags, dots_q);
         return vlevel<1>(mg, 0, mg->op0, b, out, flags, dots_q);
     }
     return vlevel<1>(mg, l, mg->lv[l].op(), b, out, flags, nullptr);
@@ -859,6 +871,7 @@ nn_status enqueue_iterations(nn_mg* mg, float* x)
 {
     for (int parity = 0; parity < 2; ++parity) {
         if (mg->vec0 == 4) NN_TRY(enqueue_iteration_v<4>(mg, x, parity));
+        else if (mg->vec0 == 2) NN_TRY(enqueue_iteration_v<2>(mg, x, parity));
         else NN_TRY(enqueue_iteration_v<1>(mg, x, parity));
     }
     return NN_OK;
@@ -954,7 +967,7 @@ extern "C" nn_status nn_mg_create(nn_pcg* pc, int levels, nn_mg** out)
     nn_ctx_retain(ctx);
     mg->pc = pc;
     mg->op0 = Op0{nx, ny, nz, D, invd, invd_c, (float)alpha, (float)(1.0 + beta)};
-    mg->vec0 = nx % 4 == 0 ? 4 : 1;
+    mg->vec0 = nx % NN_MG_VEC == 0 ? NN_MG_VEC : (nx % 2 == 0 ? 2 : 1);
     mg->lv.resize(nl);
     nn_status st = NN_OK;
     float mass = (float)(1.0 + beta);
@@ -1038,6 +1051,7 @@ extern "C" nn_status nn_mg_solve(nn_mg* mg, const float* d_b, float* d_x, double
     NN_CHECK_LAUNCH(ctx, "k_fcg_set");
     const dim3 blk = shape_for(ctx, L.nx / mg->vec0, L.ny * L.nz).block;
     if (mg->vec0 == 4) k_fcg_init<4><<<mg->nblocks, blk, 0, cs>>>(mg->op0, d_b, d_x, mg->r, red);
+    else if (mg->vec0 == 2) k_fcg_init<2><<<mg->nblocks, blk, 0, cs>>>(mg->op0, d_b, d_x, mg->r, red);
     else k_fcg_init<1><<<mg->nblocks, blk, 0, cs>>>(mg->op0, d_b, d_x, mg->r, red);
     NN_CHECK_LAUNCH(ctx, "k_fcg_init");
     NN_TRY(vcycle(mg, 0, mg->r, mg->z, mg->flags, nullptr));

@@ -16,6 +16,7 @@
 // Periods of steps are captured once into a CUDA graph and replayed.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -53,6 +54,14 @@ struct nn_sim {
     uint32_t* csc_src = nullptr;   // source | inhibitory << 31
     float* csc_w = nullptr;
     uint8_t* csc_d = nullptr;
+    // delay-sliced CSC (pull delivery through shared memory; null when the
+    // network does not qualify): entries ordered by (delay, column, CSC order),
+    // dsl_cp[(d - 1) * n + k] = first entry of column k with delay d
+    int32_t* dsl_cp = nullptr;
+    uint32_t* dsl_src = nullptr;
+    float* dsl_w = nullptr;
+    uint16_t* dsl_col = nullptr;   // column of each entry, relative to its block's first column
+    int dsl_cols = 0;              // columns per block of the sliced pull kernel
     // paracrine
     int grid = 0;
     int64_t G = 0;
@@ -325,6 +334,11 @@ struct PullArgs {
     const unsigned long long* base;
     int q;
     int n, n_pad, D, words;
+    const int32_t* dsl_cp;
+    const uint32_t* dsl_src;
+    const float* dsl_w;
+    const uint16_t* dsl_col;
+    int dsl_cols;
 };
 
 // Pull: a warp per postsynaptic neuron sums its CSC column against the spike
@@ -379,6 +393,159 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
         acc_e = nn_warp_sumf(acc_e);
         acc_i = nn_warp_sumf(acc_i);
         if (lane == 0) reinterpret_cast<float2*>(out)[k] = make_float2(acc_e, acc_i);
+    }
+}
+
+// Pull through shared memory.  A block owns dsl_cols consecutive columns
+// (postsynaptic neurons).  For each delay d = 1 .. D-1 it copies the spike
+// bitmap of step t + 1 - d (n_pad bits) into shared memory; its entries of
+// that delay are one contiguous range of the slice, which the block's threads
+// walk flat, four entries per 16-byte load (plus their 2-byte column
+// offsets), testing each source bit in shared memory and reading a weight only
+// where it is set.  Sums accumulate in shared memory as 64-bit fixed point
+// (weight x 2^32; integer addition does not depend on order, so the result is
+// deterministic, and exact for weights >= 2^-8).  While the block works on
+// delay d, one thread asks the bulk-copy engine to prefetch the range of
+// delay d + 1 into L2.  DRAM traffic per step: 6 B per synapse (entry word
+// and column offset), the weights of the sources that fired, the ring slot
+// written (8 B per neuron).
+constexpr int DSL_THREADS = 1024;
+constexpr int DSL_GROUPS = 3;  // groups of four entries a thread loads before testing them (2-6 measured alike)
+constexpr int DSL_MAX_DELAY = 64;
+constexpr int DSL_PAD = 8;  // slack entries after the slice arrays (16-byte load / prefetch rounding)
+constexpr double DSL_FIX = 4294967296.0;  // 2^32
+
+// L2 prefetch of [p, p + bytes) rounded out to 16 bytes, in pieces of at most
+// 64 KB (cp.async.bulk.prefetch.L2: 16-byte aligned address and size)
+__device__ __forceinline__ void dsl_prefetch(const void* p, size_t bytes)
+{
+    uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)15;
+    const uintptr_t e = (reinterpret_cast<uintptr_t>(p) + bytes + 15) & ~(uintptr_t)15;
+    while (a < e) {
+        const uint32_t n = (uint32_t)((e - a) < (uintptr_t)65536 ? (e - a) : (uintptr_t)65536);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
+        a += n;
+    }
+}
+
+__device__ __forceinline__ void dsl_take(const uint32_t* bm, uint32_t sw, int e, int e0, int e1, uint32_t col,
+                                         const float* w, unsigned long long* acc_e, unsigned long long* acc_i)
+{
+    if (e < e0 || e >= e1) return;
+    const uint32_t sid = sw & 0x7fffffffu;
+    if (!((bm[sid >> 5] >> (sid & 31)) & 1u)) return;
+    const unsigned long long v = (unsigned long long)llrintf(w[e] * (float)DSL_FIX);
+    atomicAdd((sw >> 31) ? acc_i + col : acc_e + col, v);
+}
+
+__global__ void __launch_bounds__(DSL_THREADS, 1) k_deliver_pull_sliced(PullArgs a)
+{
+    extern __shared__ uint4 dsl_smem[];
+    const uint32_t* bm = reinterpret_cast<const uint32_t*>(dsl_smem);
+    unsigned long long* acc_e = reinterpret_cast<unsigned long long*>(dsl_smem + a.words / 4);
+    unsigned long long* acc_i = acc_e + a.dsl_cols;
+    const uint64_t t1 = *a.base + (uint64_t)a.q + 1;
+    const int s1 = (int)(t1 % (uint64_t)a.D);
+    const int k0 = blockIdx.x * a.dsl_cols;
+    const int k1 = min(a.n, k0 + a.dsl_cols);
+    const int dlast = t1 < (uint64_t)(a.D - 1) ? (int)t1 : a.D - 1;  // delays beyond t + 1 reach before step 0
+    for (int k = threadIdx.x; k < a.dsl_cols; k += blockDim.x) acc_e[k] = acc_i[k] = 0ull;
+    const int w4 = a.words / 4;
+    if (threadIdx.x == 0 && dlast >= 1)
+        dsl_prefetch(a.dsl_src + a.dsl_cp[k0], sizeof(uint32_t) * (size_t)(a.dsl_cp[k1] - a.dsl_cp[k0]));
+    for (int d = 1; d <= dlast; ++d) {
+        int hs = s1 - d;
+        if (hs < 0) hs += a.D;
+        const uint4* src4 = reinterpret_cast<const uint4*>(a.bitmap + (size_t)hs * a.words);
+        __syncthreads();  // the previous delay's lookups are done
+        for (int w = threadIdx.x; w < w4; w += blockDim.x) dsl_smem[w] = src4[w];
+        if (threadIdx.x == 0 && d < dlast) {
+            const int32_t* cpn = a.dsl_cp + (size_t)d * a.n;
+            dsl_prefetch(a.dsl_src + cpn[k0], sizeof(uint32_t) * (size_t)(cpn[k1] - cpn[k0]));
+            dsl_prefetch(a.dsl_col + cpn[k0], sizeof(uint16_t) * (size_t)(cpn[k1] - cpn[k0]));
+        }
+        __syncthreads();
+        const int32_t* cp = a.dsl_cp + (size_t)(d - 1) * a.n;
+        const int e0 = cp[k0], e1 = cp[k1];
+        const int stride = 4 * blockDim.x;
+        // DSL_GROUPS groups of four entries per thread in flight
+        for (int e = (e0 & ~3) + 4 * threadIdx.x; e < e1; e += DSL_GROUPS * stride) {
+            uint4 sv[DSL_GROUPS];
+            uint2 cv[DSL_GROUPS];
+#pragma unroll
+            for (int g = 0; g < DSL_GROUPS; ++g) {
+                const int f = e + g * stride;
+                if (f < e1) {
+                    sv[g] = *reinterpret_cast<const uint4*>(a.dsl_src + f);
+                    cv[g] = *reinterpret_cast<const uint2*>(a.dsl_col + f);
+                }
+            }
+#pragma unroll
+            for (int g = 0; g < DSL_GROUPS; ++g) {
+                const int f = e + g * stride;
+                if (f >= e1) break;
+                dsl_take(bm, sv[g].x, f, e0, e1, cv[g].x & 0xffffu, a.dsl_w, acc_e, acc_i);
+                dsl_take(bm, sv[g].y, f + 1, e0, e1, cv[g].x >> 16, a.dsl_w, acc_e, acc_i);
+                dsl_take(bm, sv[g].z, f + 2, e0, e1, cv[g].y & 0xffffu, a.dsl_w, acc_e, acc_i);
+                dsl_take(bm, sv[g].w, f + 3, e0, e1, cv[g].y >> 16, a.dsl_w, acc_e, acc_i);
+            }
+        }
+    }
+    __syncthreads();
+    float2* out = reinterpret_cast<float2*>(a.ring + (size_t)(t1 % (uint64_t)a.D) * a.n_pad * 2);
+    for (int k = threadIdx.x; k < k1 - k0; k += blockDim.x)
+        out[k0 + k] = make_float2((float)((double)(long long)acc_e[k] / DSL_FIX),
+                                  (float)((double)(long long)acc_i[k] / DSL_FIX));
+}
+
+// Bounds for the fixed-point sums: the longest column and the largest |weight|.
+__global__ void k_dsl_bounds(const int64_t* col_ptr, const float* csc_w, int n, unsigned int* out)
+{
+    unsigned int len = 0, wmax = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        len = max(len, (unsigned int)(col_ptr[k + 1] - col_ptr[k]));
+        for (int64_t e = col_ptr[k]; e < col_ptr[k + 1]; ++e) wmax = max(wmax, __float_as_uint(fabsf(csc_w[e])));
+    }
+    atomicMax(out, len);
+    atomicMax(out + 1, wmax);  // non-negative floats order like their bit patterns
+}
+
+// Delay-sliced layout: per column, entries counted per delay (a thread owns
+// a column, so no atomics) ...
+// (delays outside [1, dmax] cannot occur -- the network setters check them --
+// and would be left out of both passes alike)
+__global__ void k_dsl_count(const int64_t* col_ptr, const uint8_t* csc_d, int n, int dmax, int64_t* cnt)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        for (int64_t e = col_ptr[k]; e < col_ptr[k + 1]; ++e) {
+            const int d = csc_d[e];
+            if (d >= 1 && d <= dmax) cnt[(size_t)(d - 1) * n + k] += 1;
+        }
+}
+
+// ... offsets narrowed to 32 bits ...
+__global__ void k_dsl_narrow(const int64_t* off, int64_t count, int32_t* out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (int32_t)off[i];
+}
+
+// ... and each column's entries placed in CSC order within every delay slice.
+__global__ void k_dsl_fill(const int64_t* col_ptr, const uint32_t* csc_src, const float* csc_w, const uint8_t* csc_d,
+                           int n, int dmax, int cols, const int32_t* cp, uint32_t* out_src, float* out_w,
+                           uint16_t* out_col)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int pos[DSL_MAX_DELAY];
+        for (int d = 0; d < dmax; ++d) pos[d] = cp[(size_t)d * n + k];
+        for (int64_t e = col_ptr[k]; e < col_ptr[k + 1]; ++e) {
+            const int d = csc_d[e];
+            if (d < 1 || d > dmax) continue;
+            const int q = pos[d - 1]++;
+            out_src[q] = csc_src[e];
+            out_w[q] = csc_w[e];
+            out_col[q] = (uint16_t)(k % cols);
+        }
     }
 }
 
@@ -829,7 +996,26 @@ static PullArgs pull_args(nn_sim* s, int q)
     a.base = s->step;
     a.q = q;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
+    a.dsl_cp = s->dsl_cp; a.dsl_src = s->dsl_src; a.dsl_w = s->dsl_w; a.dsl_col = s->dsl_col;
+    a.dsl_cols = s->dsl_cols;
     return a;
+}
+
+// The pull gather of one step: through shared memory when the delay-sliced
+// layout exists, else the warp-per-column kernel.
+static nn_status launch_pull(nn_sim* s, const PullArgs& d, cudaStream_t cs)
+{
+    nn_ctx* ctx = s->ctx;
+    if (s->dsl_cp) {
+        const int blocks = (s->n + s->dsl_cols - 1) / s->dsl_cols;
+        const size_t smem = sizeof(uint32_t) * (size_t)s->words + 2 * sizeof(unsigned long long) * (size_t)s->dsl_cols;
+        k_deliver_pull_sliced<<<blocks, DSL_THREADS, smem, cs>>>(d);
+        NN_CHECK_LAUNCH(ctx, "k_deliver_pull_sliced");
+        return NN_OK;
+    }
+    k_deliver_pull<<<nn_grid_for(ctx, (int64_t)s->n * 32, DELIV_THREADS, 8), DELIV_THREADS, 0, cs>>>(d);
+    NN_CHECK_LAUNCH(ctx, "k_deliver_pull");
+    return NN_OK;
 }
 
 static void drop_graph(nn_sim* s)
@@ -926,6 +1112,7 @@ static void free_network(nn_sim* s)
 {
     nn_release(s->row_ptr); nn_release(s->col); nn_release(s->weight); nn_release(s->delay);
     nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
+    nn_release(s->dsl_cp); nn_release(s->dsl_src); nn_release(s->dsl_w); nn_release(s->dsl_col);
     s->nnz = 0;
 }
 
@@ -955,6 +1142,83 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     return NN_OK;
 }
 
+// Delay-sliced copy of the CSC for the shared-memory pull kernel, built when
+// one bitmap row and two 64-bit accumulators per column of a block fit in a
+// block's shared memory, delays stay within DSL_MAX_DELAY, entry offsets
+// within 32 bits and the fixed-point sums below 2^31 (longest column x
+// largest |weight|).  NN_PULL_UNSLICED=1 keeps the warp-per-column kernel
+// (for comparisons).
+static nn_status build_sliced(nn_sim* s)
+{
+    nn_ctx* ctx = s->ctx;
+    const char* env = std::getenv("NN_PULL_UNSLICED");
+    if (env && env[0] == '1') return NN_OK;
+    int smem_max = 0;
+    NN_CUDA(ctx, cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    const int cols = (s->n + ctx->num_sms - 1) / ctx->num_sms;
+    // bitmap row + two 64-bit accumulators per column
+    const size_t smem = sizeof(uint32_t) * (size_t)s->words + 2 * sizeof(unsigned long long) * (size_t)cols;
+    const int dmax = s->D - 1;
+    if (s->nnz <= 0 || smem > (size_t)smem_max || cols > 65536 || dmax > DSL_MAX_DELAY ||
+        s->nnz >= INT32_MAX - DSL_PAD || (s->words % 4))
+        return NN_OK;
+    // fixed-point range: |sum| <= longest column x largest |weight| < 2^31
+    unsigned int* bnd = nullptr;
+    NN_TRY(nn_alloc(ctx, &bnd, 2));
+    NN_CUDA(ctx, nn_zero_async(ctx, bnd, 2 * sizeof(unsigned int)));
+    k_dsl_bounds<<<nn_grid_for(ctx, s->n, 256, 8), 256, 0, ctx->stream>>>(s->col_ptr, s->csc_w, s->n, bnd);
+    NN_CHECK_LAUNCH(ctx, "k_dsl_bounds");
+    unsigned int hb[2] = {0, 0};
+    const cudaError_t ce = nn_copy_sync(ctx, hb, bnd, sizeof hb, cudaMemcpyDeviceToHost);
+    cudaFree(bnd);
+    NN_CUDA(ctx, ce);
+    float wmax;
+    std::memcpy(&wmax, &hb[1], sizeof wmax);
+    if (!(std::isfinite(wmax)) || (double)hb[0] * (double)wmax >= 2147483648.0) return NN_OK;
+    const size_t slots = (size_t)dmax * s->n + 1;
+    int64_t *cnt = nullptr, *off = nullptr;
+    nn_status st = nn_alloc(ctx, &cnt, slots);
+    if (st == NN_OK) st = nn_alloc(ctx, &off, slots);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_cp, slots + DSL_PAD);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_src, (size_t)s->nnz + DSL_PAD);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_col, (size_t)s->nnz + DSL_PAD);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_w, (size_t)s->nnz);
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, cnt, sizeof(int64_t) * slots), "build_sliced");
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, nn_zero_async(ctx, s->dsl_src + s->nnz, sizeof(uint32_t) * DSL_PAD), "build_sliced");
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, nn_zero_async(ctx, s->dsl_col + s->nnz, sizeof(uint16_t) * DSL_PAD), "build_sliced");
+    if (st == NN_OK) {
+        k_dsl_count<<<nn_grid_for(ctx, s->n, 256, 8), 256, 0, ctx->stream>>>(s->col_ptr, s->csc_d, s->n, dmax, cnt);
+        st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_count");
+    }
+    if (st == NN_OK) st = nn_scan_exclusive_i64(ctx, cnt, off, (int64_t)slots);
+    if (st == NN_OK) {
+        k_dsl_narrow<<<nn_grid_for(ctx, (int64_t)slots, 256, 8), 256, 0, ctx->stream>>>(off, (int64_t)slots,
+                                                                                          s->dsl_cp);
+        st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_narrow");
+    }
+    if (st == NN_OK) {
+        k_dsl_fill<<<nn_grid_for(ctx, s->n, 128, 8), 128, 0, ctx->stream>>>(
+            s->col_ptr, s->csc_src, s->csc_w, s->csc_d, s->n, dmax, cols, s->dsl_cp, s->dsl_src, s->dsl_w,
+            s->dsl_col);
+        st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_fill");
+    }
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, cudaFuncSetAttribute(k_deliver_pull_sliced,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                           "cudaFuncSetAttribute");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "build_sliced");
+    cudaFree(cnt);
+    cudaFree(off);
+    if (st != NN_OK) {
+        nn_release(s->dsl_cp); nn_release(s->dsl_src); nn_release(s->dsl_w); nn_release(s->dsl_col);
+        return st;
+    }
+    s->dsl_cols = cols;
+    return NN_OK;
+}
+
 static nn_status build_csc(nn_sim* s)
 {
     nn_ctx* ctx = s->ctx;
@@ -979,13 +1243,14 @@ static nn_status build_csc(nn_sim* s)
     }
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     cudaFree(edge_of);
-    return NN_OK;
+    return build_sliced(s);
 }
 
 static nn_status after_network(nn_sim* s)
 {
     drop_graph(s);
     nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
+    nn_release(s->dsl_cp); nn_release(s->dsl_src); nn_release(s->dsl_w); nn_release(s->dsl_col);
     if (s->cfg.delivery == NN_DELIVERY_PULL) NN_TRY(build_csc(s));
     return NN_OK;
 }
@@ -1448,9 +1713,7 @@ static nn_status enqueue_step(nn_sim* s, int qk, int qe)
     NN_CHECK_LAUNCH(ctx, "k_hh_step");
     if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_b[qe], cs, cudaEventRecordExternal));
     if (s->cfg.delivery == NN_DELIVERY_PULL) {
-        PullArgs d = pull_args(s, qk);
-        k_deliver_pull<<<nn_grid_for(ctx, (int64_t)s->n * 32, DELIV_THREADS, 8), DELIV_THREADS, 0, cs>>>(d);
-        NN_CHECK_LAUNCH(ctx, "k_deliver_pull");
+        NN_TRY(launch_pull(s, pull_args(s, qk), cs));
     }
     if (tm) {
         NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_c[qe], cs, cudaEventRecordExternal));
@@ -1738,6 +2001,14 @@ extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
     return NN_OK;
 }
 
+extern "C" nn_status nn_sim_pull_info(nn_sim* s, int* sliced, int* cols)
+{
+    if (!s || !sliced || !cols) return NN_ERR_INVALID_ARG;
+    *sliced = s->dsl_cp ? 1 : 0;
+    *cols = s->dsl_cp ? s->dsl_cols : 0;
+    return NN_OK;
+}
+
 extern "C" nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int count, int mode)
 {
     if (!s || (count > 0 && !d_list) || count < 0 || count > s->n) return NN_ERR_INVALID_ARG;
@@ -1761,10 +2032,7 @@ extern "C" nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int cou
                                                                        s->words);
         NN_CHECK_LAUNCH(ctx, "k_list_bitmap");
     }
-    PullArgs d = pull_args(s, 0);
-    k_deliver_pull<<<nn_grid_for(ctx, (int64_t)s->n * 32, DELIV_THREADS, 8), DELIV_THREADS, 0, cs>>>(d);
-    NN_CHECK_LAUNCH(ctx, "k_deliver_pull");
-    return NN_OK;
+    return launch_pull(s, pull_args(s, 0), cs);
 }
 
 extern "C" nn_status nn_sim_run_host(nn_sim* s, const float* h_in, int nsteps, float* h_out, int64_t* h_spikes)

@@ -5,6 +5,7 @@
     python -m neuronephys_clean_gb300.profile_cases cghet    # 3 PCG iterations, 128^3, lognormal D
     python -m neuronephys_clean_gb300.profile_cases conv128  # 3x3x3 convs (16->16, 48->16) + wgrad at 128^3
     python -m neuronephys_clean_gb300.profile_cases mg256    # multigrid FCG solve to 1e-6, 256^3, lognormal D
+    python -m neuronephys_clean_gb300.profile_cases pull1m   # one pull gather, 1M neurons, 1e8 synapses, delays 1..20
 
 Each case holds a few GB at most and launches a handful of kernels, so that
 an ncu capture of it ends by itself; every case also runs without ncu.
@@ -78,7 +79,21 @@ def mg256(ctx):
     mg.solve(b, x, rtol=1e-6)
 
 
-CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128, "mg256": mg256}
+def pull1m(ctx):
+    n = 1_000_000
+    c = nn.default_config(n)
+    c.seed, c.max_delay, c.delivery = 1, 20, nn.NN_DELIVERY_PULL
+    s = nn.Simulation(ctx, c)
+    sp = nn.default_net_spec(nn.NN_NET_GAUSS)
+    sp.k, sp.sigma, sp.w_mu, sp.w_sigma, sp.dmax = 100, 0.1, -1.0, 1.0, 20
+    s.generate_network(sp)
+    s.init_state(-65.0, 0.0, 0.0)
+    s.step(21)  # past the longest delay: the gather covers every delay slice
+    lst = np.sort(np.random.default_rng(5).choice(n, 1000, replace=False)).astype(np.int32)
+    s.deliver_spikes(ctx.to_device(lst), len(lst), nn.NN_DELIVERY_PULL)
+
+
+CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128, "mg256": mg256, "pull1m": pull1m}
 
 
 def main(argv: list[str]) -> None:

@@ -104,6 +104,36 @@ def test_push_pull_agree_and_pull_is_deterministic(ctx):
     assert np.array_equal(gpu_state(b), gpu_state(c))
 
 
+def test_sliced_pull_matches_warp_pull(ctx, monkeypatch):
+    """Pull delivery through the shared-memory bitmap (delay-sliced CSC) and
+    through the warp-per-column kernel (NN_PULL_UNSLICED=1): same rasters,
+    states within the last-bits spread of two summation orders; each is
+    deterministic.  Gaussian network with delays 1..20, membrane potentials
+    spread over [-65, -35] mV so that spikes start at once."""
+    def run(unsliced):
+        if unsliced:
+            monkeypatch.setenv("NN_PULL_UNSLICED", "1")
+        else:
+            monkeypatch.delenv("NN_PULL_UNSLICED", raising=False)
+        c = nn.default_config(4096)
+        c.seed, c.max_delay, c.raster_capacity, c.delivery = 9, 20, 100000, 1
+        s = nn.Simulation(ctx, c)
+        spec = nn.default_net_spec(nn.NN_NET_GAUSS)
+        spec.k, spec.dmax, spec.w_mu = 40, 20, 0.0
+        s.generate_network(spec)
+        assert s.pull_info()[0] == (not unsliced)
+        s.init_state(-65.0, 6.0, 12.0)
+        s.set_field("V", np.random.default_rng(3).uniform(-65, -35, 4096).astype(np.float32))
+        s.step(400)
+        return raster_set(*s.raster()), gpu_state(s), np.stack([s.get_field("GE"), s.get_field("GI")])
+    a, b, u = run(False), run(False), run(True)
+    assert len(a[0]) > 100
+    assert a[0] == b[0] and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert a[0] == u[0]
+    np.testing.assert_allclose(a[1], u[1], rtol=1e-3, atol=1e-3)
+    np.testing.assert_allclose(a[2], u[2], rtol=1e-4, atol=1e-5)
+
+
 def test_delays_parity(ctx, orc):
     """Gaussian network with delays U{1..20}: raster and state vs the oracle."""
     n, seed = 2744, 31
