@@ -20,7 +20,8 @@ LIB = PKG / "lib" / "libneuronephys.so"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 
-SOURCES = ["nn_api.cu", "nn_ref.cu", "nn_pcg.cu", "nn_cg.cu", "nn_sim.cu", "nn_conv.cu", "nn_unet.cu", "nn_probe.cu", "nn_io.cu", "nn_bpcg.cu", "nn_cortex.cu", "nn_mg.cu"]
+SOURCES = ["nn_api.cu", "nn_ref.cu", "nn_pcg.cu", "nn_cg.cu", "nn_sim.cu", "nn_conv.cu", "nn_unet.cu", "nn_probe.cu", "nn_io.cu", "nn_bpcg.cu", "nn_cortex.cu", "nn_mg.cu",
+           "nn_step.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
           "-I", str(INCLUDE), "-I", str(CSRC)]

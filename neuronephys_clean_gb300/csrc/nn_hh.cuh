@@ -33,80 +33,198 @@ inline nn_hh_dev nn_hh_to_dev(const nn_hh_params& p)
     return d;
 }
 
-__device__ __forceinline__ float nn_xexprel(float u, float emu)
-{
-    const float u2 = u * u;
-    const float series = 1.0f + u * 0.5f + u2 * (1.0f / 12.0f + u2 * (-1.0f / 720.0f + u2 * (1.0f / 30240.0f)));
-    const float direct = __fdividef(u, 1.0f - emu);
-    return fabsf(u) < 0.5f ? series : direct;
-}
+// ---- lane vectors ----
+// W neurons computed together.  With W = 2 every add, subtract, multiply and
+// fused multiply-add is one packed two-lane FP32 instruction (PTX .f32x2,
+// sm_100 family); with W = 1 the same operations run one lane at a time.
+// Each operation is explicitly rounded and the packed instructions round each
+// lane as the scalar ones do.  The assembler may still fuse a packed multiply
+// whose result feeds a packed add into one fused multiply-add, depending on
+// the surrounding code; so no product below feeds a sum directly (sums of
+// products are written as explicit fused multiply-adds, and constant factors
+// are folded into the coefficients that use them).  The two forms then give
+// bit-identical results.  Exponentials and reciprocals stay per lane.
+template <int W>
+struct nn_vf {
+    float v[W];
+};
 
-struct nn_rates { float am, bm, ah, bh, an, bn; };
-
-__device__ __forceinline__ nn_rates nn_hh_rates(float V)
+template <int W>
+__device__ __forceinline__ nn_vf<W> vb(float x)  // broadcast
 {
-    nn_rates r;
-    const float um = (V + 40.0f) * 0.1f;
-    const float un = (V + 55.0f) * 0.1f;  // = um + 1.5
-    const float em = __expf(-um);
-    r.am = nn_xexprel(um, em);
-    r.an = 0.1f * nn_xexprel(un, em * 0.22313016014842982f);  // e^{-un} = e^{-um} e^{-1.5}
-    const float q = __expf((V + 65.0f) * (-1.0f / 80.0f));  // e^{-(V+65)/80}
-    r.bn = 0.125f * q;
-    const float q2 = q * q;
-    const float q4 = q2 * q2;                                 // e^{-(V+65)/20}
-    r.ah = 0.07f * q4;
-    const float q8 = q4 * q4;                                 // e^{-(V+65)/10}
-    r.bh = __fdividef(1.0f, 1.0f + 20.085536923187668f * q8); // 1/(1+e^{-(V+35)/10})
-    r.bm = 4.0f * __expf((V + 65.0f) * (-1.0f / 18.0f));
+    nn_vf<W> r;
+#pragma unroll
+    for (int l = 0; l < W; ++l) r.v[l] = x;
     return r;
 }
 
-struct nn_hh_state { float V, m, h, n, ge, gi; };
+#define NN_F32X2(op, ins)                                                                                  \
+    __device__ __forceinline__ nn_vf<2> op(const nn_vf<2>& a, const nn_vf<2>& b)                          \
+    {                                                                                                      \
+        nn_vf<2> d;                                                                                        \
+        asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t" ins         \
+            " rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"                                                   \
+            : "=f"(d.v[0]), "=f"(d.v[1])                                                                   \
+            : "f"(a.v[0]), "f"(a.v[1]), "f"(b.v[0]), "f"(b.v[1]));                                          \
+        return d;                                                                                          \
+    }
+NN_F32X2(vadd, "add.rn.f32x2")
+NN_F32X2(vsub, "sub.rn.f32x2")
+NN_F32X2(vmul, "mul.rn.f32x2")
+#undef NN_F32X2
 
-__device__ __forceinline__ nn_hh_state nn_hh_rhs(const nn_hh_dev& p, float gna, float iext, float gpu,
-                                                 const nn_hh_state& y)
+__device__ __forceinline__ nn_vf<2> vfma(const nn_vf<2>& a, const nn_vf<2>& b, const nn_vf<2>& c)  // a*b + c
 {
-    const nn_rates r = nn_hh_rates(y.V);
-    const float m3h = y.m * y.m * y.m * y.h;
-    const float n2 = y.n * y.n;
-    const float n4 = n2 * n2;
-    float cur = iext;
-    cur -= gna * m3h * (y.V - p.ENa);
-    cur -= p.gK * n4 * (y.V - p.EK);
-    cur -= p.gL * (y.V - p.EL);
-    cur -= y.ge * (y.V - p.Ee);
-    cur -= y.gi * (y.V - p.Ei);
-    cur -= gpu * (y.V - p.E_par);
-    nn_hh_state f;
-    f.V = cur * p.C_inv;
-    f.m = r.am - (r.am + r.bm) * y.m;
-    f.h = r.ah - (r.ah + r.bh) * y.h;
-    f.n = r.an - (r.an + r.bn) * y.n;
-    f.ge = -y.ge * p.inv_tau_e;
-    f.gi = -y.gi * p.inv_tau_i;
+    nn_vf<2> d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.v[0]), "=f"(d.v[1])
+        : "f"(a.v[0]), "f"(a.v[1]), "f"(b.v[0]), "f"(b.v[1]), "f"(c.v[0]), "f"(c.v[1]));
+    return d;
+}
+
+__device__ __forceinline__ nn_vf<1> vadd(const nn_vf<1>& a, const nn_vf<1>& b) { return {{__fadd_rn(a.v[0], b.v[0])}}; }
+__device__ __forceinline__ nn_vf<1> vsub(const nn_vf<1>& a, const nn_vf<1>& b) { return {{__fsub_rn(a.v[0], b.v[0])}}; }
+__device__ __forceinline__ nn_vf<1> vmul(const nn_vf<1>& a, const nn_vf<1>& b) { return {{__fmul_rn(a.v[0], b.v[0])}}; }
+__device__ __forceinline__ nn_vf<1> vfma(const nn_vf<1>& a, const nn_vf<1>& b, const nn_vf<1>& c)
+{
+    return {{__fmaf_rn(a.v[0], b.v[0], c.v[0])}};
+}
+
+// u / (1 - e^{-u}) given den = 1 - e^{-u}: series for |u| < 0.5, direct elsewhere
+template <int W>
+__device__ __forceinline__ nn_vf<W> nn_xexprel(const nn_vf<W>& u, const nn_vf<W>& den)
+{
+    const nn_vf<W> u2 = vmul(u, u);
+    // series = 1 + u/2 + u^2/12 - u^4/720 + u^6/30240
+    //        = 1 + u (1/2 + u (1/12 + u^2 (-1/720 + u^2 / 30240)))
+    nn_vf<W> t = vfma(u2, vfma(u2, vb<W>(1.0f / 30240.0f), vb<W>(-1.0f / 720.0f)), vb<W>(1.0f / 12.0f));
+    t = vfma(u, t, vb<W>(0.5f));
+    const nn_vf<W> series = vfma(u, t, vb<W>(1.0f));
+    nn_vf<W> r;
+#pragma unroll
+    for (int l = 0; l < W; ++l) r.v[l] = fabsf(u.v[l]) < 0.5f ? series.v[l] : __fdividef(u.v[l], den.v[l]);
+    return r;
+}
+
+// Opening rates a_x and the totals s_x = a_x + b_x.
+template <int W>
+struct nn_rates {
+    nn_vf<W> am, sm, ah, sh, an, sn;
+};
+
+template <int W>
+__device__ __forceinline__ nn_rates<W> nn_hh_rates(const nn_vf<W>& V)
+{
+    nn_rates<W> r;
+    const nn_vf<W> um = vmul(vadd(V, vb<W>(40.0f)), vb<W>(0.1f));
+    const nn_vf<W> un = vmul(vadd(V, vb<W>(55.0f)), vb<W>(0.1f));
+    const nn_vf<W> v65 = vadd(V, vb<W>(65.0f));
+    const nn_vf<W> aq = vmul(v65, vb<W>(-1.0f / 80.0f));
+    const nn_vf<W> ab = vmul(v65, vb<W>(-1.0f / 18.0f));
+    nn_vf<W> em, q, eb;
+#pragma unroll
+    for (int l = 0; l < W; ++l) {
+        em.v[l] = __expf(-um.v[l]);
+        q.v[l] = __expf(aq.v[l]);   // e^{-(V+65)/80}
+        eb.v[l] = __expf(ab.v[l]);  // e^{-(V+65)/18}
+    }
+    r.am = nn_xexprel(um, vsub(vb<W>(1.0f), em));
+    const nn_vf<W> xn = nn_xexprel(un, vfma(vb<W>(-0.22313016014842982f), em, vb<W>(1.0f)));  // e^{-un} = e^{-um} e^{-1.5}
+    r.an = vmul(vb<W>(0.1f), xn);
+    r.sn = vfma(vb<W>(0.125f), q, r.an);                // + b_n = 0.125 e^{-(V+65)/80}
+    const nn_vf<W> q2 = vmul(q, q);
+    const nn_vf<W> q4 = vmul(q2, q2);                   // e^{-(V+65)/20}
+    r.ah = vmul(vb<W>(0.07f), q4);
+    const nn_vf<W> q8 = vmul(q4, q4);                   // e^{-(V+65)/10}
+    const nn_vf<W> den = vfma(vb<W>(20.085536923187668f), q8, vb<W>(1.0f));  // 1 + e^{-(V+35)/10}
+    nn_vf<W> bh;
+#pragma unroll
+    for (int l = 0; l < W; ++l) bh.v[l] = __fdividef(1.0f, den.v[l]);
+    r.sh = vfma(vb<W>(0.07f), q4, bh);
+    r.sm = vfma(vb<W>(4.0f), eb, r.am);                 // + b_m = 4 e^{-(V+65)/18}
+    return r;
+}
+
+template <int W>
+struct nn_hh_state {
+    nn_vf<W> V, m, h, n, ge, gi;
+};
+
+// Right-hand side with two factors left out: the V component is the total
+// current (dV/dt = current / C) and the g_e, g_i components are the
+// conductances themselves (dg/dt = -g / tau); the RK4 coefficients below
+// carry 1/C and -1/tau.  ngna = -gNa * (per-neuron scale), ngpu = -g_par *
+// density (negated once per step, so every current term is one fused
+// multiply-add).
+template <int W>
+__device__ __forceinline__ nn_hh_state<W> nn_hh_rhs(const nn_hh_dev& p, const nn_vf<W>& ngna, const nn_vf<W>& iext,
+                                                    const nn_vf<W>& ngpu, const nn_hh_state<W>& y)
+{
+    const nn_rates<W> r = nn_hh_rates(y.V);
+    const nn_vf<W> m3h = vmul(vmul(vmul(y.m, y.m), y.m), y.h);
+    const nn_vf<W> n2 = vmul(y.n, y.n);
+    const nn_vf<W> n4 = vmul(n2, n2);
+    nn_vf<W> cur = vfma(vmul(ngna, m3h), vsub(y.V, vb<W>(p.ENa)), iext);
+    cur = vfma(vmul(vb<W>(-p.gK), n4), vsub(y.V, vb<W>(p.EK)), cur);
+    cur = vfma(vb<W>(-p.gL), vsub(y.V, vb<W>(p.EL)), cur);
+    cur = vfma(vmul(vb<W>(-1.0f), y.ge), vsub(y.V, vb<W>(p.Ee)), cur);
+    cur = vfma(vmul(vb<W>(-1.0f), y.gi), vsub(y.V, vb<W>(p.Ei)), cur);
+    cur = vfma(ngpu, vsub(y.V, vb<W>(p.E_par)), cur);
+    nn_hh_state<W> f;
+    f.V = cur;
+    f.m = vfma(vmul(vb<W>(-1.0f), r.sm), y.m, r.am);
+    f.h = vfma(vmul(vb<W>(-1.0f), r.sh), y.h, r.ah);
+    f.n = vfma(vmul(vb<W>(-1.0f), r.sn), y.n, r.an);
+    f.ge = y.ge;
+    f.gi = y.gi;
     return f;
 }
 
-__device__ __forceinline__ nn_hh_state nn_axpy(const nn_hh_state& y, float a, const nn_hh_state& k)
+// Per-component factors of the right-hand side (1/C for V, 1 for the gates,
+// -1/tau for the conductances) times a step length.
+struct nn_hh_coef {
+    float V, x, ge, gi;
+};
+
+__device__ __forceinline__ nn_hh_coef nn_hh_scaled(const nn_hh_dev& p, float h)
 {
-    return nn_hh_state{y.V + a * k.V, y.m + a * k.m, y.h + a * k.h, y.n + a * k.n, y.ge + a * k.ge, y.gi + a * k.gi};
+    return nn_hh_coef{h * p.C_inv, h, -h * p.inv_tau_e, -h * p.inv_tau_i};
 }
 
-// gna = gNa * (per-neuron scale); gpu = g_par * interpolated density.
-__device__ __forceinline__ void nn_hh_rk4(const nn_hh_dev& p, float gna, float iext, float gpu, nn_hh_state& y)
+template <int W>
+__device__ __forceinline__ nn_hh_state<W> nn_axpy(const nn_hh_state<W>& y, const nn_hh_coef& c, const nn_hh_state<W>& k)
 {
-    const float dt = p.dt, h2 = 0.5f * p.dt, s6 = p.dt * (1.0f / 6.0f);
-    const nn_hh_state k1 = nn_hh_rhs(p, gna, iext, gpu, y);
-    const nn_hh_state k2 = nn_hh_rhs(p, gna, iext, gpu, nn_axpy(y, h2, k1));
-    const nn_hh_state k3 = nn_hh_rhs(p, gna, iext, gpu, nn_axpy(y, h2, k2));
-    const nn_hh_state k4 = nn_hh_rhs(p, gna, iext, gpu, nn_axpy(y, dt, k3));
-    y.V += s6 * (k1.V + 2.0f * (k2.V + k3.V) + k4.V);
-    y.m += s6 * (k1.m + 2.0f * (k2.m + k3.m) + k4.m);
-    y.h += s6 * (k1.h + 2.0f * (k2.h + k3.h) + k4.h);
-    y.n += s6 * (k1.n + 2.0f * (k2.n + k3.n) + k4.n);
-    y.ge += s6 * (k1.ge + 2.0f * (k2.ge + k3.ge) + k4.ge);
-    y.gi += s6 * (k1.gi + 2.0f * (k2.gi + k3.gi) + k4.gi);
+    return nn_hh_state<W>{vfma(k.V, vb<W>(c.V), y.V), vfma(k.m, vb<W>(c.x), y.m), vfma(k.h, vb<W>(c.x), y.h),
+                          vfma(k.n, vb<W>(c.x), y.n), vfma(k.ge, vb<W>(c.ge), y.ge), vfma(k.gi, vb<W>(c.gi), y.gi)};
+}
+
+// y + c (k1 + 2 (k2 + k3) + k4)
+template <int W>
+__device__ __forceinline__ nn_vf<W> nn_rk4_comb(const nn_vf<W>& y, float c, const nn_vf<W>& k1, const nn_vf<W>& k2,
+                                                const nn_vf<W>& k3, const nn_vf<W>& k4)
+{
+    const nn_vf<W> t = vadd(vfma(vadd(k2, k3), vb<W>(2.0f), k1), k4);
+    return vfma(t, vb<W>(c), y);
+}
+
+// One RK4 step of W neurons (external current held over the stages).
+template <int W>
+__device__ __forceinline__ void nn_hh_rk4(const nn_hh_dev& p, const nn_vf<W>& ngna, const nn_vf<W>& iext,
+                                          const nn_vf<W>& ngpu, nn_hh_state<W>& y)
+{
+    const nn_hh_coef c2 = nn_hh_scaled(p, 0.5f * p.dt), c4 = nn_hh_scaled(p, p.dt);
+    const nn_hh_coef c6 = nn_hh_scaled(p, p.dt * (1.0f / 6.0f));
+    const nn_hh_state<W> k1 = nn_hh_rhs(p, ngna, iext, ngpu, y);
+    const nn_hh_state<W> k2 = nn_hh_rhs(p, ngna, iext, ngpu, nn_axpy(y, c2, k1));
+    const nn_hh_state<W> k3 = nn_hh_rhs(p, ngna, iext, ngpu, nn_axpy(y, c2, k2));
+    const nn_hh_state<W> k4 = nn_hh_rhs(p, ngna, iext, ngpu, nn_axpy(y, c4, k3));
+    y.V = nn_rk4_comb(y.V, c6.V, k1.V, k2.V, k3.V, k4.V);
+    y.m = nn_rk4_comb(y.m, c6.x, k1.m, k2.m, k3.m, k4.m);
+    y.h = nn_rk4_comb(y.h, c6.x, k1.h, k2.h, k3.h, k4.h);
+    y.n = nn_rk4_comb(y.n, c6.x, k1.n, k2.n, k3.n, k4.n);
+    y.ge = nn_rk4_comb(y.ge, c6.ge, k1.ge, k2.ge, k3.ge, k4.ge);
+    y.gi = nn_rk4_comb(y.gi, c6.gi, k1.gi, k2.gi, k3.gi, k4.gi);
 }
 
 // Standard normals for the neuron pair (2k, 2k+1) at one step from the

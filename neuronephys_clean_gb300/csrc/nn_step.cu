@@ -1,0 +1,192 @@
+// The neuron update: one RK4 step of every neuron with threshold detection,
+// compaction and push delivery (see the kernel comment).
+#include "nn_step.cuh"
+
+namespace {
+
+// One simulation step, NPT consecutive neurons per lane:
+//   ring slot t%D -> (ge, gi) jump, RK4 with noise, upward threshold crossing,
+//   warp-aggregated compaction (one atomic per warp with spikes), spike bitmap
+//   (pull), voxel deposit, raster, and -- in push mode -- the delivery itself:
+//   the warp that found the spikes scatters their out-edges into ring slots
+//   (t+d)%D with red.global.add (d >= 1, so never the slot this launch reads).
+// Loop trip counts are warp-uniform so the warp collectives stay converged.
+// Resident blocks per SM the neuron update is compiled for: 3 (85 registers)
+// is the fastest of 1, 3 and 4 with packed pairs on the 1M-neuron workload.
+#ifndef NN_HH_MIN_BLOCKS
+#define NN_HH_MIN_BLOCKS 3
+#endif
+template <int NPT>
+__global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
+{
+    const uint64_t t = *a.base + (uint64_t)a.q;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.counts[(t + 1) & 1] = 0;  // next step's count
+    const int slot = (int)(t % (uint64_t)a.D);
+    float* ring_slot = a.ring + (size_t)slot * a.n_pad * 2;
+    int* list = a.list + (size_t)(t & 1) * a.n_pad;
+    int* cnt = a.counts + (t & 1);
+    uint32_t* bm = a.bitmap ? a.bitmap + (size_t)slot * a.words : nullptr;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int chunk = 32 * NPT;
+    const int nchunks = a.n_pad / chunk;
+    for (int ch = warp; ch < nchunks; ch += nwarps) {
+        const int i0 = ch * chunk + lane * NPT;
+        float V[NPT], M[NPT], H[NPT], N[NPT], GE[NPT], GI[NPT], ID[NPT];
+        vload<NPT>(a.V, i0, V);
+        vload<NPT>(a.m, i0, M);
+        vload<NPT>(a.h, i0, H);
+        vload<NPT>(a.nn, i0, N);
+        vload<NPT>(a.ge, i0, GE);
+        vload<NPT>(a.gi, i0, GI);
+        vload<NPT>(a.idrive, i0, ID);
+        float RG[2 * NPT];
+        if (NPT == 1) {
+            const float2 v = *reinterpret_cast<const float2*>(ring_slot + 2 * i0);
+            RG[0] = v.x; RG[1] = v.y;
+        } else {
+#pragma unroll
+            for (int q = 0; q < NPT / 2; ++q) {
+                const float4 v = *reinterpret_cast<const float4*>(ring_slot + 2 * i0 + 4 * q);
+                RG[4 * q] = v.x; RG[4 * q + 1] = v.y; RG[4 * q + 2] = v.z; RG[4 * q + 3] = v.w;
+            }
+        }
+        float GS[NPT], UP[NPT];
+        if (a.gna_scale) vload<NPT>(a.gna_scale, i0, GS);
+        else {
+#pragma unroll
+            for (int q = 0; q < NPT; ++q) GS[q] = 1.0f;
+        }
+        if (a.upar) vload<NPT>(a.upar, i0, UP);
+        else {
+#pragma unroll
+            for (int q = 0; q < NPT; ++q) UP[q] = 0.0f;
+        }
+        // noise: one Philox draw and one Box-Muller per neuron pair
+        float Z[NPT];
+        if (NPT == 1) {
+            Z[0] = nn_normal(a.seed, (uint32_t)i0, t);
+        } else {
+#pragma unroll
+            for (int q = 0; q < NPT; q += 2) nn_normal_pair(a.seed, (uint32_t)(i0 + q) >> 1, t, Z[q], Z[q + 1]);
+        }
+        uint32_t mask = 0;
+        bool bad = false;
+        bool any_in = false;
+        // RK4 on neuron pairs through packed two-lane arithmetic (one lane
+        // when NPT = 1; the results are the same bits either way)
+        constexpr int W = NPT >= 2 ? 2 : 1;
+#pragma unroll
+        for (int p0 = 0; p0 < NPT; p0 += W) {
+            nn_hh_state<W> y;
+            nn_vf<W> ngna, iext, ngpu;
+#pragma unroll
+            for (int l = 0; l < W; ++l) {
+                const int q = p0 + l;
+                y.V.v[l] = V[q]; y.m.v[l] = M[q]; y.h.v[l] = H[q]; y.n.v[l] = N[q];
+                y.ge.v[l] = __fadd_rn(GE[q], RG[2 * q]);
+                y.gi.v[l] = __fadd_rn(GI[q], RG[2 * q + 1]);
+                any_in |= (RG[2 * q] != 0.0f) | (RG[2 * q + 1] != 0.0f);
+                iext.v[l] = __fmaf_rn(a.p.noise_sigma, Z[q], ID[q]);
+                ngna.v[l] = -__fmul_rn(a.p.gNa, GS[q]);
+                ngpu.v[l] = -__fmul_rn(a.p.g_par, UP[q]);
+            }
+            nn_hh_rk4<W>(a.p, ngna, iext, ngpu, y);
+#pragma unroll
+            for (int l = 0; l < W; ++l) {
+                const int q = p0 + l;
+                const bool valid = i0 + q < a.n;
+                const float vn = y.V.v[l];
+                if (valid && V[q] < a.p.v_thresh && vn >= a.p.v_thresh) mask |= 1u << q;
+                if (valid && !isfinite(vn)) bad = true;
+                V[q] = vn; M[q] = y.m.v[l]; H[q] = y.h.v[l]; N[q] = y.n.v[l]; GE[q] = y.ge.v[l]; GI[q] = y.gi.v[l];
+            }
+        }
+        vstore<NPT>(a.V, i0, V);
+        vstore<NPT>(a.m, i0, M);
+        vstore<NPT>(a.h, i0, H);
+        vstore<NPT>(a.nn, i0, N);
+        vstore<NPT>(a.ge, i0, GE);
+        vstore<NPT>(a.gi, i0, GI);
+        if (a.zero_ring && any_in) {
+            if (NPT == 1) {
+                *reinterpret_cast<float2*>(ring_slot + 2 * i0) = make_float2(0.0f, 0.0f);
+            } else {
+#pragma unroll
+                for (int q = 0; q < NPT / 2; ++q)
+                    *reinterpret_cast<float4*>(ring_slot + 2 * i0 + 4 * q) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        }
+        if (bad) atomicOr(a.err, 1);
+        // spike bitmap word of 32 consecutive neurons (pull delivery)
+        if (bm) {
+            uint32_t bits = mask << ((lane * NPT) & 31);
+#pragma unroll
+            for (int o = 1; o < 32 / NPT; o <<= 1) bits |= __shfl_xor_sync(0xffffffffu, bits, o);
+            if ((lane % (32 / NPT)) == 0) bm[(ch * chunk + lane * NPT) >> 5] = bits;
+        }
+        const int c = __popc(mask);
+        if (!__any_sync(0xffffffffu, c != 0)) continue;
+        // warp-aggregated compaction, totals and raster: one atomic each per warp
+        int inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int tv = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += tv;
+        }
+        const int tot = __shfl_sync(0xffffffffu, inc, 31);
+        int base = 0;
+        unsigned long long rbase = 0;
+        if (lane == 31) {
+            base = atomicAdd(cnt, tot);
+            atomicAdd(a.total, (unsigned long long)tot);
+            if (a.raster) rbase = atomicAdd(a.rcount, (unsigned long long)tot);
+        }
+        base = __shfl_sync(0xffffffffu, base, 31);
+        rbase = __shfl_sync(0xffffffffu, rbase, 31);
+        int pos = base + inc - c;
+        unsigned long long rpos = rbase + (unsigned long long)(inc - c);
+#pragma unroll
+        for (int q = 0; q < NPT; ++q)
+            if (mask & (1u << q)) {
+                list[pos++] = i0 + q;
+                if (a.src) atomicAdd(a.src + a.vox[i0 + q], 1.0f);
+                if (a.raster && rpos < (unsigned long long)a.rcap) a.raster[rpos] = make_int2((int)t, i0 + q);
+                ++rpos;
+            }
+        // push delivery of this warp's spikes, all lanes over each out-edge list
+        if (a.row_ptr) {
+            unsigned who = __ballot_sync(0xffffffffu, mask != 0);
+            while (who) {
+                const int sl_lane = __ffs(who) - 1;
+                who &= who - 1;
+                const uint32_t m = __shfl_sync(0xffffffffu, mask, sl_lane);
+#pragma unroll
+                for (int q = 0; q < NPT; ++q) {
+                    if (!(m & (1u << q))) continue;
+                    const int j = ch * chunk + sl_lane * NPT + q;
+                    const int chn = a.is_inh[j] ? 1 : 0;
+                    const int64_t beg = a.row_ptr[j], end = a.row_ptr[j + 1];
+                    for (int64_t e = beg + lane; e < end; e += 32) {
+                        int sl = slot + (int)a.delay[e];
+                        if (sl >= a.D) sl -= a.D;
+                        atomicAdd(a.ring + 2 * ((size_t)sl * a.n_pad + a.col[e]) + chn, a.weight[e]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t nn_launch_hh_step(const StepArgs& a, int npt, int blocks, int tpb, cudaStream_t cs)
+{
+    switch (npt) {
+        case 1: k_hh_step<1><<<blocks, tpb, 0, cs>>>(a); break;
+        case 2: k_hh_step<2><<<blocks, tpb, 0, cs>>>(a); break;
+        default: k_hh_step<4><<<blocks, tpb, 0, cs>>>(a); break;
+    }
+    return cudaPeekAtLastError();
+}

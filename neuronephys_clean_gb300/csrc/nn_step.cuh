@@ -1,0 +1,67 @@
+// The neuron update's launch arguments and its launcher (the kernel is in
+// nn_step.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nn_hh.cuh"
+
+struct StepArgs {
+    float *V, *m, *h, *nn, *ge, *gi;
+    const float* idrive;
+    const float* gna_scale;
+    const float* upar;
+    float* ring;            // float2 (E, I) per neuron, D slots
+    uint32_t* bitmap;       // pull delivery: spike bitmap of the last D steps
+    int* list;              // spikes of the step (by step parity)
+    int* counts;
+    const unsigned long long* base;  // first step of the current period
+    int q;                  // this launch's step within the period
+    // push delivery (row_ptr == nullptr: pull delivery runs as its own kernel)
+    const int64_t* row_ptr;
+    const int32_t* col;
+    const float* weight;
+    const uint8_t* delay;
+    const uint8_t* is_inh;
+    unsigned long long* total;
+    unsigned long long* rcount;
+    int2* raster;
+    long long rcap;
+    const int32_t* vox;
+    float* src;
+    int* err;
+    int n, n_pad, D, words;
+    int zero_ring;
+    uint64_t seed;
+    nn_hh_dev p;
+};
+
+template <int NPT> struct VecT;
+template <> struct VecT<1> { using type = float; };
+template <> struct VecT<2> { using type = float2; };
+template <> struct VecT<4> { using type = float4; };
+
+template <int NPT>
+__device__ __forceinline__ void vload(const float* base, int i0, float (&out)[NPT])
+{
+    using V = typename VecT<NPT>::type;
+    const V v = *reinterpret_cast<const V*>(base + i0);
+    const float* pv = reinterpret_cast<const float*>(&v);
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) out[q] = pv[q];
+}
+
+template <int NPT>
+__device__ __forceinline__ void vstore(float* base, int i0, const float (&in)[NPT])
+{
+    using V = typename VecT<NPT>::type;
+    V v;
+    float* pv = reinterpret_cast<float*>(&v);
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) pv[q] = in[q];
+    *reinterpret_cast<V*>(base + i0) = v;
+}
+
+// One step of every neuron on stream cs (NPT neurons per thread: 1, 2 or 4).
+cudaError_t nn_launch_hh_step(const StepArgs& a, int npt, int blocks, int tpb, cudaStream_t cs);
