@@ -51,7 +51,7 @@ WORKLOADS = {
                # iterations of the FP64 oracle PCG to 1e-6 on this seeded instance
                # (oracle.pcg7 run to convergence once; the CPU arms time a bounded
                # number of iterations and scale by this count)
-               fp64_iters=329, train_rhs=6, train_steps=400),
+               fp64_iters=329, train_rhs=6, train_steps=400, lmg_train_steps=1500),
     "c1": dict(workload="hh_1k_er_p0.01_grid32", n=1000, kind="er", p=0.01, w_max=0.5, dmax=1, inh=0.2,
                i_lo=5.0, i_hi=15.0, grid=32, timescale=100, par_D=1.0, par_decay=0.0, total_steps=10000),
 }
@@ -608,6 +608,7 @@ def run_cg(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
                 "d2h_bytes_per_step": 4 * G},
     }
     line["multigrid"] = multigrid_cg(nn, ctx, pc, G, db, ms_solve, it_mean, args)
+    line["learned_multigrid"] = learned_multigrid_cg(nn, ctx, pc, wl, shape, G, db, ms_solve, it_mean, args)
     if args.learned:
         line["learned"] = learned_cg(nn, ctx, pc, wl, shape, db, ms_solve, it_mean, args)
     if args.cpu_baseline:
@@ -639,6 +640,52 @@ def multigrid_cg(nn, ctx, pc, G, db, plain_ms, plain_iters, args) -> dict:
             "ms_per_iteration": ms / statistics.mean(its), "vs_plain_time": ms / plain_ms,
             "vs_plain_iterations": statistics.mean(its) / plain_iters,
             "solution_norm": float(np.linalg.norm(dx.numpy().astype(np.float64)))}
+
+
+def learned_multigrid_cg(nn, ctx, pc, wl, shape, G, db, plain_ms, plain_iters, args) -> dict:
+    """Multigrid FCG whose 32^3 level (and all below) is solved by the U-Net:
+    training pairs from classical solves of fresh right-hand sides, Adam on
+    the GPU, then timed solves of the bench right-hand side.  Beside it: the
+    classical hierarchy on the same object, and the hierarchy cut at 32^3
+    (eight Jacobi sweeps there instead of the levels below)."""
+    from neuronephys_clean_gb300 import fields
+    level = 3
+    lm = nn.LearnedMultigrid(pc, level=level, seed=7)
+    t0 = time.perf_counter()
+    rhs = [fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=2000 + j) for j in range(wl["train_rhs"])]
+    pairs = lm.add_solves(rhs)
+    t_pairs = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = lm.train(wl["lmg_train_steps"], 1e-3)
+    t_train = time.perf_counter() - t0
+    dx = ctx.empty((G,), np.float32)
+
+    def timed(solve):
+        for _ in range(max(1, args.warmup)):
+            dx.zero()
+            solve(db, dx)
+        times, its, rel = [], [], 0.0
+        for _ in range(args.steps):
+            dx.zero()
+            ctx.time_begin()
+            it, rel = solve(db, dx)
+            times.append(ctx.time_end())
+            its.append(it)
+        return statistics.mean(times), statistics.mean(its), rel
+
+    ms, it, rel = timed(lambda b, x: lm.solve(b, x, 1e-6))
+    lm.use_network(False)
+    ms_c, it_c, _ = timed(lambda b, x: lm.solve(b, x, 1e-6))
+    lm.close()
+    cut = nn.MultigridPCG(pc, level + 1)
+    ms_t, it_t, _ = timed(lambda b, x: cut.solve(b, x, 1e-6))
+    cut.close()
+    return {"ms_to_tol": ms, "iterations": it, "relres": rel, "vs_plain_time": ms / plain_ms,
+            "vs_plain_iterations": it / plain_iters, "network_level_grid": shape[0] >> level,
+            "classical_hierarchy": {"ms_to_tol": ms_c, "iterations": it_c},
+            "cut_at_network_level": {"ms_to_tol": ms_t, "iterations": it_t},
+            "training": {"pairs": pairs, "pair_generation_s": t_pairs, "adam_steps": wl["lmg_train_steps"],
+                         "train_s": t_train, "final_loss": loss}}
 
 
 def learned_cg(nn, ctx, pc, wl, shape, db, plain_ms, plain_iters, args) -> dict:

@@ -471,6 +471,30 @@ NN_API nn_status nn_mg_apply(nn_mg* mg, const float* d_r, float* d_z);
 NN_API nn_status nn_mg_solve(nn_mg* mg, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
                              double* relres);
 
+/* Multigrid with a learned coarse-level solver (no counterpart in the
+ * reference).  The geometric hierarchy of nn_mg_create in which one coarse
+ * level (level >= 1; its sides multiples of 4) and everything below it are
+ * replaced by the 3D conv U-Net of the learned preconditioner: the level's
+ * right-hand side b goes in divided by its RMS, together with the log of the
+ * level's diagonal; the output times that RMS is the level's correction,
+ * followed by the V-cycle's post-smoothing there.  nn_lmg_add_solve solves
+ * A x = b with the classical hierarchy from x = 0 (d_x receives the solution)
+ * and stores, for every V-cycle, the right-hand side that reached the level
+ * and its solution on that level as a training pair (*pairs_added);
+ * nn_lmg_train runs Adam steps over the stored pairs; nn_lmg_solve runs
+ * flexible CG to the same relative residual as nn_pcg_solve.
+ * nn_lmg_use_network(lm, 0) switches back to the classical hierarchy, for
+ * comparisons.  The nn_pcg (and its cell field) must outlive the nn_lmg. */
+typedef struct nn_lmg nn_lmg;
+NN_API nn_status nn_lmg_create(nn_pcg* pc, int level, uint64_t seed, nn_lmg** out);
+NN_API nn_status nn_lmg_destroy(nn_lmg* lm);
+NN_API nn_status nn_lmg_add_solve(nn_lmg* lm, const float* d_b, float* d_x, int* pairs_added);
+NN_API nn_status nn_lmg_pairs(nn_lmg* lm, int* n);
+NN_API nn_status nn_lmg_train(nn_lmg* lm, int steps, float lr, float* mean_loss);
+NN_API nn_status nn_lmg_use_network(nn_lmg* lm, int enable);
+NN_API nn_status nn_lmg_solve(nn_lmg* lm, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
+                              double* relres);
+
 /* Learned two-grid preconditioner for the 7-point operator of an nn_pcg
  * (grid sides multiples of 8): Jacobi smoothing on the fine grid and a
  * coarse-grid correction by a 3-level 3D conv U-Net (16/32/64 channels, BF16

@@ -24,7 +24,7 @@ from . import _lib as L
 from ._lib import HHParams, KernelTimes, LeapfrogParams, NetSpec, ParacrineRefParams, SimConfig, SolveStats
 
 __all__ = ["NNError", "Context", "DeviceArray", "HHEphys", "AtomicCoupling", "AdjacencyList",
-           "ChunkedAdjacencyList", "UniformRandomNetwork", "ParacrineModule", "Simulation", "PCG", "MultigridPCG",
+           "ChunkedAdjacencyList", "UniformRandomNetwork", "ParacrineModule", "Simulation", "PCG", "MultigridPCG", "LearnedMultigrid",
            "SimConfig", "HHParams", "NetSpec", "LeapfrogParams", "ParacrineRefParams",
            "lib", "NN_SIGNAL_COUNT", "NN_SIGNAL_OUTPUT", "FIELDS"]
 
@@ -673,6 +673,63 @@ class MultigridPCG:
     def close(self):
         if self.handle:
             lib().nn_mg_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LearnedMultigrid:
+    """Multigrid FCG whose coarse level `level` (and everything below it) is
+    solved by the learned 3D conv U-Net (nn_lmg_*).  Train with
+    add_solves(rhs) + train(); use_network(False) gives the classical
+    hierarchy on the same object.  The PCG object must stay alive."""
+
+    def __init__(self, pcg: PCG, level: int = 3, seed: int = 7):
+        self.ctx, self.pcg = pcg.ctx, pcg
+        self.handle = C.c_void_p()
+        _check(lib().nn_lmg_create(pcg.handle, level, seed, C.byref(self.handle)), self.ctx, "nn_lmg_create")
+
+    def add_solves(self, rhs_list) -> int:
+        """Solve each right-hand side (host arrays) with the classical hierarchy
+        and keep the level's right-hand sides and solutions as training pairs;
+        returns the number of pairs added."""
+        total = 0
+        for b in rhs_list:
+            hb = np.ascontiguousarray(b, np.float32).ravel()
+            db = self.ctx.to_device(hb)
+            dx = self.ctx.empty((hb.size,), np.float32)
+            k = C.c_int(0)
+            _check(lib().nn_lmg_add_solve(self.handle, db.ptr, dx.ptr, C.byref(k)), self.ctx, "nn_lmg_add_solve")
+            total += k.value
+        return total
+
+    @property
+    def pairs(self) -> int:
+        n = C.c_int(0)
+        _check(lib().nn_lmg_pairs(self.handle, C.byref(n)), self.ctx, "nn_lmg_pairs")
+        return n.value
+
+    def train(self, steps: int, lr: float = 1e-3) -> float:
+        loss = C.c_float(0)
+        _check(lib().nn_lmg_train(self.handle, steps, lr, C.byref(loss)), self.ctx, "nn_lmg_train")
+        return loss.value
+
+    def use_network(self, on: bool = True) -> None:
+        _check(lib().nn_lmg_use_network(self.handle, int(on)), self.ctx, "nn_lmg_use_network")
+
+    def solve(self, b: DeviceArray, x: DeviceArray, rtol: float = 1e-6, max_iter: int = 1000) -> tuple[int, float]:
+        it, rel = C.c_int(0), C.c_double(0)
+        _check(lib().nn_lmg_solve(self.handle, b.ptr, x.ptr, rtol, max_iter, C.byref(it), C.byref(rel)), self.ctx,
+               "nn_lmg_solve")
+        return it.value, rel.value
+
+    def close(self):
+        if self.handle:
+            lib().nn_lmg_destroy(self.handle)
             self.handle = C.c_void_p()
 
     def __del__(self):

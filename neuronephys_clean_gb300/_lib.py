@@ -167,6 +167,13 @@ _SIGS = {
     "nn_mg_levels": (c_int, [c_void_p, P(c_int)]),
     "nn_mg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
     "nn_mg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
+    "nn_lmg_create": (c_int, [c_void_p, c_int, c_uint64, P(c_void_p)]),
+    "nn_lmg_destroy": (c_int, [c_void_p]),
+    "nn_lmg_add_solve": (c_int, [c_void_p, c_void_p, c_void_p, P(c_int)]),
+    "nn_lmg_pairs": (c_int, [c_void_p, P(c_int)]),
+    "nn_lmg_train": (c_int, [c_void_p, c_int, c_float, P(c_float)]),
+    "nn_lmg_use_network": (c_int, [c_void_p, c_int]),
+    "nn_lmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_learned_create": (c_int, [c_void_p, c_uint64, P(c_void_p)]),
     "nn_learned_destroy": (c_int, [c_void_p]),
     "nn_learned_add_pair": (c_int, [c_void_p, c_void_p, c_void_p]),

@@ -159,6 +159,21 @@ void nn_pcg_info(const nn_pcg* pc, nn_ctx** ctx, int* nx, int* ny, int* nz, cons
 // The operator's coefficients: A = (1 + beta) I + alpha L_D.
 void nn_pcg_coefficients(const nn_pcg* pc, double* alpha, double* beta);
 
+// multigrid internals (nn_mg.cu) used by the learned coarse solver (nn_unet.cu)
+struct nn_mg;
+// replaces the treatment of one level: x = solve(b) on that level's grid,
+// followed by the V-cycle's post-smoothing there; enqueued on the context
+// stream, never synchronising (it may run inside a captured graph)
+typedef nn_status (*nn_mg_level_fn)(void* user, const float* d_b, float* d_x);
+// sees the right-hand side reaching one level in each V-cycle (enqueue only)
+typedef nn_status (*nn_mg_record_fn)(void* user, const float* d_b);
+nn_status nn_mg_set_level_solver(nn_mg* mg, int level, nn_mg_level_fn fn, void* user);  // fn null: classical
+nn_status nn_mg_set_recorder(nn_mg* mg, int level, nn_mg_record_fn fn, void* user);    // fn null: off
+// dims and diagonal of level >= 1
+nn_status nn_mg_level_dims(const nn_mg* mg, int level, int* nx, int* ny, int* nz, const float** diag);
+// Jacobi-PCG on level >= 1 from x = 0 to rtol (synchronising; for training targets)
+nn_status nn_mg_level_cg(nn_mg* mg, int level, const float* d_b, float* d_x, double rtol, int max_iter, int* iters);
+
 // batched PCG (nn_bpcg.cu)
 int64_t nn_bpcg_cells(const nn_bpcg* bp);
 const int64_t* nn_bpcg_offsets(const nn_bpcg* bp);

@@ -698,6 +698,95 @@ __global__ void __launch_bounds__(MG_THREADS) k_fcg_update(float* x, float* r, c
     }
 }
 
+// ---------------------------------------------- Jacobi-PCG on one level --
+// (training targets for a learned level solver; host-driven, small grids)
+
+// x = 0; r = b; p = D^-1 r; (r, D^-1 r), (b, b)
+__global__ void __launch_bounds__(MG_THREADS) k_lcg_init(OpF op, const float* b, float* x, float* r, float* p, Red red)
+{
+    float acc[2] = {0.0f, 0.0f};
+    MG_ROWS(op.ny, op.nz, row)
+    {
+        for (int i = threadIdx.x; i < op.nx; i += blockDim.x) {
+            const int c = i + op.nx * row;
+            const float bc = b[c];
+            x[c] = 0.0f;
+            r[c] = bc;
+            const float z = __fdividef(bc, op.diag[c]);
+            p[c] = z;
+            acc[0] += bc * z;
+            acc[1] += bc * bc;
+        }
+    }
+    double o[2];
+    if (mg_reduce<2>(acc, red.partials, red.ticket, o) && is_tid0()) {
+        red.scal[S_RZ] = o[0];
+        red.scal[S_BB] = o[1];
+        red.scal[S_RR] = o[1];
+    }
+}
+
+// q = A p; (p, q)
+__global__ void __launch_bounds__(MG_THREADS) k_lcg_ap(OpF op, const float* p, float* q, Red red)
+{
+    float acc[1] = {0.0f};
+    MG_ROWS(op.ny, op.nz, row)
+    {
+        const int j = row % op.ny, k = row / op.ny;
+        for (int i = threadIdx.x; i < op.nx; i += blockDim.x) {
+            const int c = i + op.nx * row;
+            Nb<1> pn;
+            gather(FPlain{p}, c, i, j, k, op.nx, op.ny, op.nz, pn);
+            float qv[1], dg[1];
+            op.template apply<1>(c, i, j, k, pn, qv, dg);
+            q[c] = qv[0];
+            acc[0] += pn.c[0] * qv[0];
+        }
+    }
+    double o[1];
+    if (mg_reduce<1>(acc, red.partials, red.ticket, o) && is_tid0()) red.scal[S_PQ] = o[0];
+}
+
+// a = (r, z) / (p, q); x += a p; r -= a q; new (r, z) and (r, r); beta
+__global__ void __launch_bounds__(MG_THREADS) k_lcg_update(OpF op, float* x, float* r, const float* p, const float* q,
+                                                           Red red)
+{
+    const double pq = red.scal[S_PQ];
+    const float a = pq > 0.0 ? (float)(red.scal[S_RZ] / pq) : 0.0f;
+    float acc[2] = {0.0f, 0.0f};
+    MG_ROWS(op.ny, op.nz, row)
+    {
+        for (int i = threadIdx.x; i < op.nx; i += blockDim.x) {
+            const int c = i + op.nx * row;
+            x[c] += a * p[c];
+            const float rc = r[c] - a * q[c];
+            r[c] = rc;
+            acc[0] += rc * __fdividef(rc, op.diag[c]);
+            acc[1] += rc * rc;
+        }
+    }
+    double o[2];
+    if (mg_reduce<2>(acc, red.partials, red.ticket, o) && is_tid0()) {
+        const double rz_old = red.scal[S_RZ];
+        red.scal[S_BETA] = rz_old > 0.0 ? o[0] / rz_old : 0.0;
+        red.scal[S_RZ] = o[0];
+        red.scal[S_RR] = o[1];
+    }
+}
+
+// p = D^-1 r + beta p
+__global__ void __launch_bounds__(MG_THREADS) k_lcg_dir(OpF op, const float* r, float* p, Red red)
+{
+    const float bt = (float)red.scal[S_BETA];
+    MG_ROWS(op.ny, op.nz, row)
+    {
+        for (int i = threadIdx.x; i < op.nx; i += blockDim.x) {
+            const int c = i + op.nx * row;
+            p[c] = __fdividef(r[c], op.diag[c]) + bt * p[c];
+        }
+    }
+}
+
 }  // namespace
 
 // ================================================================ object ==
@@ -731,6 +820,16 @@ struct nn_mg {
     float* graph_x = nullptr;    // solution array the graph was captured for
     int64_t graph_launches = 0;
     int last_iters = 0;
+    // optional replacement of one level's coarse treatment (that level's
+    // pre-smoothing and everything below it) by a caller's solver
+    int hook_level = -1;
+    nn_mg_level_fn hook_fn = nullptr;
+    void* hook_user = nullptr;
+    // optional recorder of the right-hand sides that reach one level (solves
+    // then run without the captured graph)
+    int rec_level = -1;
+    nn_mg_record_fn rec_fn = nullptr;
+    void* rec_user = nullptr;
 };
 
 namespace {
@@ -799,6 +898,22 @@ template <int V, class Op>
 nn_status vlevel(nn_mg* mg, int l, const Op& op, const float* b, float* out, const int* flags, const float* dots_q)
 {
     MgLevel& L = mg->lv[l];
+    if (mg->rec_fn && l == mg->rec_level) NN_TRY(mg->rec_fn(mg->rec_user, b));
+    if (mg->hook_fn && l == mg->hook_level) {
+        // the caller's solver for this level, then nu smoothing sweeps
+        float* cur = L.x;
+        float* oth = L.t;
+        NN_TRY(mg->hook_fn(mg->hook_user, b, cur));
+        for (int s = 0; s < mg->nu; ++s) {
+            float* dst = (s == mg->nu - 1 && out != cur) ? out : oth;
+            NN_TRY((launch_jacobi<V, false>(mg, op, b, cur, dst, flags)));
+            oth = cur;
+            cur = dst;
+        }
+        if (cur != out)
+            NN_CUDA(mg->ctx, cudaMemcpyAsync(out, cur, sizeof(float) * L.G, cudaMemcpyDeviceToDevice, mg->ctx->stream));
+        return NN_OK;
+    }
     const bool coarsest = l + 1 == (int)mg->lv.size();
     const int sweeps = coarsest ? mg->coarse_sweeps : mg->nu;
     // pre-smoothing (or the coarsest solve): ping-pong, ending in L.x
@@ -992,7 +1107,7 @@ extern "C" nn_status nn_mg_create(nn_pcg* pc, int levels, nn_mg** out)
     mg->nblocks = std::max(1, std::min((G + MG_THREADS - 1) / MG_THREADS, ctx->num_sms * 8));
     if (st == NN_OK) st = nn_alloc(ctx, &mg->scal, S_COUNT);
     if (st == NN_OK) st = nn_alloc(ctx, &mg->flags, F_COUNT);
-    if (st == NN_OK) st = nn_alloc(ctx, &mg->partials, (size_t)2 * mg->nblocks);
+    if (st == NN_OK) st = nn_alloc(ctx, &mg->partials, (size_t)2 * std::max(mg->nblocks, ctx->num_sms * 8));
     if (st == NN_OK) st = nn_alloc(ctx, &mg->ticket, 1);
     if (st == NN_OK)
         st = nn_cuda_check(ctx, cudaMallocHost((void**)&mg->h_flags, sizeof(int) * F_COUNT), "cudaMallocHost");
@@ -1046,7 +1161,7 @@ extern "C" nn_status nn_mg_solve(nn_mg* mg, const float* d_b, float* d_x, double
     const MgLevel& L = mg->lv[0];
     const double rtol2 = rtol * rtol;
     const Red red = red_of(mg);
-    NN_TRY(ensure_graph(mg, d_x));
+    if (!mg->rec_fn) NN_TRY(ensure_graph(mg, d_x));
     k_fcg_set<<<1, 1, 0, cs>>>(mg->scal, mg->flags, rtol2, max_iter);
     NN_CHECK_LAUNCH(ctx, "k_fcg_set");
     const dim3 blk = shape_for(ctx, L.nx / mg->vec0, L.ny * L.nz).block;
@@ -1058,13 +1173,17 @@ extern "C" nn_status nn_mg_solve(nn_mg* mg, const float* d_b, float* d_x, double
     k_fcg_first<<<mg->nblocks, dim3(MG_THREADS), 0, cs>>>(mg->r, mg->z, mg->p[0], L.G, red);
     NN_CHECK_LAUNCH(ctx, "k_fcg_first");
     // graph launches (two iterations each); the first chunk covers the last
-    // solve's iteration count
+    // solve's iteration count.  While recording, the iterations are enqueued
+    // directly instead (the recorder copies to a new place each time).
     int launched = 0;
     int chunk = mg->last_iters > 0 ? (mg->last_iters + 1) / 2 : 4;
     while (launched < max_iter) {
         const int k = std::min(chunk, (max_iter - launched + 1) / 2);
-        for (int q = 0; q < k; ++q) NN_CUDA(ctx, cudaGraphLaunch(mg->graph, cs));
-        ctx->launches += mg->graph_launches * k;
+        for (int q = 0; q < k; ++q) {
+            if (mg->rec_fn) NN_TRY(enqueue_iterations(mg, d_x));
+            else NN_CUDA(ctx, cudaGraphLaunch(mg->graph, cs));
+        }
+        if (!mg->rec_fn) ctx->launches += mg->graph_launches * k;
         launched += 2 * k;
         NN_CUDA(ctx, cudaMemcpyAsync(mg->h_flags, mg->flags, sizeof(int) * F_COUNT, cudaMemcpyDeviceToHost, cs));
         NN_CUDA(ctx, cudaStreamSynchronize(cs));
@@ -1083,5 +1202,71 @@ extern "C" nn_status nn_mg_solve(nn_mg* mg, const float* d_b, float* d_x, double
     if (!(sc[S_RR] <= rtol2 * sc[S_BB]))
         return nn_fail(ctx, NN_ERR_NOT_CONVERGED, "multigrid FCG did not reach rtol %g in %d iterations", rtol,
                        max_iter);
+    return NN_OK;
+}
+
+// ------------------------------------------------ hooks for level solvers --
+
+nn_status nn_mg_set_level_solver(nn_mg* mg, int level, nn_mg_level_fn fn, void* user)
+{
+    if (!mg || (fn && (level < 1 || level >= (int)mg->lv.size()))) return NN_ERR_INVALID_ARG;
+    drop_graph(mg);
+    mg->hook_level = fn ? level : -1;
+    mg->hook_fn = fn;
+    mg->hook_user = user;
+    mg->last_iters = 0;
+    return NN_OK;
+}
+
+nn_status nn_mg_set_recorder(nn_mg* mg, int level, nn_mg_record_fn fn, void* user)
+{
+    if (!mg || (fn && (level < 1 || level >= (int)mg->lv.size()))) return NN_ERR_INVALID_ARG;
+    mg->rec_level = fn ? level : -1;
+    mg->rec_fn = fn;
+    mg->rec_user = user;
+    return NN_OK;
+}
+
+nn_status nn_mg_level_dims(const nn_mg* mg, int level, int* nx, int* ny, int* nz, const float** diag)
+{
+    if (!mg || level < 1 || level >= (int)mg->lv.size()) return NN_ERR_INVALID_ARG;
+    const MgLevel& L = mg->lv[level];
+    *nx = L.nx;
+    *ny = L.ny;
+    *nz = L.nz;
+    *diag = L.diag;
+    return NN_OK;
+}
+
+nn_status nn_mg_level_cg(nn_mg* mg, int level, const float* d_b, float* d_x, double rtol, int max_iter, int* iters)
+{
+    if (!mg || !d_b || !d_x || level < 1 || level >= (int)mg->lv.size()) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = mg->ctx;
+    cudaStream_t cs = ctx->stream;
+    MgLevel& L = mg->lv[level];
+    const OpF op = L.op();
+    const Red red = red_of(mg);
+    const Shape sh = shape_for(ctx, L.nx, L.ny * L.nz);
+    // work vectors: the level's own x / t buffers serve as r and p, the
+    // next-finer level's t as q (all larger than this level)
+    float* r = L.x;
+    float* p = L.t;
+    float* q = mg->lv[level - 1].t;
+    k_lcg_init<<<sh.grid, sh.block, 0, cs>>>(op, d_b, d_x, r, p, red);
+    NN_CHECK_LAUNCH(ctx, "k_lcg_init");
+    double sc[S_COUNT];
+    int it = 0;
+    for (; it < max_iter; ++it) {
+        NN_CUDA(ctx, nn_copy_sync(ctx, sc, mg->scal, sizeof sc, cudaMemcpyDeviceToHost));
+        if (!(sc[S_RR] > rtol * rtol * sc[S_BB])) break;
+        k_lcg_ap<<<sh.grid, sh.block, 0, cs>>>(op, p, q, red);
+        NN_CHECK_LAUNCH(ctx, "k_lcg_ap");
+        k_lcg_update<<<sh.grid, sh.block, 0, cs>>>(op, d_x, r, p, q, red);
+        NN_CHECK_LAUNCH(ctx, "k_lcg_update");
+        k_lcg_dir<<<sh.grid, sh.block, 0, cs>>>(op, r, p, red);
+        NN_CHECK_LAUNCH(ctx, "k_lcg_dir");
+    }
+    if (iters) *iters = it;
+    if (!std::isfinite(sc[S_RR])) return nn_fail(ctx, NN_ERR_NUMERIC, "level CG: non-finite residual");
     return NN_OK;
 }

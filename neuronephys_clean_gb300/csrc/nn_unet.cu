@@ -932,3 +932,235 @@ extern "C" nn_status nn_learned_net_gradient(nn_learned* lp, const float* d_rc, 
     }
     return NN_OK;
 }
+
+// ------------------------------------------ learned coarse-level solver --
+
+namespace {
+// out = b / d (the Jacobi-scaled right-hand side, whose solution has the
+// scale of the input)
+__global__ void k_div(const float* b, const float* d, float* out, int64_t n)
+{
+    GRID_LOOP(i, n) out[i] = b[i] / d[i];
+}
+}  // namespace
+//
+// A multigrid hierarchy (nn_mg, all levels) in which the treatment of one
+// coarse level -- its pre-smoothing and every level below it -- is replaced
+// by the U-Net: x_L = s N(D^-1 b_L / s, f), s = rms(D^-1 b_L), D the level's
+// diagonal, f = log D minus its mean, followed by the V-cycle's
+// post-smoothing on that level.  (D^-1 b has the scale of the solution; b
+// itself is thousands of times larger on a coarse level.)  Training pairs: the right-hand sides that reach that level while
+// the classical hierarchy solves given systems, and their solutions on that
+// level (Jacobi-PCG to 1e-7).  Without the network (use_network = 0) the
+// hierarchy is the classical one.
+
+struct nn_lmg {
+    nn_ctx* ctx = nullptr;
+    nn_pcg* pc = nullptr;
+    nn_mg* mg = nullptr;
+    nn_unet* net = nullptr;
+    int level = 0, nx = 0, ny = 0, nz = 0;
+    int64_t Gc = 0, G = 0;  // cells of the network's level and of the fine grid
+    float* feat = nullptr;
+    const float* diag = nullptr;  // the level's diagonal (owned by the hierarchy)
+    float* bs = nullptr;          // D^-1 b of the level solve
+    std::vector<float*> pair_b, pair_e, rec;
+    size_t max_pairs = 4096;
+    uint64_t rng = 0x2545F4914F6CDD1Dull;
+    int use_net = 1;
+};
+
+static nn_status lmg_level_solve(void* user, const float* b, float* x)
+{
+    nn_lmg* lm = static_cast<nn_lmg*>(user);
+    NN_TRY(launch(lm->ctx, lm->Gc, "k_div", k_div, b, lm->diag, lm->bs, lm->Gc));
+    NN_TRY(unet_forward(lm->net, lm->bs, lm->feat));
+    return launch(lm->ctx, lm->Gc, "k_scale_out", k_scale_out, (const float*)lm->net->y32,
+                  (const double*)lm->net->scal, x, lm->Gc);
+}
+
+static nn_status lmg_record(void* user, const float* b)
+{
+    nn_lmg* lm = static_cast<nn_lmg*>(user);
+    if (lm->pair_b.size() + lm->rec.size() >= lm->max_pairs) return NN_OK;
+    float* v = nullptr;
+    NN_TRY(nn_alloc(lm->ctx, &v, (size_t)lm->Gc));
+    lm->rec.push_back(v);
+    NN_CUDA(lm->ctx, cudaMemcpyAsync(v, b, sizeof(float) * lm->Gc, cudaMemcpyDeviceToDevice, lm->ctx->stream));
+    return NN_OK;
+}
+
+// training input of a recorded right-hand side: D^-1 b (in place)
+static nn_status lmg_scale_input(nn_lmg* lm, float* b)
+{
+    return launch(lm->ctx, lm->Gc, "k_div", k_div, (const float*)b, lm->diag, b, lm->Gc);
+}
+
+static nn_status lmg_apply_mode(nn_lmg* lm)
+{
+    return nn_mg_set_level_solver(lm->mg, lm->level, lm->use_net ? lmg_level_solve : nullptr, lm);
+}
+
+extern "C" nn_status nn_lmg_destroy(nn_lmg* lm)
+{
+    if (!lm) return NN_OK;
+    if (lm->ctx) cudaStreamSynchronize(lm->ctx->stream);
+    if (lm->mg) nn_mg_destroy(lm->mg);
+    nn_unet_free(lm->net);
+    cudaFree(lm->feat);
+    cudaFree(lm->bs);
+    for (float* v : lm->pair_b) cudaFree(v);
+    for (float* v : lm->pair_e) cudaFree(v);
+    for (float* v : lm->rec) cudaFree(v);
+    nn_ctx* ctx = lm->ctx;
+    delete lm;
+    if (ctx) nn_ctx_release(ctx);
+    return NN_OK;
+}
+
+extern "C" nn_status nn_lmg_create(nn_pcg* pc, int level, uint64_t seed, nn_lmg** out)
+{
+    if (!pc || !out || level < 1) return NN_ERR_INVALID_ARG;
+    *out = nullptr;
+    nn_ctx* ctx;
+    int fx, fy, fz;
+    const float* invd;
+    float invd_c;
+    const float* D;
+    nn_pcg_info(pc, &ctx, &fx, &fy, &fz, &invd, &invd_c, &D);
+    nn_lmg* lm = new nn_lmg();
+    lm->ctx = ctx;
+    nn_ctx_retain(ctx);
+    lm->pc = pc;
+    lm->level = level;
+    lm->G = (int64_t)fx * fy * fz;
+    nn_status st = nn_mg_create(pc, 0, &lm->mg);
+    const float* diag = nullptr;
+    if (st == NN_OK) st = nn_mg_level_dims(lm->mg, level, &lm->nx, &lm->ny, &lm->nz, &diag);
+    if (st == NN_OK && (lm->nx % 4 || lm->ny % 4 || lm->nz % 4))
+        st = nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_lmg_create: level %d is %dx%dx%d; the network needs sides that are "
+                     "multiples of 4", level, lm->nx, lm->ny, lm->nz);
+    if (st == NN_OK) {
+        lm->Gc = (int64_t)lm->nx * lm->ny * lm->nz;
+        st = nn_unet_make(ctx, lm->nz, lm->ny, lm->nx, seed, &lm->net);
+    }
+    if (st == NN_OK) st = nn_alloc(ctx, &lm->feat, (size_t)lm->Gc);
+    if (st == NN_OK) st = nn_alloc(ctx, &lm->bs, (size_t)lm->Gc);
+    lm->diag = diag;
+    if (st == NN_OK) {
+        // feature channel: log diag - mean
+        std::vector<float> h((size_t)lm->Gc);
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, h.data(), diag, sizeof(float) * h.size(), cudaMemcpyDeviceToHost),
+                           "nn_lmg_create");
+        if (st == NN_OK) {
+            double mean = 0.0;
+            for (float& v : h) {
+                v = std::log(std::max(v, 1e-30f));
+                mean += v;
+            }
+            mean /= (double)h.size();
+            for (float& v : h) v = (float)(v - mean);
+            st = nn_cuda_check(ctx, nn_copy_sync(ctx, lm->feat, h.data(), sizeof(float) * h.size(),
+                                                 cudaMemcpyHostToDevice), "nn_lmg_create");
+        }
+    }
+    // one forward pass on zeros, so that every kernel's attributes are set
+    // before a solve may capture the network into a graph
+    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, lm->net->y32, sizeof(float) * lm->Gc), "nn_lmg_create");
+    if (st == NN_OK) st = unet_forward(lm->net, lm->net->y32, lm->feat);
+    if (st == NN_OK) st = check_err(lm->net);
+    if (st == NN_OK) st = lmg_apply_mode(lm);
+    if (st != NN_OK) {
+        nn_lmg_destroy(lm);
+        return st;
+    }
+    *out = lm;
+    return NN_OK;
+}
+
+// Solve A x = b with the classical hierarchy from x = 0, record the
+// right-hand sides that reach the network's level, and store each with its
+// solution on that level as a training pair.
+extern "C" nn_status nn_lmg_add_solve(nn_lmg* lm, const float* d_b, float* d_x, int* pairs_added)
+{
+    if (!lm || !d_b || !d_x) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = lm->ctx;
+    NN_TRY(nn_mg_set_level_solver(lm->mg, lm->level, nullptr, nullptr));
+    NN_TRY(nn_mg_set_recorder(lm->mg, lm->level, lmg_record, lm));
+    NN_CUDA(ctx, nn_zero_async(ctx, d_x, sizeof(float) * lm->G));
+    int it = 0;
+    double rel = 0.0;
+    nn_status st = nn_mg_solve(lm->mg, d_b, d_x, 1e-6, 500, &it, &rel);
+    nn_mg_set_recorder(lm->mg, lm->level, nullptr, nullptr);
+    int added = 0;
+    for (float* b : lm->rec) {
+        float* e = nullptr;
+        if (st == NN_OK) st = nn_alloc(ctx, &e, (size_t)lm->Gc);
+        if (st == NN_OK) st = nn_mg_level_cg(lm->mg, lm->level, b, e, 1e-7, 5000, nullptr);
+        if (st == NN_OK) st = lmg_scale_input(lm, b);
+        if (st == NN_OK) {
+            lm->pair_b.push_back(b);
+            lm->pair_e.push_back(e);
+            ++added;
+        } else {
+            cudaFree(b);
+            cudaFree(e);
+        }
+    }
+    lm->rec.clear();
+    const nn_status st2 = lmg_apply_mode(lm);
+    if (pairs_added) *pairs_added = added;
+    return st != NN_OK ? st : st2;
+}
+
+extern "C" nn_status nn_lmg_train(nn_lmg* lm, int steps, float lr, float* mean_loss)
+{
+    if (!lm || steps < 0 || !(lr > 0.0f)) return NN_ERR_INVALID_ARG;
+    if (lm->pair_b.empty()) return nn_fail(lm->ctx, NN_ERR_INVALID_ARG, "nn_lmg_train: no training pairs");
+    nn_ctx* ctx = lm->ctx;
+    nn_unet* u = lm->net;
+    NN_CUDA(ctx, cudaMemsetAsync(u->scal + 1, 0, sizeof(double), ctx->stream));
+    NN_CUDA(ctx, cudaMemsetAsync(u->err, 0, sizeof(int), ctx->stream));
+    for (int it = 0; it < steps; ++it) {
+        lm->rng ^= lm->rng << 13;
+        lm->rng ^= lm->rng >> 7;
+        lm->rng ^= lm->rng << 17;
+        const size_t k = (size_t)(lm->rng % lm->pair_b.size());
+        NN_TRY(unet_forward(u, lm->pair_b[k], lm->feat));
+        NN_TRY(launch(ctx, u->G0, "k_net_loss", k_net_loss, (const float*)u->y32, (const float*)lm->pair_e[k],
+                      (const double*)u->scal, (uint4*)u->gOUT, u->g[0], u->scal + 1));
+        NN_TRY(unet_backward(u));
+        NN_TRY(unet_adam(u, lr));
+    }
+    NN_TRY(check_err(u));
+    double loss = 0.0;
+    NN_CUDA(ctx, nn_copy_sync(ctx, &loss, u->scal + 1, sizeof(double), cudaMemcpyDeviceToHost));
+    if (mean_loss) *mean_loss = steps ? (float)(loss / ((double)steps * u->G0)) : 0.0f;
+    // the weights changed: the solver's captured graph holds the repacked
+    // buffers by address, which stay the same, so it remains valid
+    return NN_OK;
+}
+
+extern "C" nn_status nn_lmg_use_network(nn_lmg* lm, int enable)
+{
+    if (!lm) return NN_ERR_INVALID_ARG;
+    lm->use_net = enable != 0;
+    return lmg_apply_mode(lm);
+}
+
+extern "C" nn_status nn_lmg_pairs(nn_lmg* lm, int* n)
+{
+    if (!lm || !n) return NN_ERR_INVALID_ARG;
+    *n = (int)lm->pair_b.size();
+    return NN_OK;
+}
+
+extern "C" nn_status nn_lmg_solve(nn_lmg* lm, const float* d_b, float* d_x, double rtol, int max_iter, int* iters,
+                                  double* relres)
+{
+    if (!lm) return NN_ERR_INVALID_ARG;
+    NN_CUDA(lm->ctx, cudaMemsetAsync(lm->net->err, 0, sizeof(int), lm->ctx->stream));
+    const nn_status st = nn_mg_solve(lm->mg, d_b, d_x, rtol, max_iter, iters, relres);
+    const nn_status st2 = check_err(lm->net);
+    return st != NN_OK ? st : st2;
+}
