@@ -51,7 +51,7 @@ WORKLOADS = {
                # iterations of the FP64 oracle PCG to 1e-6 on this seeded instance
                # (oracle.pcg7 run to convergence once; the CPU arms time a bounded
                # number of iterations and scale by this count)
-               fp64_iters=329, train_rhs=6, train_steps=400, lmg_train_steps=1500),
+               fp64_iters=329, train_rhs=6, train_steps=400, lmg_train_steps=3000),
     "c1": dict(workload="hh_1k_er_p0.01_grid32", n=1000, kind="er", p=0.01, w_max=0.5, dmax=1, inh=0.2,
                i_lo=5.0, i_hi=15.0, grid=32, timescale=100, par_D=1.0, par_decay=0.0, total_steps=10000),
 }
