@@ -358,10 +358,26 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_list(const int* list,
         const int j = list[q];
         const int chn = is_inh[j] ? 1 : 0;
         const int64_t beg = row_ptr[j], end = row_ptr[j + 1];
-        for (int64_t e = beg + lane; e < end; e += 32) {
-            int sl = slot + (int)delay[e];
-            if (sl >= D) sl -= D;
-            atomicAdd(ring + 2 * ((size_t)sl * n_pad + col[e]) + chn, weight[e]);
+        // PUSH_UNROLL edges per lane loaded before their reductions
+        for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * PUSH_UNROLL) {
+            int tgt[PUSH_UNROLL], dl[PUSH_UNROLL];
+            float w[PUSH_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; ++u) {
+                const int64_t e = e0 + 32 * u;
+                if (e < end) {
+                    tgt[u] = col[e];
+                    w[u] = weight[e];
+                    dl[u] = delay[e];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < PUSH_UNROLL; ++u) {
+                if (e0 + 32 * u >= end) break;
+                int sl = slot + dl[u];
+                if (sl >= D) sl -= D;
+                atomicAdd(ring + 2 * ((size_t)sl * n_pad + tgt[u]) + chn, w[u]);
+            }
         }
     }
 }

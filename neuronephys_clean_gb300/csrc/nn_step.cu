@@ -155,8 +155,23 @@ __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
                 if (a.raster && rpos < (unsigned long long)a.rcap) a.raster[rpos] = make_int2((int)t, i0 + q);
                 ++rpos;
             }
-        // push delivery of this warp's spikes, all lanes over each out-edge list
+        // push delivery of this warp's spikes: every spiking lane loads its
+        // own rows' bounds and types at once, then all lanes scatter each
+        // spike's out-edges (nn_push_row)
         if (a.row_ptr) {
+            int64_t rb[NPT], re[NPT];
+            int rc[NPT];
+#pragma unroll
+            for (int q = 0; q < NPT; ++q) {
+                rb[q] = re[q] = 0;
+                rc[q] = 0;
+                if (mask & (1u << q)) {
+                    const int j = i0 + q;
+                    rb[q] = a.row_ptr[j];
+                    re[q] = a.row_ptr[j + 1];
+                    rc[q] = a.is_inh[j] ? 1 : 0;
+                }
+            }
             unsigned who = __ballot_sync(0xffffffffu, mask != 0);
             while (who) {
                 const int sl_lane = __ffs(who) - 1;
@@ -165,14 +180,10 @@ __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
 #pragma unroll
                 for (int q = 0; q < NPT; ++q) {
                     if (!(m & (1u << q))) continue;
-                    const int j = ch * chunk + sl_lane * NPT + q;
-                    const int chn = a.is_inh[j] ? 1 : 0;
-                    const int64_t beg = a.row_ptr[j], end = a.row_ptr[j + 1];
-                    for (int64_t e = beg + lane; e < end; e += 32) {
-                        int sl = slot + (int)a.delay[e];
-                        if (sl >= a.D) sl -= a.D;
-                        atomicAdd(a.ring + 2 * ((size_t)sl * a.n_pad + a.col[e]) + chn, a.weight[e]);
-                    }
+                    const int64_t beg = __shfl_sync(0xffffffffu, rb[q], sl_lane);
+                    const int64_t end = __shfl_sync(0xffffffffu, re[q], sl_lane);
+                    const int chn = __shfl_sync(0xffffffffu, rc[q], sl_lane);
+                    nn_push_row(a, beg, end, chn, slot, lane);
                 }
             }
         }

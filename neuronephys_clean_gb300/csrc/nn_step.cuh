@@ -63,5 +63,36 @@ __device__ __forceinline__ void vstore(float* base, int i0, const float (&in)[NP
     *reinterpret_cast<V*>(base + i0) = v;
 }
 
+// Scatter one spike's out-edges [beg, end) into the delay ring (all 32 lanes
+// of the warp): each lane loads PUSH_UNROLL edges (target, weight, delay)
+// before issuing their reductions, so a row of up to 32 * PUSH_UNROLL edges
+// costs one load round trip.  slot: the current step's ring slot; chn: 0
+// excitatory, 1 inhibitory.
+constexpr int PUSH_UNROLL = 4;
+
+__device__ __forceinline__ void nn_push_row(const StepArgs& a, int64_t beg, int64_t end, int chn, int slot, int lane)
+{
+    for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * PUSH_UNROLL) {
+        int tgt[PUSH_UNROLL], dl[PUSH_UNROLL];
+        float w[PUSH_UNROLL];
+#pragma unroll
+        for (int u = 0; u < PUSH_UNROLL; ++u) {
+            const int64_t e = e0 + 32 * u;
+            if (e < end) {
+                tgt[u] = a.col[e];
+                w[u] = a.weight[e];
+                dl[u] = a.delay[e];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < PUSH_UNROLL; ++u) {
+            if (e0 + 32 * u >= end) break;
+            int sl = slot + dl[u];
+            if (sl >= a.D) sl -= a.D;
+            atomicAdd(a.ring + 2 * ((size_t)sl * a.n_pad + tgt[u]) + chn, w[u]);
+        }
+    }
+}
+
 // One step of every neuron on stream cs (NPT neurons per thread: 1, 2 or 4).
 cudaError_t nn_launch_hh_step(const StepArgs& a, int npt, int blocks, int tpb, cudaStream_t cs);
