@@ -360,8 +360,10 @@ def cpu_baseline(sim, wl: dict, args) -> dict:
 def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | None:
     """Spike delivery alone on the workload's network at firing fractions
     1e-4 .. 3e-1 of the neurons per step: push scatter (13 B per synaptic
-    event) and pull CSC gather (9 B per synapse + 8 B ring write per neuron),
-    CUDA-event timed, achieved algorithmic GB/s against the measured HBM peak."""
+    event) and pull gather (the chunked layout: one 4-byte entry word per
+    synapse, the weights of the synapses whose source fired, 8 B ring write
+    per neuron), CUDA-event timed, achieved algorithmic GB/s against the
+    measured HBM peak."""
     if rank != 0:
         return None
     import neuronephys_clean_gb300 as nn
@@ -397,24 +399,28 @@ def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | Non
             if mode == nn.NN_DELIVERY_PUSH:
                 nbytes = events * PUSH_BYTES_PER_EVENT
             elif sliced:
-                # entry words and column offsets + weights of arriving synapses
-                # + ring slot written + the D - 1 bitmap rows staged
-                nbytes = nnz * 6 + hits * 4 + n * 8 + dmax * (n // 8)
+                # entry words + weights of arriving synapses + ring slot
+                # written + the D - 1 bitmap rows read
+                nbytes = nnz * 4 + hits * 4 + n * 8 + dmax * (n // 8)
             else:
                 nbytes = nnz * PULL_CSC_BYTES_PER_SYNAPSE + n * 8 + n // 8
             res[name] = {"ms": ms, "GBs": nbytes / (ms * 1e-3) / 1e9, "frac_of_peak": nbytes / (ms * 1e-3) / 1e9 / hbm_peak}
             if mode == nn.NN_DELIVERY_PULL:
                 csc = nnz * PULL_CSC_BYTES_PER_SYNAPSE + n * 8 + n // 8
                 res[name]["bytes"] = nbytes
-                res[name]["GBs_csc_basis"] = csc / (ms * 1e-3) / 1e9
+                # the rate at which a sweep over the 9-byte CSC entries would
+                # have to run to finish in the same time
+                res[name]["GBs_csc9_equivalent"] = csc / (ms * 1e-3) / 1e9
+                res[name]["synapses_per_s"] = nnz / (ms * 1e-3)
         rows.append(res)
     cross = next((r["fraction"] for r in rows if r["pull"]["ms"] < r["push"]["ms"]), None)
     sim.close()
     ctx.close()
     return {"metric": "spike delivery GB/s vs firing fraction", "workload": wl["workload"], "neurons": n,
             "synapses": nnz, "peak_GBs": hbm_peak, "peak_source": peak_kind,
-            "pull_kernel": (f"k_deliver_pull_sliced (shared-memory bitmap, {cols} columns per block; bytes: 6 per "
-                            "synapse + 4 per arriving synapse + 8 per neuron + the bitmap rows)")
+            "pull_kernel": (f"k_deliver_pull_sliced (chunked entries and bitmap ranges staged by bulk copies, "
+                            f"{cols} columns per block; bytes: 4 per synapse + 4 per arriving synapse + 8 per "
+                            "neuron + the bitmap rows)")
             if sliced else "k_deliver_pull (warp per column; bytes: the 9-byte CSC entry per synapse)",
             "sweep": rows,
             "push_pull_crossover_fraction": cross}

@@ -22,6 +22,13 @@ __device__ __forceinline__ void nn_mbar_expect_tx(uint64_t* bar, uint32_t bytes)
                  : "memory");
 }
 
+// One arrival (release semantics: this thread's earlier shared-memory reads
+// are ordered before the phase it helps complete).
+__device__ __forceinline__ void nn_mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(nn_smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool nn_mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit)
 {
     const uint32_t addr = nn_smem_u32(bar);

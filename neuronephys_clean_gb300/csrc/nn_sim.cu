@@ -22,6 +22,7 @@
 
 #include "nn_hh.cuh"
 #include "nn_internal.cuh"
+#include "nn_ptx.cuh"
 #include "nn_step.cuh"
 
 struct nn_pcg;
@@ -55,14 +56,18 @@ struct nn_sim {
     uint32_t* csc_src = nullptr;   // source | inhibitory << 31
     float* csc_w = nullptr;
     uint8_t* csc_d = nullptr;
-    // delay-sliced CSC (pull delivery through shared memory; null when the
-    // network does not qualify): entries ordered by (delay, column, CSC order),
-    // dsl_cp[(d - 1) * n + k] = first entry of column k with delay d
-    int32_t* dsl_cp = nullptr;
-    uint32_t* dsl_src = nullptr;
-    float* dsl_w = nullptr;
-    uint16_t* dsl_col = nullptr;   // column of each entry, relative to its block's first column
+    // chunked CSC of the shared-memory pull (null when the network does not
+    // qualify): entries ordered by (column block, delay, source bucket), cut
+    // into chunks (see k_deliver_pull_sliced)
+    int4* dsl_chunk = nullptr;     // {first entry, end entry, first bitmap word, words << 8 | delay}
+    int32_t* dsl_cptr = nullptr;   // [block][j]: first chunk of the block with delay > j (j = 0: first chunk)
+    uint32_t* dsl_ent = nullptr;   // entry words, chunk by chunk (each padded to a multiple of four)
+    float* dsl_w = nullptr;        // their weights
     int dsl_cols = 0;              // columns per block of the sliced pull kernel
+    int dsl_ring = 0;              // bitmap slots in shared memory
+    int dsl_slotw = 0;             // words per slot
+    int dsl_cmax = 0;              // most chunks of one block
+    int dsl_dmax = 0;              // longest delay of the layout
     // paracrine
     int grid = 0;
     int64_t G = 0;
@@ -125,11 +130,12 @@ struct PullArgs {
     const unsigned long long* base;
     int q;
     int n, n_pad, D, words;
-    const int32_t* dsl_cp;
-    const uint32_t* dsl_src;
+    const int4* dsl_chunk;
+    const int32_t* dsl_cptr;
+    const uint32_t* dsl_ent;
     const float* dsl_w;
-    const uint16_t* dsl_col;
-    int dsl_cols;
+    int dsl_cols, dsl_ring, dsl_slotw, dsl_cmax, dsl_dmax;
+    int* err;
 };
 
 // Pull: a warp per postsynaptic neuron sums its CSC column against the spike
@@ -188,103 +194,228 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
 }
 
 // Pull through shared memory.  A block owns dsl_cols consecutive columns
-// (postsynaptic neurons).  For each delay d = 1 .. D-1 it copies the spike
-// bitmap of step t + 1 - d (n_pad bits) into shared memory; its entries of
-// that delay are one contiguous range of the slice, which the block's threads
-// walk flat, four entries per 16-byte load (plus their 2-byte column
-// offsets), testing each source bit in shared memory and reading a weight only
-// where it is set.  Sums accumulate in shared memory as 64-bit fixed point
-// (weight x 2^32; integer addition does not depend on order, so the result is
-// deterministic, and exact for weights >= 2^-8).  While the block works on
-// delay d, one thread asks the bulk-copy engine to prefetch the range of
-// delay d + 1 into L2.  DRAM traffic per step: 6 B per synapse (entry word
-// and column offset), the weights of the sources that fired, the ring slot
-// written (8 B per neuron).
-constexpr int DSL_THREADS = 1024;
-constexpr int DSL_GROUPS = 3;  // groups of four entries a thread loads before testing them (2-6 measured alike)
+// (postsynaptic neurons).  Its synapses are stored as one run per block,
+// ordered by delay and, within a delay, by source bucket (DSL_BUCKET_WORDS
+// bitmap words = 16,384 consecutive source neurons), and cut into chunks of
+// at most DSL_CHUNK entries that span at most DSL_SPAN buckets.  An entry is
+// one 32-bit word: the source's offset from the chunk's first bucket (17
+// bits), the column offset within the block (14 bits) and the inhibitory bit.
+// A chunk of delay d needs only its buckets' words of the spike bitmap of step
+// t + 1 - d; two bulk copies stage those words (from L2) and the chunk's
+// entries (from DRAM) into one of dsl_ring shared-memory slots, completing on
+// the slot's "full" mbarrier.  Every consumer thread tests DSL_EPT entries of
+// each chunk (16-byte reads; a warp reads consecutive words) against the
+// staged bitmap, all lookups before any use.  Hits go to a per-warp queue of
+// (entry, word) pairs in shared memory; a warp empties its queue when it could
+// overflow and at the end, every lane loading all its weights before it adds
+// any.  A warp done with a chunk arrives on the slot's "empty" mbarrier; one
+// producer warp waits for it and refills the slot with the chunk dsl_ring
+// places later.  Consumer warps drift apart by up to dsl_ring - 1 chunks, and
+// no block-wide barrier separates the delays.  Sums accumulate in
+// shared memory as 64-bit fixed point (weight x 2^32; integer addition does
+// not depend on order, so the result is deterministic, and exact for weights
+// >= 2^-8).  DRAM traffic per step: 4 B per synapse, the weights of the
+// sources that fired, the ring slot written (8 B per neuron); the bitmap words
+// come from L2.
+// Every wait is bounded: a thread that gives up sets error bit 2 and the
+// block's abort flag; the block then waits (bounded) for its copies in flight
+// and leaves without writing its columns.
+constexpr int DSL_THREADS = 512;                  // consumer threads (plus one producer warp)
+constexpr int DSL_WARPS = DSL_THREADS / 32;
+constexpr int DSL_EPT = 8;                        // entries per consumer thread and chunk
+constexpr int DSL_CHUNK = DSL_EPT * DSL_THREADS;  // entries per chunk at most
+constexpr int DSL_BUCKET_WORDS = 512;             // bitmap words per source bucket
+constexpr int DSL_SPAN = 8;                       // buckets per chunk at most: source offsets below 2^17
+constexpr int DSL_MAX_RING = 6;                   // slots at most
+constexpr int DSL_HITCAP = 128;                   // hits a warp's queue holds
+constexpr int DSL_MAX_COLS = 16384;               // 14-bit column offsets
 constexpr int DSL_MAX_DELAY = 64;
-constexpr int DSL_PAD = 8;  // slack entries after the slice arrays (16-byte load / prefetch rounding)
 constexpr double DSL_FIX = 4294967296.0;  // 2^32
+constexpr uint32_t DSL_WAIT_LIMIT = 1u << 22;
+static_assert(DSL_SPAN * DSL_BUCKET_WORDS * 32 <= (1 << 17), "source offsets take 17 bits");
 
-// L2 prefetch of [p, p + bytes) rounded out to 16 bytes, in pieces of at most
-// 64 KB (cp.async.bulk.prefetch.L2: 16-byte aligned address and size)
-__device__ __forceinline__ void dsl_prefetch(const void* p, size_t bytes)
+// Stage chunk m = {first entry, entries, first word, words << 8 | delay}: its
+// bitmap words of the row of step t + 1 - d, then its entries (a multiple of
+// four words; the layout pads every chunk).
+__device__ __forceinline__ void dsl_issue(const PullArgs& a, int s1, int4 m, uint32_t* dst, uint64_t* bar)
 {
-    uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)15;
-    const uintptr_t e = (reinterpret_cast<uintptr_t>(p) + bytes + 15) & ~(uintptr_t)15;
-    while (a < e) {
-        const uint32_t n = (uint32_t)((e - a) < (uintptr_t)65536 ? (e - a) : (uintptr_t)65536);
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
-        a += n;
+    int hs = s1 - (m.w & 255);
+    if (hs < 0) hs += a.D;
+    const uint32_t bw = (uint32_t)(m.w >> 8) * 4u;
+    const uint32_t be = (uint32_t)((m.y + 3) & ~3) * 4u;
+    nn_mbar_expect_tx(bar, bw + be);
+    nn_bulk_g2s(dst, a.bitmap + (size_t)hs * a.words + m.z, bw, bar);
+    nn_bulk_g2s(dst + a.dsl_slotw, a.dsl_ent + m.x, be, bar);
+}
+
+// Add a warp's queued hits {entry, word}: each lane loads its weights, then
+// adds them to the columns' sums.
+__device__ __forceinline__ void dsl_drain(const uint2* q, int cnt, int lane, const float* w,
+                                          unsigned long long* acc_e, unsigned long long* acc_i)
+{
+    constexpr int PER = DSL_HITCAP / 32;
+    uint32_t ew[PER];
+    float wv[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int i = lane + 32 * k;
+        ew[k] = 0u;
+        wv[k] = 0.0f;
+        if (i < cnt) {
+            const uint2 h = q[i];
+            ew[k] = h.y;
+            wv[k] = w[h.x];
+        }
     }
+#pragma unroll
+    for (int k = 0; k < PER; ++k)
+        if (lane + 32 * k < cnt) {
+            const uint32_t col = (ew[k] >> 17) & 0x3fffu;
+            atomicAdd(((ew[k] >> 31) ? acc_i : acc_e) + col, (unsigned long long)llrintf(wv[k] * (float)DSL_FIX));
+        }
 }
 
-__device__ __forceinline__ void dsl_take(const uint32_t* bm, uint32_t sw, int e, int e0, int e1, uint32_t col,
-                                         const float* w, unsigned long long* acc_e, unsigned long long* acc_i)
+__global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(PullArgs a)
 {
-    if (e < e0 || e >= e1) return;
-    const uint32_t sid = sw & 0x7fffffffu;
-    if (!((bm[sid >> 5] >> (sid & 31)) & 1u)) return;
-    const unsigned long long v = (unsigned long long)llrintf(w[e] * (float)DSL_FIX);
-    atomicAdd((sw >> 31) ? acc_i + col : acc_e + col, v);
-}
-
-__global__ void __launch_bounds__(DSL_THREADS, 1) k_deliver_pull_sliced(PullArgs a)
-{
-    extern __shared__ uint4 dsl_smem[];
-    const uint32_t* bm = reinterpret_cast<const uint32_t*>(dsl_smem);
-    unsigned long long* acc_e = reinterpret_cast<unsigned long long*>(dsl_smem + a.words / 4);
+    extern __shared__ __align__(128) unsigned char dsl_smem[];
+    const int R = a.dsl_ring, SW = a.dsl_slotw, SL = a.dsl_slotw + DSL_CHUNK;  // slot: bitmap words, entries
+    uint32_t* ring = reinterpret_cast<uint32_t*>(dsl_smem);
+    unsigned long long* acc_e = reinterpret_cast<unsigned long long*>(ring + (size_t)R * SL);
     unsigned long long* acc_i = acc_e + a.dsl_cols;
+    uint2* hitq = reinterpret_cast<uint2*>(acc_i + a.dsl_cols);  // [DSL_WARPS][DSL_HITCAP]
+    int4* tab = reinterpret_cast<int4*>(hitq + DSL_WARPS * DSL_HITCAP);
+    uint64_t* full = reinterpret_cast<uint64_t*>(tab + a.dsl_cmax);
+    uint64_t* empty = full + R;
+    int* last = reinterpret_cast<int*>(empty + R);  // last chunk issued into a slot
+    __shared__ volatile int abort_flag;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t t1 = *a.base + (uint64_t)a.q + 1;
     const int s1 = (int)(t1 % (uint64_t)a.D);
     const int k0 = blockIdx.x * a.dsl_cols;
     const int k1 = min(a.n, k0 + a.dsl_cols);
-    const int dlast = t1 < (uint64_t)(a.D - 1) ? (int)t1 : a.D - 1;  // delays beyond t + 1 reach before step 0
-    for (int k = threadIdx.x; k < a.dsl_cols; k += blockDim.x) acc_e[k] = acc_i[k] = 0ull;
-    const int w4 = a.words / 4;
-    if (threadIdx.x == 0 && dlast >= 1)
-        dsl_prefetch(a.dsl_src + a.dsl_cp[k0], sizeof(uint32_t) * (size_t)(a.dsl_cp[k1] - a.dsl_cp[k0]));
-    for (int d = 1; d <= dlast; ++d) {
-        int hs = s1 - d;
-        if (hs < 0) hs += a.D;
-        const uint4* src4 = reinterpret_cast<const uint4*>(a.bitmap + (size_t)hs * a.words);
-        __syncthreads();  // the previous delay's lookups are done
-        for (int w = threadIdx.x; w < w4; w += blockDim.x) dsl_smem[w] = src4[w];
-        if (threadIdx.x == 0 && d < dlast) {
-            const int32_t* cpn = a.dsl_cp + (size_t)d * a.n;
-            dsl_prefetch(a.dsl_src + cpn[k0], sizeof(uint32_t) * (size_t)(cpn[k1] - cpn[k0]));
-            dsl_prefetch(a.dsl_col + cpn[k0], sizeof(uint16_t) * (size_t)(cpn[k1] - cpn[k0]));
+    // delays beyond t + 1 reach before step 0
+    const int dlast = min(t1 < (uint64_t)(a.D - 1) ? (int)t1 : a.D - 1, a.dsl_dmax);
+    const int32_t* cp = a.dsl_cptr + (size_t)blockIdx.x * (a.dsl_dmax + 1);
+    const int cfirst = cp[0];
+    const int C = dlast >= 1 ? cp[dlast] - cfirst : 0;
+    for (int k = tid; k < a.dsl_cols; k += blockDim.x) acc_e[k] = acc_i[k] = 0ull;
+    for (int c = tid; c < C; c += blockDim.x) tab[c] = a.dsl_chunk[cfirst + c];
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int r = 0; r < R; ++r) {
+            nn_mbar_init(&full[r], 1);
+            nn_mbar_init(&empty[r], DSL_WARPS);
+            last[r] = -1;
         }
-        __syncthreads();
-        const int32_t* cp = a.dsl_cp + (size_t)(d - 1) * a.n;
-        const int e0 = cp[k0], e1 = cp[k1];
-        const int stride = 4 * blockDim.x;
-        // DSL_GROUPS groups of four entries per thread in flight
-        for (int e = (e0 & ~3) + 4 * threadIdx.x; e < e1; e += DSL_GROUPS * stride) {
-            uint4 sv[DSL_GROUPS];
-            uint2 cv[DSL_GROUPS];
+        nn_mbar_fence_init();
+    }
+    __syncthreads();
+    if (warp == DSL_WARPS) {
+        // producer: the first dsl_ring chunks, then chunk c once every
+        // consumer warp is done with chunk c - dsl_ring
+        if (lane == 0)
+            for (int c = 0; c < C; ++c) {
+                const int slot = c % R;
+                if (c >= R) {
+                    if (!nn_mbar_wait(&empty[slot], (uint32_t)((c / R - 1) & 1), DSL_WAIT_LIMIT)) {
+                        abort_flag = 1;
+                        break;
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                }
+                last[slot] = c;
+                dsl_issue(a, s1, tab[c], ring + (size_t)slot * SL, &full[slot]);
+            }
+    } else {
+        uint2* hq = hitq + warp * DSL_HITCAP;
+        int hcnt = 0;  // hits in this warp's queue (the same in every lane)
+        int slot = 0;
+        uint32_t phase = 0;
+        for (int c = 0; c < C; ++c) {
+            // (another warp's abort shows up here as a wait that runs out)
+            const bool landed = __all_sync(0xffffffffu, nn_mbar_wait(&full[slot], phase, DSL_WAIT_LIMIT));
+            if (!landed) {
+                abort_flag = 1;
+                break;
+            }
+            const int4 m = tab[c];
+            const uint32_t* bm = ring + (size_t)slot * SL;
+            const uint4* ent = reinterpret_cast<const uint4*>(bm + SW);
+            uint32_t ew[DSL_EPT];
 #pragma unroll
-            for (int g = 0; g < DSL_GROUPS; ++g) {
-                const int f = e + g * stride;
-                if (f < e1) {
-                    sv[g] = *reinterpret_cast<const uint4*>(a.dsl_src + f);
-                    cv[g] = *reinterpret_cast<const uint2*>(a.dsl_col + f);
+            for (int g = 0; g < DSL_EPT / 4; ++g) {
+                const uint4 v = ent[tid + DSL_THREADS * g];
+                ew[4 * g] = v.x;
+                ew[4 * g + 1] = v.y;
+                ew[4 * g + 2] = v.z;
+                ew[4 * g + 3] = v.w;
+            }
+            // entry q of this thread: 4 (tid + DSL_THREADS (q / 4)) + q % 4.
+            // Its source bit: word (offset >> 5) of the staged range, bit
+            // (offset & 31) -- the low five bits of the entry word -- rotated
+            // into bit q of hit.  In a partial chunk, words past its end
+            // (padding, or left from an earlier chunk) are looked up at word 0
+            // and masked.
+            uint32_t hit = 0;
+            if (m.y == DSL_CHUNK) {
+#pragma unroll
+                for (int q = 0; q < DSL_EPT; ++q) {
+                    const uint32_t wv = bm[(ew[q] >> 5) & 0xfffu];
+                    hit |= __funnelshift_r(wv, wv, ew[q] - (uint32_t)q) & (1u << q);
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < DSL_EPT; ++q) {
+                    const int i = 4 * (tid + DSL_THREADS * (q / 4)) + (q % 4);
+                    const bool in = i < m.y;
+                    const uint32_t e = in ? ew[q] : 0u;
+                    const uint32_t wv = bm[(e >> 5) & 0xfffu];
+                    hit |= __funnelshift_r(wv, wv, e - (uint32_t)q) & (in ? (1u << q) : 0u);
                 }
             }
+            // the slot's words are all read: release it to the producer
+            __syncwarp();
+            if (lane == 0) nn_mbar_arrive(&empty[slot]);
+            if (__any_sync(0xffffffffu, hit != 0)) {
 #pragma unroll
-            for (int g = 0; g < DSL_GROUPS; ++g) {
-                const int f = e + g * stride;
-                if (f >= e1) break;
-                dsl_take(bm, sv[g].x, f, e0, e1, cv[g].x & 0xffffu, a.dsl_w, acc_e, acc_i);
-                dsl_take(bm, sv[g].y, f + 1, e0, e1, cv[g].x >> 16, a.dsl_w, acc_e, acc_i);
-                dsl_take(bm, sv[g].z, f + 2, e0, e1, cv[g].y & 0xffffu, a.dsl_w, acc_e, acc_i);
-                dsl_take(bm, sv[g].w, f + 3, e0, e1, cv[g].y >> 16, a.dsl_w, acc_e, acc_i);
+                for (int q = 0; q < DSL_EPT; ++q) {
+                    const bool h = (hit >> q) & 1u;
+                    const unsigned b = __ballot_sync(0xffffffffu, h);
+                    if (!b) continue;
+                    if (hcnt + __popc(b) > DSL_HITCAP) {
+                        __syncwarp();
+                        dsl_drain(hq, hcnt, lane, a.dsl_w, acc_e, acc_i);
+                        __syncwarp();
+                        hcnt = 0;
+                    }
+                    if (h) {
+                        const int i = 4 * (tid + DSL_THREADS * (q / 4)) + (q % 4);
+                        hq[hcnt + __popc(b & ((1u << lane) - 1u))] = make_uint2((uint32_t)(m.x + i), ew[q]);
+                    }
+                    hcnt += __popc(b);
+                }
             }
+            if (++slot == R) {
+                slot = 0;
+                phase ^= 1u;
+            }
+        }
+        if (!abort_flag && hcnt > 0) {
+            __syncwarp();
+            dsl_drain(hq, hcnt, lane, a.dsl_w, acc_e, acc_i);
         }
     }
     __syncthreads();
+    if (abort_flag) {
+        if (tid == 0) {
+            atomicOr(a.err, 2);
+            for (int r = 0; r < R; ++r)
+                if (last[r] >= 0) nn_mbar_wait(&full[r], (uint32_t)((last[r] / R) & 1), DSL_WAIT_LIMIT);
+        }
+        return;
+    }
     float2* out = reinterpret_cast<float2*>(a.ring + (size_t)(t1 % (uint64_t)a.D) * a.n_pad * 2);
-    for (int k = threadIdx.x; k < k1 - k0; k += blockDim.x)
+    for (int k = tid; k < k1 - k0; k += blockDim.x)
         out[k0 + k] = make_float2((float)((double)(long long)acc_e[k] / DSL_FIX),
                                   (float)((double)(long long)acc_i[k] / DSL_FIX));
 }
@@ -301,41 +432,66 @@ __global__ void k_dsl_bounds(const int64_t* col_ptr, const float* csc_w, int n, 
     atomicMax(out + 1, wmax);  // non-negative floats order like their bit patterns
 }
 
-// Delay-sliced layout: per column, entries counted per delay (a thread owns
-// a column, so no atomics) ...
+// Chunked layout.  Entries counted per (column block, delay, source bucket), a
+// thread per column ...
 // (delays outside [1, dmax] cannot occur -- the network setters check them --
 // and would be left out of both passes alike)
-__global__ void k_dsl_count(const int64_t* col_ptr, const uint8_t* csc_d, int n, int dmax, int64_t* cnt)
+__device__ __forceinline__ size_t dsl_key(int k, int cols, int dmax, int nb, int d, uint32_t sw)
+{
+    const int bucket = (int)((sw & 0x7fffffffu) >> 5) / DSL_BUCKET_WORDS;
+    return ((size_t)(k / cols) * dmax + (d - 1)) * nb + bucket;
+}
+
+__global__ void k_dsl_count(const int64_t* col_ptr, const uint32_t* csc_src, const uint8_t* csc_d, int n, int cols,
+                            int dmax, int nb, unsigned int* cnt)
 {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
         for (int64_t e = col_ptr[k]; e < col_ptr[k + 1]; ++e) {
             const int d = csc_d[e];
-            if (d >= 1 && d <= dmax) cnt[(size_t)(d - 1) * n + k] += 1;
+            if (d >= 1 && d <= dmax) atomicAdd(&cnt[dsl_key(k, cols, dmax, nb, d, csc_src[e])], 1u);
         }
 }
 
-// ... offsets narrowed to 32 bits ...
-__global__ void k_dsl_narrow(const int64_t* off, int64_t count, int32_t* out)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = (int32_t)off[i];
-}
-
-// ... and each column's entries placed in CSC order within every delay slice.
+// ... placed at their bucket's cursor (first entry of the bucket, from the
+// host's scan of the counts; the order inside a bucket is the order of the
+// atomics and may differ between builds -- the fixed-point sums do not depend
+// on it) ...
 __global__ void k_dsl_fill(const int64_t* col_ptr, const uint32_t* csc_src, const float* csc_w, const uint8_t* csc_d,
-                           int n, int dmax, int cols, const int32_t* cp, uint32_t* out_src, float* out_w,
+                           int n, int cols, int dmax, int nb, unsigned int* cursor, uint32_t* out_src, float* out_w,
                            uint16_t* out_col)
 {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        int pos[DSL_MAX_DELAY];
-        for (int d = 0; d < dmax; ++d) pos[d] = cp[(size_t)d * n + k];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
         for (int64_t e = col_ptr[k]; e < col_ptr[k + 1]; ++e) {
             const int d = csc_d[e];
             if (d < 1 || d > dmax) continue;
-            const int q = pos[d - 1]++;
-            out_src[q] = csc_src[e];
+            const uint32_t sw = csc_src[e];
+            const unsigned int q = atomicAdd(&cursor[dsl_key(k, cols, dmax, nb, d, sw)], 1u);
+            out_src[q] = sw;
             out_w[q] = csc_w[e];
             out_col[q] = (uint16_t)(k % cols);
+        }
+}
+
+// ... and packed chunk by chunk into entry words (each chunk padded with
+// zero entries to a multiple of four); ustart: the chunk's first entry in the
+// bucketed arrays.
+__global__ void k_dsl_pack(const int4* chunk, const int32_t* ustart, int nchunks, const uint32_t* src,
+                           const uint16_t* col, const float* w, uint32_t* ent, float* wout)
+{
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int4 m = chunk[c];
+        const int us = ustart[c];
+        const int padded = (m.y + 3) & ~3;
+        for (int i = threadIdx.x; i < padded; i += blockDim.x) {
+            uint32_t word = 0u;
+            float wv = 0.0f;
+            if (i < m.y) {
+                const uint32_t sw = src[us + i];
+                word = ((sw & 0x7fffffffu) - (uint32_t)m.z * 32u) | ((uint32_t)col[us + i] << 17) | (sw & 0x80000000u);
+                wv = w[us + i];
+            }
+            ent[m.x + i] = word;
+            wout[m.x + i] = wv;
         }
     }
 }
@@ -803,20 +959,33 @@ static PullArgs pull_args(nn_sim* s, int q)
     a.base = s->step;
     a.q = q;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
-    a.dsl_cp = s->dsl_cp; a.dsl_src = s->dsl_src; a.dsl_w = s->dsl_w; a.dsl_col = s->dsl_col;
-    a.dsl_cols = s->dsl_cols;
+    a.dsl_chunk = s->dsl_chunk; a.dsl_cptr = s->dsl_cptr;
+    a.dsl_ent = s->dsl_ent; a.dsl_w = s->dsl_w;
+    a.dsl_cols = s->dsl_cols; a.dsl_ring = s->dsl_ring; a.dsl_slotw = s->dsl_slotw;
+    a.dsl_cmax = s->dsl_cmax; a.dsl_dmax = s->dsl_dmax;
+    a.err = s->err;
     return a;
 }
 
-// The pull gather of one step: through shared memory when the delay-sliced
-// layout exists, else the warp-per-column kernel.
+// Dynamic shared memory of k_deliver_pull_sliced: the slots (slotw bitmap
+// words and a chunk of entries each), two 64-bit sums per column, the warps'
+// hit queues, the block's chunk table, and per slot two mbarriers (full,
+// empty) and the last chunk issued.
+static size_t dsl_smem_bytes(int ring, int slotw, int cols, int cmax)
+{
+    return (size_t)ring * (slotw + DSL_CHUNK) * 4 + (size_t)cols * 16 + (size_t)DSL_WARPS * DSL_HITCAP * 8 +
+           (size_t)cmax * 16 + (size_t)ring * 20;
+}
+
+// The pull gather of one step: through shared memory when the chunked layout
+// exists, else the warp-per-column kernel.
 static nn_status launch_pull(nn_sim* s, const PullArgs& d, cudaStream_t cs)
 {
     nn_ctx* ctx = s->ctx;
-    if (s->dsl_cp) {
+    if (s->dsl_chunk) {
         const int blocks = (s->n + s->dsl_cols - 1) / s->dsl_cols;
-        const size_t smem = sizeof(uint32_t) * (size_t)s->words + 2 * sizeof(unsigned long long) * (size_t)s->dsl_cols;
-        k_deliver_pull_sliced<<<blocks, DSL_THREADS, smem, cs>>>(d);
+        k_deliver_pull_sliced<<<blocks, DSL_THREADS + 32,
+                                dsl_smem_bytes(s->dsl_ring, s->dsl_slotw, s->dsl_cols, s->dsl_cmax), cs>>>(d);
         NN_CHECK_LAUNCH(ctx, "k_deliver_pull_sliced");
         return NN_OK;
     }
@@ -919,7 +1088,7 @@ static void free_network(nn_sim* s)
 {
     nn_release(s->row_ptr); nn_release(s->col); nn_release(s->weight); nn_release(s->delay);
     nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
-    nn_release(s->dsl_cp); nn_release(s->dsl_src); nn_release(s->dsl_w); nn_release(s->dsl_col);
+    nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w);
     s->nnz = 0;
 }
 
@@ -949,12 +1118,15 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     return NN_OK;
 }
 
-// Delay-sliced copy of the CSC for the shared-memory pull kernel, built when
-// one bitmap row and two 64-bit accumulators per column of a block fit in a
-// block's shared memory, delays stay within DSL_MAX_DELAY, entry offsets
-// within 32 bits and the fixed-point sums below 2^31 (longest column x
-// largest |weight|).  NN_PULL_UNSLICED=1 keeps the warp-per-column kernel
-// (for comparisons).
+// Chunked copy of the CSC for the shared-memory pull kernel (see
+// k_deliver_pull_sliced), built when the block's sums, chunk table and at
+// least two slots fit in a block's shared memory, a block has at most
+// DSL_MAX_COLS columns, delays stay within DSL_MAX_DELAY, entry offsets within
+// 32 bits and the fixed-point sums below 2^31 (longest column x largest
+// |weight|).  The host cuts each (block, delay) run into chunks from the
+// bucket counts; the entries are first placed by bucket, then packed chunk by
+// chunk.  NN_PULL_UNSLICED=1 keeps the warp-per-column kernel (for
+// comparisons).
 static nn_status build_sliced(nn_sim* s)
 {
     nn_ctx* ctx = s->ctx;
@@ -963,11 +1135,12 @@ static nn_status build_sliced(nn_sim* s)
     int smem_max = 0;
     NN_CUDA(ctx, cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
     const int cols = (s->n + ctx->num_sms - 1) / ctx->num_sms;
-    // bitmap row + two 64-bit accumulators per column
-    const size_t smem = sizeof(uint32_t) * (size_t)s->words + 2 * sizeof(unsigned long long) * (size_t)cols;
+    const int nblk = (s->n + cols - 1) / cols;
     const int dmax = s->D - 1;
-    if (s->nnz <= 0 || smem > (size_t)smem_max || cols > 65536 || dmax > DSL_MAX_DELAY ||
-        s->nnz >= INT32_MAX - DSL_PAD || (s->words % 4))
+    const int nb = (s->words + DSL_BUCKET_WORDS - 1) / DSL_BUCKET_WORDS;
+    const int slotw = std::min(s->words, DSL_SPAN * DSL_BUCKET_WORDS);
+    if (s->nnz <= 0 || dsl_smem_bytes(2, slotw, cols, 0) > (size_t)smem_max || cols > DSL_MAX_COLS || dmax < 1 ||
+        dmax > DSL_MAX_DELAY || s->nnz >= INT32_MAX / 2 || (s->words % 4))
         return NN_OK;
     // fixed-point range: |sum| <= longest column x largest |weight| < 2^31
     unsigned int* bnd = nullptr;
@@ -982,47 +1155,130 @@ static nn_status build_sliced(nn_sim* s)
     float wmax;
     std::memcpy(&wmax, &hb[1], sizeof wmax);
     if (!(std::isfinite(wmax)) || (double)hb[0] * (double)wmax >= 2147483648.0) return NN_OK;
-    const size_t slots = (size_t)dmax * s->n + 1;
-    int64_t *cnt = nullptr, *off = nullptr;
-    nn_status st = nn_alloc(ctx, &cnt, slots);
-    if (st == NN_OK) st = nn_alloc(ctx, &off, slots);
-    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_cp, slots + DSL_PAD);
-    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_src, (size_t)s->nnz + DSL_PAD);
-    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_col, (size_t)s->nnz + DSL_PAD);
-    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_w, (size_t)s->nnz);
-    if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, cnt, sizeof(int64_t) * slots), "build_sliced");
-    if (st == NN_OK)
-        st = nn_cuda_check(ctx, nn_zero_async(ctx, s->dsl_src + s->nnz, sizeof(uint32_t) * DSL_PAD), "build_sliced");
-    if (st == NN_OK)
-        st = nn_cuda_check(ctx, nn_zero_async(ctx, s->dsl_col + s->nnz, sizeof(uint16_t) * DSL_PAD), "build_sliced");
+    // entries per (block, delay, bucket)
+    const size_t nkeys = (size_t)nblk * dmax * nb;
+    unsigned int* cnt = nullptr;
+    NN_TRY(nn_alloc(ctx, &cnt, nkeys));
+    std::vector<unsigned int> h(nkeys);
+    nn_status st = nn_cuda_check(ctx, nn_zero_async(ctx, cnt, sizeof(unsigned int) * nkeys), "build_sliced");
     if (st == NN_OK) {
-        k_dsl_count<<<nn_grid_for(ctx, s->n, 256, 8), 256, 0, ctx->stream>>>(s->col_ptr, s->csc_d, s->n, dmax, cnt);
+        k_dsl_count<<<nn_grid_for(ctx, s->n, 256, 8), 256, 0, ctx->stream>>>(s->col_ptr, s->csc_src, s->csc_d, s->n,
+                                                                            cols, dmax, nb, cnt);
         st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_count");
     }
-    if (st == NN_OK) st = nn_scan_exclusive_i64(ctx, cnt, off, (int64_t)slots);
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, h.data(), cnt, sizeof(unsigned int) * nkeys, cudaMemcpyDeviceToHost),
+                           "build_sliced");
+    // bucket offsets (block-major), chunks and their padded starts
+    std::vector<int4> chunks;         // {padded first entry, entries, first word, words << 8 | delay}
+    std::vector<int32_t> ustart;      // first entry in the bucketed arrays
+    std::vector<int32_t> cptr((size_t)nblk * (dmax + 1));
+    int cmax = 0;
+    int64_t pos = 0, ppos = 0;
     if (st == NN_OK) {
-        k_dsl_narrow<<<nn_grid_for(ctx, (int64_t)slots, 256, 8), 256, 0, ctx->stream>>>(off, (int64_t)slots,
-                                                                                          s->dsl_cp);
-        st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_narrow");
+        for (int b = 0; b < nblk; ++b) {
+            const size_t c_b = chunks.size();
+            cptr[(size_t)b * (dmax + 1)] = (int32_t)c_b;
+            for (int d = 1; d <= dmax; ++d) {
+                bool open = false;
+                int64_t start = 0;
+                int len = 0, b0 = 0, b1 = 0;
+                auto close = [&]() {
+                    const int w0 = b0 * DSL_BUCKET_WORDS;
+                    const int w1 = std::min((b1 + 1) * DSL_BUCKET_WORDS, s->words);
+                    chunks.push_back(make_int4((int)ppos, len, w0, ((w1 - w0) << 8) | d));
+                    ustart.push_back((int32_t)start);
+                    ppos += (len + 3) & ~3;
+                    open = false;
+                };
+                for (int bk = 0; bk < nb; ++bk) {
+                    const size_t key = ((size_t)b * dmax + (d - 1)) * nb + bk;
+                    int64_t left = h[key];
+                    h[key] = (unsigned int)pos;
+                    while (left > 0) {
+                        if (open && (len == DSL_CHUNK || bk - b0 >= DSL_SPAN)) close();
+                        if (!open) {
+                            open = true;
+                            start = pos;
+                            len = 0;
+                            b0 = bk;
+                        }
+                        const int take = (int)std::min<int64_t>(left, DSL_CHUNK - len);
+                        len += take;
+                        pos += take;
+                        left -= take;
+                        b1 = bk;
+                    }
+                }
+                if (open) close();
+                cptr[(size_t)b * (dmax + 1) + d] = (int32_t)chunks.size();
+            }
+            cmax = std::max(cmax, (int)(chunks.size() - c_b));
+        }
     }
+    // slots: as many as fit, up to DSL_MAX_RING (at least two)
+    int ring = DSL_MAX_RING;
+    while (ring >= 2 && dsl_smem_bytes(ring, slotw, cols, cmax) > (size_t)smem_max) --ring;
+    if (st != NN_OK || pos > s->nnz || ppos >= INT32_MAX || chunks.empty() || ring < 2) {
+        cudaFree(cnt);
+        return st;
+    }
+    // place by bucket into temporary arrays, then pack chunk by chunk
+    uint32_t* t_src = nullptr;
+    uint16_t* t_col = nullptr;
+    float* t_w = nullptr;
+    int32_t* d_ustart = nullptr;
+    const size_t E = (size_t)std::max<int64_t>(pos, 1);
+    st = nn_cuda_check(ctx, nn_copy_sync(ctx, cnt, h.data(), sizeof(unsigned int) * nkeys, cudaMemcpyHostToDevice),
+                       "build_sliced");
+    if (st == NN_OK) st = nn_alloc(ctx, &t_src, E);
+    if (st == NN_OK) st = nn_alloc(ctx, &t_col, E);
+    if (st == NN_OK) st = nn_alloc(ctx, &t_w, E);
+    if (st == NN_OK) st = nn_alloc(ctx, &d_ustart, ustart.size());
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_chunk, chunks.size());
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_cptr, cptr.size());
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_ent, (size_t)ppos);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_w, (size_t)ppos);
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, s->dsl_chunk, chunks.data(), sizeof(int4) * chunks.size(),
+                                             cudaMemcpyHostToDevice), "build_sliced");
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, s->dsl_cptr, cptr.data(), sizeof(int32_t) * cptr.size(),
+                                             cudaMemcpyHostToDevice), "build_sliced");
+    if (st == NN_OK)
+        st = nn_cuda_check(ctx, nn_copy_sync(ctx, d_ustart, ustart.data(), sizeof(int32_t) * ustart.size(),
+                                             cudaMemcpyHostToDevice), "build_sliced");
     if (st == NN_OK) {
         k_dsl_fill<<<nn_grid_for(ctx, s->n, 128, 8), 128, 0, ctx->stream>>>(
-            s->col_ptr, s->csc_src, s->csc_w, s->csc_d, s->n, dmax, cols, s->dsl_cp, s->dsl_src, s->dsl_w,
-            s->dsl_col);
+            s->col_ptr, s->csc_src, s->csc_w, s->csc_d, s->n, cols, dmax, nb, cnt, t_src, t_w, t_col);
         st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_fill");
     }
+    if (st == NN_OK) {
+        const int nc = (int)chunks.size();
+        k_dsl_pack<<<std::min(nc, ctx->num_sms * 16), 256, 0, ctx->stream>>>(s->dsl_chunk, d_ustart, nc, t_src, t_col,
+                                                                            t_w, s->dsl_ent, s->dsl_w);
+        st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_pack");
+    }
+    const size_t smem = dsl_smem_bytes(ring, slotw, cols, cmax);
     if (st == NN_OK)
         st = nn_cuda_check(ctx, cudaFuncSetAttribute(k_deliver_pull_sliced,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                            "cudaFuncSetAttribute");
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "build_sliced");
     cudaFree(cnt);
-    cudaFree(off);
+    cudaFree(t_src);
+    cudaFree(t_col);
+    cudaFree(t_w);
+    cudaFree(d_ustart);
     if (st != NN_OK) {
-        nn_release(s->dsl_cp); nn_release(s->dsl_src); nn_release(s->dsl_w); nn_release(s->dsl_col);
+        nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w);
         return st;
     }
     s->dsl_cols = cols;
+    s->dsl_ring = ring;
+    s->dsl_slotw = slotw;
+    s->dsl_cmax = cmax;
+    s->dsl_dmax = dmax;
     return NN_OK;
 }
 
@@ -1057,7 +1313,7 @@ static nn_status after_network(nn_sim* s)
 {
     drop_graph(s);
     nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
-    nn_release(s->dsl_cp); nn_release(s->dsl_src); nn_release(s->dsl_w); nn_release(s->dsl_col);
+    nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w);
     if (s->cfg.delivery == NN_DELIVERY_PULL) NN_TRY(build_csc(s));
     return NN_OK;
 }
@@ -1456,6 +1712,7 @@ static nn_status check_err(nn_sim* s)
     int e = 0;
     NN_CUDA(s->ctx, cudaMemcpyAsync(&e, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->ctx->stream));
     NN_CUDA(s->ctx, cudaStreamSynchronize(s->ctx->stream));
+    if (e & 2) return nn_fail(s->ctx, NN_ERR_TIMEOUT, "pull delivery: a bitmap-copy wait gave up");
     if (e) return nn_fail(s->ctx, NN_ERR_NUMERIC, "non-finite membrane potential detected");
     return NN_OK;
 }
@@ -1807,8 +2064,8 @@ extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
 extern "C" nn_status nn_sim_pull_info(nn_sim* s, int* sliced, int* cols)
 {
     if (!s || !sliced || !cols) return NN_ERR_INVALID_ARG;
-    *sliced = s->dsl_cp ? 1 : 0;
-    *cols = s->dsl_cp ? s->dsl_cols : 0;
+    *sliced = s->dsl_chunk ? 1 : 0;
+    *cols = s->dsl_chunk ? s->dsl_cols : 0;
     return NN_OK;
 }
 

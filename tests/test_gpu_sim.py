@@ -134,6 +134,36 @@ def test_sliced_pull_matches_warp_pull(ctx, monkeypatch):
     np.testing.assert_allclose(a[2], u[2], rtol=1e-4, atol=1e-5)
 
 
+def test_chunked_pull_many_buckets(ctx, monkeypatch):
+    """The chunked pull on a network whose (block, delay) runs span several
+    source buckets and exceed one chunk (150k neurons, 100 synapses each,
+    delays 1..20: about 4,900 entries per run over ten 16,384-source
+    buckets; weights lognormal(-1, 1) nS), against the warp-per-column kernel:
+    same rasters, inputs within the spread of two summation orders."""
+    def run(unsliced):
+        if unsliced:
+            monkeypatch.setenv("NN_PULL_UNSLICED", "1")
+        else:
+            monkeypatch.delenv("NN_PULL_UNSLICED", raising=False)
+        n = 150_000
+        c = nn.default_config(n)
+        c.seed, c.max_delay, c.raster_capacity, c.delivery = 5, 20, 2_000_000, 1
+        s = nn.Simulation(ctx, c)
+        spec = nn.default_net_spec(nn.NN_NET_GAUSS)
+        spec.k, spec.dmax, spec.w_mu = 100, 20, -1.0
+        s.generate_network(spec)
+        assert s.pull_info()[0] == (not unsliced)
+        s.init_state(-65.0, 6.0, 12.0)
+        s.set_field("V", np.random.default_rng(4).uniform(-65, -35, n).astype(np.float32))
+        s.step(45)
+        return raster_set(*s.raster()), np.stack([s.get_field("GE"), s.get_field("GI")])
+    a, b, u = run(False), run(False), run(True)
+    assert len(a[0]) > 1000
+    assert a[0] == b[0] and np.array_equal(a[1], b[1])
+    assert a[0] == u[0]
+    np.testing.assert_allclose(a[1], u[1], rtol=1e-4, atol=1e-5)
+
+
 def test_delays_parity(ctx, orc):
     """Gaussian network with delays U{1..20}: raster and state vs the oracle."""
     n, seed = 2744, 31
