@@ -13,8 +13,9 @@
 //   u   = M r                      w   = A u
 //   g = (r, u), d = (w, u), rho = (r, r)   -> one reduction
 //   b_{i+1} = g / g_old,  a_{i+1} = g / (d - b_{i+1} g / a_i)
-// One kernel does all of it: a block owns a 32 x 8 x 16 tile and marches in
-// z; planes of r, w and s (with a one-cell halo, the TMA box starting 16-byte
+// One kernel does all of it: a block owns a 32 x 16 x zc tile (each thread two
+// rows, iy and iy + 8) and marches in z; planes of r, w and s (with a one-cell
+// halo, the TMA box starting 16-byte
 // aligned at x0 - 4) are staged into shared memory by cp.async.bulk.tensor
 // through a 4-deep mbarrier pipeline; out-of-range boxes are zero-filled by
 // the TMA unit, which is exactly the Dirichlet boundary.  u = M r_new is formed
@@ -36,11 +37,13 @@
 
 namespace {
 constexpr int CG_THREADS = 256;
-constexpr int TX = 32, TY = 8;             // tile; its depth in z (zc) is chosen per plan
-constexpr int BXW = 40, BYW = 10;            // TMA box: x from x0 - 4, y from y0 - 1
+constexpr int TX = 32, TY = 16;            // tile; its depth in z (zc) is chosen per plan
+constexpr int HY = TY / 2;                   // a thread's second row is 8 below its first
+constexpr int BXW = 40, BYW = TY + 2;        // TMA box: x from x0 - 4, y from y0 - 1
 constexpr int RX = TX + 2, RY = TY + 2;      // u region (tile + halo)
-constexpr int PLANE_BYTES = BXW * BYW * 4;   // 1600
-constexpr int PLANE_STRIDE = 1664;           // 128-byte multiple
+constexpr int PLANE_BYTES = BXW * BYW * 4;   // 2880
+constexpr int PLANE_STRIDE = 2944;           // 128-byte multiple
+static_assert(CG_THREADS == TX * HY && PLANE_STRIDE >= PLANE_BYTES && PLANE_STRIDE % 128 == 0, "tile shape");
 constexpr int PX_BYTES = TX * TY * 4;        // p, x interior boxes (owned planes only)
 constexpr int STAGES = 3;
 constexpr int RING = 3;                      // u-ring slots: planes k-2 .. k
@@ -55,7 +58,7 @@ struct Layout {
 };
 static_assert(Layout<true>::SMEM_BYTES <= 227 * 1024, "shared memory");
 constexpr uint32_t WAIT_LIMIT = 1u << 20;
-constexpr int HALO_CELLS = 2 * RX + 2 * TY;  // 84
+constexpr int HALO_CELLS = 2 * RX + 2 * TY;  // 100
 
 enum { C_GAMMA = 0, C_ALPHA, C_BETA, C_RR, C_BB, C_DELTA, C_COUNT };
 
@@ -255,10 +258,12 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init_w(CgArgs a, const float*
     }
 }
 
+__device__ void cg_finish(const CgArgs& a, float acc_g, float acc_d, float acc_r);
+
 // One CG iteration (see the file comment).  One tile per block.  tm_d and
 // tm_m (D and 1/diag) are read only by the HET variant.
 template <bool HET>
-__global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant__ CUtensorMap tm_r,
+__global__ void __launch_bounds__(CG_THREADS, 4) k_cg_iter(const __grid_constant__ CUtensorMap tm_r,
                                                         const __grid_constant__ CUtensorMap tm_w,
                                                         const __grid_constant__ CUtensorMap tm_s,
                                                         const __grid_constant__ CUtensorMap tm_d,
@@ -318,12 +323,13 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
     if (tid == 0)
         for (int j = 0; j < STAGES && j < np; ++j) issue(j);
 
-    // per-thread invariants: interior cell, its offsets in a staged plane, in
-    // the u region and in a p/x box, its global index without z; the halo
-    // cell this thread fills (tid < HALO_CELLS)
+    // per-thread invariants: interior cells (rows iy and iy + HY), their
+    // offsets in a staged plane, in the u region and in a p/x box, the global
+    // index of the first without z; the halo cell this thread fills
+    // (tid < HALO_CELLS)
     const int ix = tid & 31, iy = tid >> 5;
     const int gx = x0 + ix, gy = y0 + iy;
-    const bool col_in = gx < a.nx && gy < a.ny;
+    const bool col_in[2] = {gx < a.nx && gy < a.ny, gx < a.nx && gy + HY < a.ny};
     const int ib = (iy + 1) * BXW + ix + 4;
     const int iu = (iy + 1) * RX + ix + 1;
     const int ip = iy * TX + ix;
@@ -373,20 +379,22 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
         float* Dk = Dr + SL * RY * RX;
         const bool plane_in = k >= 0 && k < a.nz;
         // interior cells: s, r, u and the pointwise p, x updates for owned planes
-        {
-            const float sv = W[ib] + beta * S[ib];
-            const float rv_old = R[ib];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int bh = ib + h * HY * BXW, uh = iu + h * HY * RX, ph = ip + h * HY * TX;
+            const float sv = W[bh] + beta * S[bh];
+            const float rv_old = R[bh];
             const float rv = rv_old - alpha * sv;
-            const bool in = col_in && plane_in;
-            const float mi = HET ? Mst[ib] : a.invd;
+            const bool in = col_in[h] && plane_in;
+            const float mi = HET ? Mst[bh] : a.invd;
             const float uv = in ? mi * rv : 0.0f;
-            Uk[iu] = uv;
-            if (HET) Dk[iu] = Dst[ib];
+            Uk[uh] = uv;
+            if (HET) Dk[uh] = Dst[bh];
             if (in && k >= z0 && k < z1) {
-                const int c = cxy + sz * k;
-                const float pv = mi * rv_old + beta * Ps[ip];
+                const int c = cxy + h * HY * sy + sz * k;
+                const float pv = mi * rv_old + beta * Ps[ph];
                 a.p[c] = pv;
-                a.x[c] = Xs[ip] + alpha * pv;
+                a.x[c] = Xs[ph] + alpha * pv;
                 a.s_out[c] = sv;
                 a.r_out[c] = rv;
                 acc_g += rv * uv;
@@ -405,28 +413,32 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
         // refill this stage with the plane STAGES ahead
         if (tid == 0 && j + STAGES < np) issue(j + STAGES);
         // w = A u for the plane behind (k - 1), owned when j >= 2
-        if (j >= 2 && col_in && k - 1 < z1) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!(j >= 2 && col_in[h] && k - 1 < z1)) continue;
             const int kb = k - 1;
+            const int uh = iu + h * HY * RX;
             const float* Um = U + SM * RY * RX;
             const float* Uc = U + SC * RY * RX;
-            const float uc = Uc[iu];
+            const float uc = Uc[uh];
             float wv;
             if (HET) {
                 const float* Dm = Dr + SM * RY * RX;
                 const float* Dc = Dr + SC * RY * RX;
-                const float dc = Dc[iu];
-                float acc = face_coef(dc, Dc[iu - 1], gx > 0) * (uc - Uc[iu - 1]);
-                acc += face_coef(dc, Dc[iu + 1], gx < a.nx - 1) * (uc - Uc[iu + 1]);
-                acc += face_coef(dc, Dc[iu - RX], gy > 0) * (uc - Uc[iu - RX]);
-                acc += face_coef(dc, Dc[iu + RX], gy < a.ny - 1) * (uc - Uc[iu + RX]);
-                acc += face_coef(dc, Dm[iu], kb > 0) * (uc - Um[iu]);
-                acc += face_coef(dc, Dk[iu], kb < a.nz - 1) * (uc - Uk[iu]);
+                const int gyh = gy + h * HY;
+                const float dc = Dc[uh];
+                float acc = face_coef(dc, Dc[uh - 1], gx > 0) * (uc - Uc[uh - 1]);
+                acc += face_coef(dc, Dc[uh + 1], gx < a.nx - 1) * (uc - Uc[uh + 1]);
+                acc += face_coef(dc, Dc[uh - RX], gyh > 0) * (uc - Uc[uh - RX]);
+                acc += face_coef(dc, Dc[uh + RX], gyh < a.ny - 1) * (uc - Uc[uh + RX]);
+                acc += face_coef(dc, Dm[uh], kb > 0) * (uc - Um[uh]);
+                acc += face_coef(dc, Dk[uh], kb < a.nz - 1) * (uc - Uk[uh]);
                 wv = a.onepb * uc + a.op_alpha * acc;
             } else {
-                const float nb = Uc[iu - 1] + Uc[iu + 1] + Uc[iu - RX] + Uc[iu + RX] + Um[iu] + Uk[iu];
+                const float nb = Uc[uh - 1] + Uc[uh + 1] + Uc[uh - RX] + Uc[uh + RX] + Um[uh] + Uk[uh];
                 wv = (a.onepb + 6.0f * a.op_alpha) * uc - a.op_alpha * nb;
             }
-            a.w_out[cxy + sz * kb] = wv;
+            a.w_out[cxy + h * HY * sy + sz * kb] = wv;
             acc_d += wv * uc;
         }
         return true;
@@ -444,6 +456,13 @@ __global__ void __launch_bounds__(CG_THREADS, 8) k_cg_iter(const __grid_constant
         }
         return;
     }
+    cg_finish(a, acc_g, acc_d, acc_r);
+}
+
+// The iteration's reduction of (r, u), (w, u), (r, r) and, in the last block
+// to arrive, the next iteration's scalars and the stop flag.
+__device__ void cg_finish(const CgArgs& a, float acc_g, float acc_d, float acc_r)
+{
     float v[3] = {acc_g, acc_d, acc_r};
     double out[3];
     if (cg_reduce(3, v, a.partials, a.ticket, out) && threadIdx.x == 0) {
@@ -603,7 +622,7 @@ nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, d
                           : cudaFuncSetAttribute(k_cg_iter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  Layout<false>::SMEM_BYTES);
         if (e != cudaSuccess) st = nn_cuda_check(ctx, e, "cudaFuncSetAttribute(k_cg_iter)");
-        // all of the unified L1/shared storage as shared memory: 8 blocks per SM
+        // all of the unified L1/shared storage as shared memory: the most blocks per SM
         e = D ? cudaFuncSetAttribute(k_cg_iter<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100)
               : cudaFuncSetAttribute(k_cg_iter<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if (st == NN_OK && e != cudaSuccess) st = nn_cuda_check(ctx, e, "cudaFuncSetAttribute(carveout)");
@@ -809,17 +828,9 @@ nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, i
             }
             NN_CUDA(ctx, cudaEventRecord(pl->ev_a[nchunks], cs));
         }
-        for (int q = 0; q < chunk && it < max_iter; ++q, ++it) {
-            const int pin = it & 1, pout = pin ^ 1;
-            CgArgs a = cg_args(pl, d_x, rtol, max_iter, pout);
-            if (het)
-                k_cg_iter<true><<<pl->tiles, CG_THREADS, Layout<true>::SMEM_BYTES, cs>>>(
-                    pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], pl->map_d, pl->map_m, pl->map_p, map_x, a);
-            else
-                k_cg_iter<false><<<pl->tiles, CG_THREADS, Layout<false>::SMEM_BYTES, cs>>>(
-                    pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], pl->map_p, pl->map_p, pl->map_p, map_x, a);
-            NN_CHECK_LAUNCH(ctx, "k_cg_iter");
-        }
+        const int n = std::min(chunk, max_iter - it);
+        NN_TRY(enqueue_iters(pl, d_x, map_x, rtol, max_iter, it, n, cs));
+        it += n;
         if (pl->timing) NN_CUDA(ctx, cudaEventRecord(pl->ev_b[nchunks], cs));
         ++nchunks;
     }

@@ -89,3 +89,4 @@ def test_single_kernel_and_two_kernel_paths_agree(ctx, orc, shape, hetero, monke
         assert np.linalg.norm(x - ref) <= 1e-5 * np.linalg.norm(ref)
         its.append(it)
     assert abs(its[0] - its[1]) <= 2
+
