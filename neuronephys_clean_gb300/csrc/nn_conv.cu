@@ -14,9 +14,11 @@
 // and the epilogue (bias, ReLU, optional gradient mask, BF16 store with zeros
 // on pads) reads the accumulator back with tcgen05.ld.
 //
-// Weight gradient: CUDA-core FP32 over the same staged windows; a thread owns
-// an 8 x 8 (cin x cout) block of one tap, persistent CTAs accumulate over many
-// tiles in registers and add to the FP32 gradient once.
+// Weight gradient: for each (dz, dy) pair one GEMM on the tensor cores with
+// M = COUT (padded to 128), N = 3 * CIN (the three dx taps), K = voxels, over
+// staged gradient tiles and x windows read as MN-major operands (channels
+// contiguous; see k_conv3_wgrad).  Persistent CTAs accumulate over many tiles
+// in tensor memory and add to the FP32 gradient once.
 #include <cuda_bf16.h>
 
 #include "nn_conv.cuh"
@@ -207,80 +209,164 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
 
 // ------------------------------------------------------------- wgrad --
 
-constexpr int WG_THREADS = 256;
+// dW[(dz, dy, dx)][ci][co] += sum over voxels o of x(o + shift)[ci] gy(o)[co]:
+// per (dz, dy) one GEMM D (M x N) = A (M x K) B^T for all three dx taps, with
+// M = 128 rows (TMEM lane = output channel; rows past COUT are discarded),
+// N = 3 * CIN (column dx * CIN + ci), K = the voxels of a tile.  A is the
+// staged gradient tile; both operands are read MN-major: 16 bytes hold 8
+// channels of one voxel, so a core matrix is 8 consecutive voxels (128
+// contiguous bytes).  For narrow inputs (CIN <= 32) B is the x window staged
+// three times, shifted by dx voxels, so that one MMA per K step covers the
+// three taps; wider inputs stage the 130-voxel window once and issue one MMA
+// per tap (N = CIN), reading it at byte offsets 0, 16, 32 (fewer bytes per
+// slot, more CTAs per SM).  The rows of A past COUT read whatever in-bounds
+// shared memory follows (their results are never used).  The accumulator covers all of the CTA's tiles;
+// STAGES slots double-buffer the bulk copies against the MMAs, and the
+// epilogue adds D to the FP32 gradient once.
+constexpr int WG_THREADS = 128;
+constexpr int WG_MP = 128;                             // M
+constexpr int WG_BLOCK = TILE * 16;                    // one 8-channel block of a tile (2,048 bytes)
+constexpr int WG_A_SPAN = (WG_MP / 8) * WG_BLOCK;      // bytes the 128 rows of A address
 
 template <int CIN, int COUT>
 struct WgCfg {
-    static constexpr int NB = 3 * (CIN / 8) * (COUT / 8);    // (dx, cin block, cout block) per (dz, dy)
-    static constexpr int NS = NB >= WG_THREADS ? 1 : WG_THREADS / NB;  // voxel splits of a tile
-    static constexpr int PASSES = (NB + WG_THREADS - 1) / WG_THREADS;
-    static constexpr int XB = (CIN / 8) * WIN * 16;           // staged x window bytes
-    static constexpr int GB = (COUT / 8) * TILE * 16;         // staged gradient tile bytes
-    static constexpr int SMEM = XB + GB;
+    static constexpr bool MERGE = CIN <= 32;                    // the three taps in one MMA
+    static constexpr int N = 3 * CIN;
+    static constexpr int NSPLIT = MERGE ? 1 : 3;                // MMAs per K step
+    static constexpr int NM = N / NSPLIT;                       // N of one MMA
+    static constexpr int B_BSTRIDE = MERGE ? WG_BLOCK : WIN_BYTES;  // between 8-channel blocks of B
+    static constexpr int A_BYTES = (COUT / 8) * WG_BLOCK;       // gradient tile
+    static constexpr int B_BYTES = MERGE ? 3 * (CIN / 8) * WG_BLOCK : (CIN / 8) * WIN_BYTES;  // x
+    static constexpr int SLOT = A_BYTES + B_BYTES;
+    static constexpr int TAIL = WG_A_SPAN > SLOT ? WG_A_SPAN - SLOT : 0;  // A rows of the last slot past it
+    static constexpr int STAGES = 2 * SLOT + TAIL <= 150 * 1024 && 3 * SLOT + TAIL <= 150 * 1024 ? 3 : 2;
+    static constexpr int SMEM = 128 + STAGES * SLOT + TAIL;
+    static constexpr uint32_t TMEM_COLS = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : N <= 256 ? 256 : 512;
+    static_assert(CIN % 8 == 0 && COUT % 8 == 0 && COUT <= WG_MP && N <= 512, "channel counts");
+    static_assert(NM % 16 == 0 && NM <= 256 && N % NSPLIT == 0, "MMA shape");
+    static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 
-// blockIdx.y = (dz, dy); persistent over tiles in blockIdx.x.
+// blockIdx.y = (dz, dy); tiles blockIdx.x, blockIdx.x + gridDim.x, ...
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad(const uint4* __restrict__ x, const uint4* __restrict__ gy,
-                                                            nn_act_geom g, float* dw)
+                                                            nn_act_geom g, float* dw, int* err)
 {
     using C = WgCfg<CIN, COUT>;
-    extern __shared__ uint4 wsm[];
-    uint4* Xs = wsm;                                // [CIN/8][WIN]
-    uint4* Gs = wsm + (CIN / 8) * WIN;              // [COUT/8][TILE]
-    const int st = blockIdx.y, dz = st / 3 - 1, dy = st % 3 - 1;
-    const int tid = threadIdx.x;
-    float acc[C::PASSES][64];
-#pragma unroll
-    for (int p = 0; p < C::PASSES; ++p)
-#pragma unroll
-        for (int i = 0; i < 64; ++i) acc[p][i] = 0.0f;
+    constexpr int S = C::STAGES;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* sm = align128(smem_raw);
+    __shared__ uint64_t full[S], done[S], acc_bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int st9 = blockIdx.y, dz = st9 / 3 - 1, dy = st9 % 3 - 1;
+    const int64_t ntiles =
+        (int64_t)blockIdx.x < g.tiles ? (g.tiles - 1 - (int64_t)blockIdx.x) / gridDim.x + 1 : 0;
+    if (tid == 0) {
+        for (int q = 0; q < S; ++q) {
+            nn_mbar_init(&full[q], 1);
+            nn_mbar_init(&done[q], 1);
+        }
+        nn_mbar_init(&acc_bar, 1);
+        nn_mbar_fence_init();
+        abort_flag = 0;
+    }
+    if (warp == 0) nn_tmem_alloc(&tmem_slot, C::TMEM_COLS);
+    nn_tc_fence_before();
+    __syncthreads();
+    nn_tc_fence_after();
+    const uint32_t tmem = tmem_slot;
 
-    for (int64_t tile = blockIdx.x; tile < g.tiles; tile += gridDim.x) {
-        const int64_t o0 = g.o_first + tile * TILE;
-        const int64_t start = o0 + dz * g.P + dy * g.R - 1;
-        __syncthreads();
-        for (int i = tid; i < (CIN / 8) * WIN; i += WG_THREADS) {
-            const int gi = i / WIN, v = i - gi * WIN;
-            Xs[i] = x[gi * g.S + g.GD + start + v];
+    if (tid == 0) {
+        int64_t issued = 0, consumed = 0;
+        // tile j into slot j % S: the gradient blocks, then x at shifts dx = 0, 1, 2
+        auto issue = [&](int64_t j) {
+            const int q = (int)(j % S);
+            const int64_t o0 = g.o_first + (blockIdx.x + j * gridDim.x) * TILE;
+            const int64_t start = o0 + dz * g.P + dy * g.R - 1;
+            unsigned char* buf = sm + q * C::SLOT;
+            nn_mbar_expect_tx(&full[q], C::A_BYTES + C::B_BYTES);
+#pragma unroll
+            for (int ob = 0; ob < COUT / 8; ++ob)
+                nn_bulk_g2s(buf + ob * WG_BLOCK, gy + ob * g.S + g.GD + o0, WG_BLOCK, &full[q]);
+            if (C::MERGE) {
+#pragma unroll
+                for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+                    for (int cb = 0; cb < CIN / 8; ++cb)
+                        nn_bulk_g2s(buf + C::A_BYTES + (dx * (CIN / 8) + cb) * WG_BLOCK,
+                                    x + cb * g.S + g.GD + start + dx, WG_BLOCK, &full[q]);
+            } else {
+#pragma unroll
+                for (int cb = 0; cb < CIN / 8; ++cb)
+                    nn_bulk_g2s(buf + C::A_BYTES + cb * WIN_BYTES, x + cb * g.S + g.GD + start, WIN_BYTES, &full[q]);
+            }
+            ++issued;
+        };
+        // A and B both MN-major (bits 15, 16 of the instruction descriptor)
+        constexpr uint32_t idesc = nn_umma_idesc_bf16(WG_MP, C::NM) | (1u << 15) | (1u << 16);
+        bool ok = true;
+        for (int64_t j = 0; j < S && j < ntiles; ++j) issue(j);
+        for (int64_t j = 0; j < ntiles; ++j) {
+            const int q = (int)(j % S);
+            ok = nn_mbar_wait(&full[q], (uint32_t)((j / S) & 1), CONV_WAIT_LIMIT);
+            if (!ok) break;
+            ++consumed;
+            nn_tc_fence_after();
+            const uint32_t abase = nn_smem_u32(sm + q * C::SLOT), bbase = abase + C::A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TILE / 16; ++kk)
+#pragma unroll
+                for (int h = 0; h < C::NSPLIT; ++h) {
+                    // MN-major no-swizzle: LBO = next 8 voxels (K), SBO = next 8 channels (M / N)
+                    // (merged: B starts at the first block of all taps; else tap h
+                    // is the window read h voxels further on)
+                    const uint32_t boff = C::MERGE ? kk * 256 : (kk * 16 + h) * 16;
+                    const uint64_t ad = nn_umma_sdesc(abase + kk * 256, 128, WG_BLOCK);
+                    const uint64_t bd = nn_umma_sdesc(bbase + boff, 128, C::B_BSTRIDE);
+                    nn_umma_bf16(tmem + h * C::NM, ad, bd, idesc, (j | kk) != 0);
+                }
+            nn_umma_commit(&done[q]);
+            if (j + S < ntiles) {
+                ok = nn_mbar_wait(&done[q], (uint32_t)((j / S) & 1), CONV_WAIT_LIMIT);
+                if (!ok) break;
+                issue(j + S);
+            }
         }
-        for (int i = tid; i < (COUT / 8) * TILE; i += WG_THREADS) {
-            const int gb = i / TILE, v = i - gb * TILE;
-            Gs[i] = gy[gb * g.S + g.GD + o0 + v];
+        nn_umma_commit(&acc_bar);
+        if (!ok) {
+            abort_flag = 1;
+            // let copies already in flight land before the CTA leaves
+            for (int64_t j = consumed; j < issued; ++j)
+                nn_mbar_wait(&full[j % S], (uint32_t)((j / S) & 1), CONV_WAIT_LIMIT);
         }
-        __syncthreads();
+    }
+    if (!nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
+    __syncthreads();
+    nn_tc_fence_after();
+    if (abort_flag) {  // block-uniform: the TMEM loads below are warp-collective
+        if (tid == 0) atomicExch(err, 1);
+    } else if (ntiles > 0) {
+        const int co = tid;  // TMEM lane == row == output channel
 #pragma unroll
-        for (int p = 0; p < C::PASSES; ++p) {
-            const int t = tid + p * WG_THREADS;
-            const int blk = t % C::NB, split = t / C::NB;
-            if (t >= C::NB * C::NS) continue;
-            const int dx = blk / ((CIN / 8) * (COUT / 8));
-            const int rem = blk - dx * (CIN / 8) * (COUT / 8);
-            const int cb = rem / (COUT / 8), ob = rem - cb * (COUT / 8);
-            const int m0 = split * TILE / C::NS, m1 = (split + 1) * TILE / C::NS;
-            for (int m = m0; m < m1; ++m) {
-                float xv[8], gv[8];
-                unpack_bf16x8(Xs[cb * WIN + m + dx], xv);
-                unpack_bf16x8(Gs[ob * TILE + m], gv);
+        for (int c0 = 0; c0 < C::N; c0 += 16) {
+            float v[16];
+            nn_tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+            if (co < COUT) {
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) acc[p][i * 8 + j] = fmaf(xv[i], gv[j], acc[p][i * 8 + j]);
+                for (int i = 0; i < 16; ++i) {
+                    const int n = c0 + i, dx = n / CIN, ci = n - dx * CIN;
+                    atomicAdd(dw + ((size_t)(st9 * 3 + dx) * CIN + ci) * COUT + co, v[i]);
+                }
             }
         }
     }
-#pragma unroll
-    for (int p = 0; p < C::PASSES; ++p) {
-        const int t = tid + p * WG_THREADS;
-        if (t >= C::NB * C::NS) continue;
-        const int blk = t % C::NB;
-        const int dx = blk / ((CIN / 8) * (COUT / 8));
-        const int rem = blk - dx * (CIN / 8) * (COUT / 8);
-        const int cb = rem / (COUT / 8), ob = rem - cb * (COUT / 8);
-        const int tap = st * 3 + dx;
-        for (int i = 0; i < 8; ++i)
-            for (int j = 0; j < 8; ++j)
-                atomicAdd(&dw[((size_t)tap * CIN + cb * 8 + i) * COUT + ob * 8 + j], acc[p][i * 8 + j]);
+    nn_tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        nn_tc_fence_after();
+        nn_tmem_dealloc(tmem, C::TMEM_COLS);
     }
 }
 
@@ -377,18 +463,26 @@ nn_status launch_fwd(nn_ctx* ctx, const ConvArgs& a)
 }
 
 template <int CIN, int COUT>
-nn_status launch_wgrad(nn_ctx* ctx, const nn_act_geom& g, const void* x, const void* gy, float* dw)
+nn_status launch_wgrad(nn_ctx* ctx, const nn_act_geom& g, const void* x, const void* gy, float* dw, int* err)
 {
     using C = WgCfg<CIN, COUT>;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static int per_sm = 0;  // resident CTAs per SM (per process, like the attribute)
+    if (!per_sm) {
         NN_CUDA(ctx, cudaFuncSetAttribute(k_conv3_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           C::SMEM));
-        attr_set = true;
+        NN_CUDA(ctx, cudaFuncSetAttribute(k_conv3_wgrad<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          100));
+        // CTAs that fit an SM's shared memory (1 KB reserved per CTA) and its
+        // 512 tensor-memory columns; more would only wait for a slot
+        int smem_sm = 0;
+        NN_CUDA(ctx, cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device));
+        per_sm = std::max(1, std::min(smem_sm / (C::SMEM + 1024), (int)(512 / C::TMEM_COLS)));
     }
-    const int64_t per_y = std::max<int64_t>(1, std::min<int64_t>(g.tiles, (int64_t)ctx->num_sms * 2));
+    // one wave of persistent CTAs over the 9 (dz, dy) pairs
+    const int64_t per_y = std::max<int64_t>(1, std::min<int64_t>(g.tiles, ((int64_t)ctx->num_sms * per_sm) / 9));
     dim3 grid((unsigned)per_y, 9);
-    k_conv3_wgrad<CIN, COUT><<<grid, WG_THREADS, C::SMEM, ctx->stream>>>((const uint4*)x, (const uint4*)gy, g, dw);
+    k_conv3_wgrad<CIN, COUT>
+        <<<grid, WG_THREADS, C::SMEM, ctx->stream>>>((const uint4*)x, (const uint4*)gy, g, dw, err);
     NN_CHECK_LAUNCH(ctx, "k_conv3_wgrad");
     return NN_OK;
 }
@@ -430,12 +524,12 @@ nn_status nn_conv_forward(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, 
 }
 
 nn_status nn_conv_wgrad(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, const void* x, const void* gy,
-                        float* dw, float* db)
+                        float* dw, float* db, int* err)
 {
     if (g.tiles <= 0) return NN_OK;
     nn_status st = NN_ERR_UNSUPPORTED;
 #define NN_X(ci, co) \
-    if (st == NN_ERR_UNSUPPORTED && cin == ci && cout == co) st = launch_wgrad<ci, co>(ctx, g, x, gy, dw);
+    if (st == NN_ERR_UNSUPPORTED && cin == ci && cout == co) st = launch_wgrad<ci, co>(ctx, g, x, gy, dw, err);
     NN_CONV_SHAPES(NN_X)
 #undef NN_X
     if (st == NN_ERR_UNSUPPORTED) return nn_fail(ctx, st, "conv3d wgrad %d -> %d is not instantiated", cin, cout);
@@ -532,5 +626,15 @@ extern "C" nn_status nn_conv3d_wgrad(nn_ctx* ctx, int nz, int ny, int nx, int ci
 {
     if (!ctx || !d_x || !d_gy || !d_dw) return NN_ERR_INVALID_ARG;
     if (!nn_conv_supported(cin, cout)) return nn_fail(ctx, NN_ERR_UNSUPPORTED, "conv3d wgrad %d -> %d", cin, cout);
-    return nn_conv_wgrad(ctx, nn_act_geometry(nz, ny, nx), cin, cout, d_x, d_gy, d_dw, d_db);
+    int* err = nullptr;
+    NN_TRY(nn_alloc(ctx, &err, 1));
+    nn_status st = nn_cuda_check(ctx, cudaMemsetAsync(err, 0, sizeof(int), ctx->stream), "memset");
+    if (st == NN_OK) st = nn_conv_wgrad(ctx, nn_act_geometry(nz, ny, nx), cin, cout, d_x, d_gy, d_dw, d_db, err);
+    int h_err = 0;
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost,
+                                                             ctx->stream), "memcpy");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "conv3d wgrad");
+    nn_release(err);
+    if (st == NN_OK && h_err) st = nn_fail(ctx, NN_ERR_TIMEOUT, "k_conv3_wgrad: a pipeline wait timed out");
+    return st;
 }

@@ -48,8 +48,9 @@ size_t nn_conv_packed_weight_bytes(int cin, int cout);
 nn_status nn_conv_forward(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, const void* x, const void* wpacked,
                           const float* bias, int relu, const void* mask, void* y, float* y32, int* err);
 // dw[27][cin][cout] += sum over voxels of x(o + tap) gy(o); db[cout] += sum gy.
+// err (device int) is set when a pipeline wait gives up.
 nn_status nn_conv_wgrad(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, const void* x, const void* gy,
-                        float* dw, float* db);
+                        float* dw, float* db, int* err);
 // Pack FP32 weights w[27][cin][cout] (tap = (dz+1)*9 + (dy+1)*3 + dx+1) into
 // the tile-ordered BF16 blocks the forward kernel streams.  With flip set the
 // packed operator is the adjoint (taps mirrored, cin and cout exchanged),

@@ -526,7 +526,7 @@ static nn_status conv_adj(nn_unet* u, int l, const void* gy, void* gx, const voi
 
 static nn_status wgrad(nn_unet* u, int l, const void* x, const void* gy)
 {
-    return nn_conv_wgrad(u->ctx, u->g[LLEVEL[l]], LCIN[l], LCOUT[l], x, gy, u->L[l].gw, u->L[l].gb);
+    return nn_conv_wgrad(u->ctx, u->g[LLEVEL[l]], LCIN[l], LCOUT[l], x, gy, u->L[l].gw, u->L[l].gb, u->err);
 }
 
 template <class K, class... A>

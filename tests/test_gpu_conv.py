@@ -77,7 +77,10 @@ def test_mask_and_dense_output(ctx):
     np.testing.assert_allclose(y32.numpy(), U.bf16(ref[0]), rtol=2.0 ** -7, atol=1e-6 * np.abs(ref).max())
 
 
-@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 64), (96, 32), (48, 16)])
+WGRAD = FWD + [(32, 16), (64, 32), (32, 96), (16, 48)]
+
+
+@pytest.mark.parametrize("cin,cout", WGRAD)
 def test_weight_gradient_matches_oracle(ctx, cin, cout):
     rng = np.random.default_rng(11 + cin * cout)
     x, gy = rand_act(rng, cin, SHAPE), rand_act(rng, cout, SHAPE)
@@ -97,3 +100,16 @@ def test_large_grid_many_tiles(ctx):
     ay = nn.Activation(ctx, shape, 32)
     nn.conv3d_forward(ctx, to_act(ctx, x), wp, ay, relu=True)
     assert_bf16_close(ay.unpack(), np.maximum(U.conv3d(x, w), 0.0))
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 96), (96, 32)])
+def test_weight_gradient_many_tiles(ctx, cin, cout):
+    """The tensor-core weight gradient over a grid of many tiles per CTA
+    (persistent CTAs accumulating in tensor memory across tiles)."""
+    shape = (18, 24, 30)
+    rng = np.random.default_rng(3 + cin + cout)
+    x, gy = rand_act(rng, cin, shape), rand_act(rng, cout, shape)
+    dw = ctx.to_device(np.zeros((27, cin, cout), np.float32))
+    nn.conv3d_wgrad(ctx, to_act(ctx, x), to_act(ctx, gy), dw, None)
+    rdw, _ = U.conv3d_weight_grad(x, gy)
+    np.testing.assert_allclose(dw.numpy(), rdw, rtol=1e-5, atol=1e-5 * np.abs(rdw).max())
