@@ -9,7 +9,8 @@
 // nn_conv.cuh) and the packed weights of the three dx taps; the three dx taps
 // are the same window read at byte offsets 0, 16, 32, which the no-swizzle
 // K-major operand layout (8-row x 16-byte core matrices, rows 16 bytes
-// apart) allows.  Two stages double-buffer the copies against the MMAs; one
+// apart) allows.  Up to nine stages are in flight at once (all nine when
+// they fit in 96 KB, so a small grid pays one copy round trip, not nine); one
 // thread issues CIN/16 MMAs (K = 16) per tap, commits them to an mbarrier,
 // and the epilogue (bias, ReLU, optional gradient mask, BF16 store with zeros
 // on pads) reads the accumulator back with tcgen05.ld.
@@ -43,7 +44,12 @@ struct ConvCfg {
     static constexpr int ACT_BYTES = G_IN * WIN_BYTES;
     static constexpr int W_BYTES = 3 * CIN * COUT * 2;  // the three dx taps of one (dz, dy)
     static constexpr int STAGE_STRIDE = (ACT_BYTES + W_BYTES + 127) / 128 * 128;
-    static constexpr int SMEM = 128 + 2 * STAGE_STRIDE + NN_CONV_SMEM_SLACK;
+    // (dz, dy) stages in flight on small grids: all nine when they fit in
+    // 96 KB, else as many as fit (at least two); large grids use two, which
+    // leaves room for more CTAs per SM
+    static constexpr int STAGES = 96 * 1024 / STAGE_STRIDE >= 9 ? 9 : (96 * 1024 / STAGE_STRIDE < 2 ? 2 : 96 * 1024 / STAGE_STRIDE);
+    static constexpr int SMEM = 128 + STAGES * STAGE_STRIDE + NN_CONV_SMEM_SLACK;  // the most a launch uses
+    static int smem(int stages) { return 128 + stages * STAGE_STRIDE + NN_CONV_SMEM_SLACK; }
     static constexpr uint32_t TMEM_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
     static_assert(SMEM <= 227 * 1024, "shared memory");
 };
@@ -58,6 +64,7 @@ struct ConvArgs {
     nn_act_geom g;
     int relu;
     int* err;
+    int stages;  // (dz, dy) stages in flight, 2 .. ConvCfg::STAGES
 };
 
 __device__ __forceinline__ unsigned char* align128(unsigned char* p)
@@ -102,17 +109,18 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
     using C = ConvCfg<CIN, COUT>;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* sm = align128(smem_raw);
-    __shared__ uint64_t full[2], done[2], acc_bar;
+    const int S = a.stages;
+    __shared__ uint64_t full[C::STAGES], done[C::STAGES], acc_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int64_t o0 = a.g.o_first + (int64_t)blockIdx.x * TILE;
 
     if (tid == 0) {
-        nn_mbar_init(&full[0], 1);
-        nn_mbar_init(&full[1], 1);
-        nn_mbar_init(&done[0], 1);
-        nn_mbar_init(&done[1], 1);
+        for (int q = 0; q < S; ++q) {
+            nn_mbar_init(&full[q], 1);
+            nn_mbar_init(&done[q], 1);
+        }
         nn_mbar_init(&acc_bar, 1);
         nn_mbar_fence_init();
         abort_flag = 0;
@@ -126,24 +134,24 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
     if (tid == 0) {
         int issued = 0;
         auto issue = [&](int st) {
-            unsigned char* buf = sm + (st & 1) * C::STAGE_STRIDE;
+            const int q = st % S;
+            unsigned char* buf = sm + q * C::STAGE_STRIDE;
             const int dz = st / 3 - 1, dy = st % 3 - 1;
             const int64_t start = o0 + dz * a.g.P + dy * a.g.R - 1;
-            nn_mbar_expect_tx(&full[st & 1], C::ACT_BYTES + C::W_BYTES);
+            nn_mbar_expect_tx(&full[q], C::ACT_BYTES + C::W_BYTES);
 #pragma unroll
             for (int gi = 0; gi < C::G_IN; ++gi)
-                nn_bulk_g2s(buf + gi * WIN_BYTES, a.x + gi * a.g.S + a.g.GD + start, WIN_BYTES, &full[st & 1]);
-            nn_bulk_g2s(buf + C::ACT_BYTES, a.w + (size_t)st * C::W_BYTES, C::W_BYTES, &full[st & 1]);
+                nn_bulk_g2s(buf + gi * WIN_BYTES, a.x + gi * a.g.S + a.g.GD + start, WIN_BYTES, &full[q]);
+            nn_bulk_g2s(buf + C::ACT_BYTES, a.w + (size_t)st * C::W_BYTES, C::W_BYTES, &full[q]);
             ++issued;
         };
-        issue(0);
-        issue(1);
+        for (int st = 0; st < S; ++st) issue(st);
         constexpr uint32_t idesc = nn_umma_idesc_bf16(128, COUT);
         bool ok = true;
         int consumed = 0;
         for (int st = 0; st < 9; ++st) {
-            const int b = st & 1;
-            ok = nn_mbar_wait(&full[b], (st >> 1) & 1, CONV_WAIT_LIMIT);
+            const int b = st % S;
+            ok = nn_mbar_wait(&full[b], (st / S) & 1, CONV_WAIT_LIMIT);
             if (!ok) break;
             ++consumed;
             nn_tc_fence_after();
@@ -158,17 +166,17 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
                     nn_umma_bf16(tmem, ad, bd, idesc, (st | dx | kc) != 0);
                 }
             nn_umma_commit(&done[b]);
-            if (st + 2 < 9) {
-                ok = nn_mbar_wait(&done[b], (st >> 1) & 1, CONV_WAIT_LIMIT);
+            if (st + S < 9) {
+                ok = nn_mbar_wait(&done[b], (st / S) & 1, CONV_WAIT_LIMIT);
                 if (!ok) break;
-                issue(st + 2);
+                issue(st + S);
             }
         }
         nn_umma_commit(&acc_bar);
         if (!ok) {
             abort_flag = 1;
             // let copies already in flight land before the CTA leaves
-            for (int st = consumed; st < issued; ++st) nn_mbar_wait(&full[st & 1], (st >> 1) & 1, CONV_WAIT_LIMIT);
+            for (int st = consumed; st < issued; ++st) nn_mbar_wait(&full[st % S], (st / S) & 1, CONV_WAIT_LIMIT);
         }
     }
     if (!nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
@@ -457,7 +465,11 @@ nn_status launch_fwd(nn_ctx* ctx, const ConvArgs& a)
         NN_CUDA(ctx, cudaFuncSetAttribute(k_conv3<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
         attr_set = true;
     }
-    k_conv3<CIN, COUT><<<(unsigned)a.g.tiles, CONV_THREADS, C::SMEM, ctx->stream>>>(a);
+    // small grids (at most four tiles per SM) are latency-bound: all their
+    // stages in flight; large ones keep two and more CTAs per SM
+    ConvArgs b = a;
+    b.stages = a.g.tiles <= (int64_t)ctx->num_sms * 4 ? C::STAGES : 2;
+    k_conv3<CIN, COUT><<<(unsigned)a.g.tiles, CONV_THREADS, C::smem(b.stages), ctx->stream>>>(b);
     NN_CHECK_LAUNCH(ctx, "k_conv3");
     return NN_OK;
 }
