@@ -3,15 +3,19 @@
 // alpha_b = dt D g_b^2) solved together, each to its own relative residual.
 //
 // The instances' cells are concatenated (instance b at cell offset off_b,
-// x fastest).  A thread block covers 256 consecutive cells of one instance,
+// x fastest).  A thread block covers CPB = 2,048 consecutive cells of one
+// instance (8 per thread, strided by the block size),
 // so every reduction is per instance: a block writes its FP64 partials, and
 // the last block of an instance to arrive (a per-instance ticket) sums them in
 // fixed order and forms that instance's scalars.  Per iteration two kernels
 // run (the structure of the two-kernel PCG: direction + operator, then
 // update), and blocks of converged instances return at once, so the batch
 // iterates until its slowest instance converges while the others stop
-// costing work.  The host reads one counter of unconverged instances per
-// chunk of iterations.
+// costing work.  The host reads the counter of unconverged instances and
+// their flags once per chunk of iterations; once instances have converged,
+// the chunk's kernels are launched over the blocks of the running instances
+// only (a list of block ids), since even a block that returns at once costs
+// its launch.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -20,6 +24,8 @@
 
 namespace {
 constexpr int BT = 256;
+constexpr int VPT = 8;            // cells per thread
+constexpr int CPB = BT * VPT;     // cells per block
 
 struct Batch {
     int n_inst;
@@ -36,17 +42,40 @@ struct Batch {
     int* flags;              // [n_inst] 0 running, 1 converged, 2 stopped (non-finite)
     int* iters;              // [n_inst]
     int* running;            // [1] unconverged instances
+    const int* work;         // launched block -> block id (null: the identity)
+    int nblocks;             // all blocks (the partials' stride)
     double rtol2;
 };
 
+// The block this CTA stands for.
+__device__ __forceinline__ int block_id(const Batch& B) { return B.work ? B.work[blockIdx.x] : (int)blockIdx.x; }
+
 enum { S_RZ = 0, S_PAP, S_RR, S_BB, S_ALPHA, S_BETA, S_COUNT };
 
+// n / g and n % g for 0 <= n < 2^24, g >= 1: the FP32 quotient is exact or
+// one off, and one correction step fixes it
+__device__ __forceinline__ int divmod_small(int n, int g, float invg, int& rem)
+{
+    int q = __float2int_rz((float)n * invg);
+    int r = n - q * g;
+    if (r < 0) {
+        --q;
+        r += g;
+    } else if (r >= g) {
+        ++q;
+        r -= g;
+    }
+    rem = r;
+    return q;
+}
+
+// (i, j, k) of cell c of a g^3 cube (g^3 < 2^24: the instance sides are at
+// most 256)
 __device__ __forceinline__ void coords(int64_t c, int g, int& i, int& j, int& k)
 {
-    i = (int)(c % g);
-    const int64_t t = c / g;
-    j = (int)(t % g);
-    k = (int)(t / g);
+    const float invg = 1.0f / (float)g;
+    const int t = divmod_small((int)c, g, invg, i);
+    k = divmod_small(t, g, invg, j);
 }
 
 // (A v)_c on the instance's cube (zero outside)
@@ -68,12 +97,12 @@ __device__ __forceinline__ float apply_cell(float onepb, float al, int g, int64_
 
 // block partial sums (FP32 within a warp, FP64 across warps); the last block
 // of instance b to arrive sums the instance's partials in block order
-__device__ bool instance_reduce(const Batch& B, int b, int nsum, const float* v, double* out)
+__device__ bool instance_reduce(const Batch& B, int blk, int b, int nsum, const float* v, double* out)
 {
     __shared__ double ws[3][BT / 32];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int nblocks = gridDim.x;
+    const int nblocks = B.nblocks;
     for (int q = 0; q < nsum; ++q) {
         float s = v[q];
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -84,7 +113,7 @@ __device__ bool instance_reduce(const Batch& B, int b, int nsum, const float* v,
         for (int q = 0; q < nsum; ++q) {
             double s = 0.0;
             for (int u = 0; u < BT / 32; ++u) s += ws[q][u];
-            B.partials[(size_t)q * nblocks + blockIdx.x] = s;
+            B.partials[(size_t)q * nblocks + blk] = s;
         }
         __threadfence();
         const unsigned nb = (unsigned)(B.blk_first[b + 1] - B.blk_first[b]);
@@ -116,12 +145,16 @@ __device__ bool instance_reduce(const Batch& B, int b, int nsum, const float* v,
 // r = b - A x, p = z = M r; partials (r, z), (b, b), (r, r)
 __global__ void __launch_bounds__(BT) k_bpcg_init(Batch B, const float* rhs, const float* x, float* r, float* p)
 {
-    const int b = B.blk_inst[blockIdx.x];
+    const int blk = block_id(B);
+    const int b = B.blk_inst[blk];
     const int g = B.side[b];
     const int64_t base = B.off[b], cells = B.off[b + 1] - base;
-    const int64_t c = (int64_t)(blockIdx.x - B.blk_first[b]) * BT + threadIdx.x;
+    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * CPB + threadIdx.x;
     float rz = 0.0f, bb = 0.0f, rr = 0.0f;
-    if (c < cells) {
+#pragma unroll
+    for (int v = 0; v < VPT; ++v) {
+        const int64_t c = c0 + v * BT;
+        if (c >= cells) break;
         const float* xb = x + base;
         const float ax = apply_cell(B.onepb, B.alpha[b], g, c, [&](int64_t q) { return xb[q]; });
         const float bv = rhs[base + c];
@@ -129,13 +162,13 @@ __global__ void __launch_bounds__(BT) k_bpcg_init(Batch B, const float* rhs, con
         const float zv = B.invd[b] * rv;
         r[base + c] = rv;
         p[base + c] = zv;
-        rz = rv * zv;
-        bb = bv * bv;
-        rr = rv * rv;
+        rz += rv * zv;
+        bb += bv * bv;
+        rr += rv * rv;
     }
     float v[3] = {rz, bb, rr};
     double out[3];
-    if (instance_reduce(B, b, 3, v, out) && threadIdx.x == 0) {
+    if (instance_reduce(B, blk, b, 3, v, out) && threadIdx.x == 0) {
         double* s = B.scal + (size_t)b * S_COUNT;
         s[S_RZ] = out[0];
         s[S_BB] = out[1];
@@ -153,27 +186,31 @@ __global__ void __launch_bounds__(BT) k_bpcg_init(Batch B, const float* rhs, con
 __global__ void __launch_bounds__(BT) k_bpcg_dir_apply(Batch B, const float* r, const float* p_old, float* p_new,
                                                        float* Ap)
 {
-    const int b = B.blk_inst[blockIdx.x];
+    const int blk = block_id(B);
+    const int b = B.blk_inst[blk];
     if (B.flags[b]) return;
     const int g = B.side[b];
     const int64_t base = B.off[b], cells = B.off[b + 1] - base;
-    const int64_t c = (int64_t)(blockIdx.x - B.blk_first[b]) * BT + threadIdx.x;
+    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * CPB + threadIdx.x;
     const double* s = B.scal + (size_t)b * S_COUNT;
     const float beta = (float)s[S_BETA], md = B.invd[b];
     float pap = 0.0f;
-    if (c < cells) {
-        const float* rb = r + base;
-        const float* pb = p_old + base;
-        auto pv = [&](int64_t q) { return md * rb[q] + beta * pb[q]; };
+    const float* rb = r + base;
+    const float* pb = p_old + base;
+    auto pv = [&](int64_t q) { return md * rb[q] + beta * pb[q]; };
+#pragma unroll
+    for (int v = 0; v < VPT; ++v) {
+        const int64_t c = c0 + v * BT;
+        if (c >= cells) break;
         const float pc = pv(c);
         p_new[base + c] = pc;
         const float ap = apply_cell(B.onepb, B.alpha[b], g, c, pv);
         Ap[base + c] = ap;
-        pap = pc * ap;
+        pap += pc * ap;
     }
     float v[1] = {pap};
     double out[1];
-    if (instance_reduce(B, b, 1, v, out) && threadIdx.x == 0) {
+    if (instance_reduce(B, blk, b, 1, v, out) && threadIdx.x == 0) {
         double* sw = B.scal + (size_t)b * S_COUNT;
         sw[S_PAP] = out[0];
         sw[S_ALPHA] = out[0] != 0.0 ? sw[S_RZ] / out[0] : 0.0;
@@ -184,24 +221,28 @@ __global__ void __launch_bounds__(BT) k_bpcg_dir_apply(Batch B, const float* r, 
 __global__ void __launch_bounds__(BT) k_bpcg_update(Batch B, float* x, float* r, const float* p, const float* Ap,
                                                     int max_iter)
 {
-    const int b = B.blk_inst[blockIdx.x];
+    const int blk = block_id(B);
+    const int b = B.blk_inst[blk];
     if (B.flags[b]) return;
     const int64_t base = B.off[b], cells = B.off[b + 1] - base;
-    const int64_t c = (int64_t)(blockIdx.x - B.blk_first[b]) * BT + threadIdx.x;
+    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * CPB + threadIdx.x;
     const double* s = B.scal + (size_t)b * S_COUNT;
     const float alpha = (float)s[S_ALPHA];
     float rz = 0.0f, rr = 0.0f;
-    if (c < cells) {
+#pragma unroll
+    for (int v = 0; v < VPT; ++v) {
+        const int64_t c = c0 + v * BT;
+        if (c >= cells) break;
         const int64_t q = base + c;
         x[q] += alpha * p[q];
         const float rv = r[q] - alpha * Ap[q];
         r[q] = rv;
-        rz = rv * (B.invd[b] * rv);
-        rr = rv * rv;
+        rz += rv * (B.invd[b] * rv);
+        rr += rv * rv;
     }
     float v[2] = {rz, rr};
     double out[2];
-    if (instance_reduce(B, b, 2, v, out) && threadIdx.x == 0) {
+    if (instance_reduce(B, blk, b, 2, v, out) && threadIdx.x == 0) {
         double* sw = B.scal + (size_t)b * S_COUNT;
         const int it = B.iters[b] + 1;
         B.iters[b] = it;
@@ -236,6 +277,10 @@ struct nn_bpcg {
     double* partials = nullptr;
     unsigned int* ticket = nullptr;
     float *r = nullptr, *p0 = nullptr, *p1 = nullptr, *Ap = nullptr;
+    // blocks of the running instances (host list, device copy)
+    std::vector<int> h_first;
+    std::vector<int> h_work, h_flags;
+    int* work = nullptr;
     // timing of the last solve (events around the iteration chunks)
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -249,7 +294,8 @@ extern "C" nn_status nn_bpcg_destroy(nn_bpcg* bp)
     if (bp->ctx) cudaStreamSynchronize(bp->ctx->stream);
     for (void* q : {(void*)bp->side, (void*)bp->blk_inst, (void*)bp->blk_first, (void*)bp->flags, (void*)bp->iters,
                     (void*)bp->running, (void*)bp->off, (void*)bp->alpha, (void*)bp->invd, (void*)bp->scal,
-                    (void*)bp->partials, (void*)bp->ticket, (void*)bp->r, (void*)bp->p0, (void*)bp->p1, (void*)bp->Ap})
+                    (void*)bp->partials, (void*)bp->ticket, (void*)bp->r, (void*)bp->p0, (void*)bp->p1, (void*)bp->Ap,
+                    (void*)bp->work})
         if (q) cudaFree(q);
     if (bp->ev0) cudaEventDestroy(bp->ev0);
     if (bp->ev1) cudaEventDestroy(bp->ev1);
@@ -276,20 +322,21 @@ extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides,
     std::vector<int> first((size_t)n_inst + 1, 0), binst;
     for (int b = 0; b < n_inst; ++b) {
         const int g = h_sides[b];
-        if (g < 1) {
+        if (g < 1 || g > 255) {
             nn_bpcg_destroy(bp);
-            return nn_fail(ctx, NN_ERR_INVALID_ARG, "batched PCG: instance %d has side %d", b, g);
+            return nn_fail(ctx, NN_ERR_INVALID_ARG, "batched PCG: instance %d has side %d (1 .. 255)", b, g);
         }
         const int64_t cells = (int64_t)g * g * g;
         bp->h_off[(size_t)b + 1] = bp->h_off[(size_t)b] + cells;
         al[b] = (float)(alpha_unit * g * g);
         iv[b] = (float)(1.0 / (1.0 + beta + 6.0 * alpha_unit * g * g));
-        const int nb = (int)((cells + BT - 1) / BT);
+        const int nb = (int)((cells + CPB - 1) / CPB);
         first[(size_t)b + 1] = first[(size_t)b] + nb;
         for (int q = 0; q < nb; ++q) binst.push_back(b);
     }
     bp->G = bp->h_off.back();
     bp->nblocks = first.back();
+    bp->h_first = first;
     bp->onepb = (float)(1.0 + beta);
     nn_status st = NN_OK;
     const size_t G = (size_t)bp->G;
@@ -299,6 +346,7 @@ extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides,
     if (st == NN_OK) st = nn_alloc(ctx, &bp->invd, (size_t)n_inst);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->blk_inst, (size_t)bp->nblocks);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->blk_first, (size_t)n_inst + 1);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->work, (size_t)bp->nblocks);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->flags, (size_t)n_inst);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->iters, (size_t)n_inst);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->running, 1);
@@ -355,6 +403,8 @@ static Batch batch_args(nn_bpcg* bp, double rtol)
     B.flags = bp->flags;
     B.iters = bp->iters;
     B.running = bp->running;
+    B.work = nullptr;
+    B.nblocks = bp->nblocks;
     B.rtol2 = rtol * rtol;
     return B;
 }
@@ -377,17 +427,34 @@ extern "C" nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, do
     NN_CHECK_LAUNCH(ctx, "k_bpcg_init");
     int running = 0, it = 0;
     const int chunk = 16;
+    bp->h_flags.assign((size_t)bp->n_inst, 0);
     while (true) {
         NN_CUDA(ctx, cudaMemcpyAsync(&running, bp->running, sizeof(int), cudaMemcpyDeviceToHost, cs));
+        NN_CUDA(ctx, cudaMemcpyAsync(bp->h_flags.data(), bp->flags, sizeof(int) * bp->n_inst,
+                                     cudaMemcpyDeviceToHost, cs));
         NN_CUDA(ctx, cudaStreamSynchronize(cs));
         if (running == 0 || it >= max_iter) break;
+        // the blocks of the instances still running (all blocks while none has stopped)
+        int grid = bp->nblocks;
+        B.work = nullptr;
+        if (running < bp->n_inst) {
+            bp->h_work.clear();
+            for (int b = 0; b < bp->n_inst; ++b)
+                if (bp->h_flags[(size_t)b] == 0)
+                    for (int k = bp->h_first[(size_t)b]; k < bp->h_first[(size_t)b + 1]; ++k) bp->h_work.push_back(k);
+            grid = (int)bp->h_work.size();
+            if (grid == 0) break;
+            NN_CUDA(ctx, cudaMemcpyAsync(bp->work, bp->h_work.data(), sizeof(int) * bp->h_work.size(),
+                                         cudaMemcpyHostToDevice, cs));
+            B.work = bp->work;
+        }
         for (int q = 0; q < chunk && it < max_iter; ++q, ++it) {
             // p0 holds z = M r at the start (beta = 0), then the directions alternate
             const float* p_old = (it & 1) ? bp->p1 : bp->p0;
             float* p_new = (it & 1) ? bp->p0 : bp->p1;
-            k_bpcg_dir_apply<<<bp->nblocks, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap);
+            k_bpcg_dir_apply<<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap);
             NN_CHECK_LAUNCH(ctx, "k_bpcg_dir_apply");
-            k_bpcg_update<<<bp->nblocks, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter);
+            k_bpcg_update<<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter);
             NN_CHECK_LAUNCH(ctx, "k_bpcg_update");
         }
     }
