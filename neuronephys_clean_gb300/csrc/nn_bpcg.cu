@@ -281,6 +281,12 @@ struct nn_bpcg {
     std::vector<int> h_first;
     std::vector<int> h_work, h_flags;
     int* work = nullptr;
+    // asynchronous solve in progress (nn_bpcg_async_*)
+    bool as_active = false;
+    float* as_x = nullptr;
+    double as_rtol = 0.0;
+    int as_max_iter = 0, as_it = 0;
+    cudaStream_t as_cs = nullptr;
     // timing of the last solve (events around the iteration chunks)
     bool timing = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -409,31 +415,52 @@ static Batch batch_args(nn_bpcg* bp, double rtol)
     return B;
 }
 
-// Solve every instance (x holds the initial guesses).  *unconverged: the
-// instances that stopped before reaching rtol (0 on success); iters
-// (nullable, n_inst entries): per-instance iteration counts; *max_iters: the
-// batch's iteration count.
-extern "C" nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter,
-                                   int* h_iters, int* max_iters, int* unconverged)
+namespace {
+
+// r0, z0 and the instances' initial scalars on stream cs
+nn_status enqueue_init(nn_bpcg* bp, const Batch& B, const float* d_b, const float* d_x, cudaStream_t cs)
 {
-    if (!bp || !d_b || !d_x || !(rtol > 0.0) || max_iter < 0) return NN_ERR_INVALID_ARG;
     nn_ctx* ctx = bp->ctx;
-    cudaStream_t cs = ctx->stream;
-    Batch B = batch_args(bp, rtol);
     NN_CUDA(ctx, cudaMemsetAsync(bp->running, 0, sizeof(int), cs));
     NN_CUDA(ctx, cudaMemsetAsync(bp->ticket, 0, sizeof(unsigned int) * bp->n_inst, cs));
     if (bp->timing) NN_CUDA(ctx, cudaEventRecord(bp->ev0, cs));
     k_bpcg_init<<<bp->nblocks, BT, 0, cs>>>(B, d_b, d_x, bp->r, bp->p0);
     NN_CHECK_LAUNCH(ctx, "k_bpcg_init");
-    int running = 0, it = 0;
+    return NN_OK;
+}
+
+// iterations it .. it + n - 1 over `grid` launched blocks (B.work: their ids)
+nn_status enqueue_iters(nn_bpcg* bp, const Batch& B, float* d_x, int it, int n, int grid, int max_iter,
+                        cudaStream_t cs)
+{
+    nn_ctx* ctx = bp->ctx;
+    for (int q = 0; q < n; ++q, ++it) {
+        // p0 holds z = M r at the start (beta = 0), then the directions alternate
+        const float* p_old = (it & 1) ? bp->p1 : bp->p0;
+        float* p_new = (it & 1) ? bp->p0 : bp->p1;
+        k_bpcg_dir_apply<<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap);
+        NN_CHECK_LAUNCH(ctx, "k_bpcg_dir_apply");
+        k_bpcg_update<<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter);
+        NN_CHECK_LAUNCH(ctx, "k_bpcg_update");
+    }
+    return NN_OK;
+}
+
+// Iterate from iteration *it until no instance runs, reading the counter and
+// the flags once per chunk; once instances have stopped, only the blocks of
+// the running ones are launched.
+nn_status iterate(nn_bpcg* bp, Batch B, float* d_x, int* it, int max_iter, cudaStream_t cs)
+{
+    nn_ctx* ctx = bp->ctx;
     const int chunk = 16;
+    int running = 0;
     bp->h_flags.assign((size_t)bp->n_inst, 0);
     while (true) {
         NN_CUDA(ctx, cudaMemcpyAsync(&running, bp->running, sizeof(int), cudaMemcpyDeviceToHost, cs));
         NN_CUDA(ctx, cudaMemcpyAsync(bp->h_flags.data(), bp->flags, sizeof(int) * bp->n_inst,
                                      cudaMemcpyDeviceToHost, cs));
         NN_CUDA(ctx, cudaStreamSynchronize(cs));
-        if (running == 0 || it >= max_iter) break;
+        if (running == 0 || *it >= max_iter) break;
         // the blocks of the instances still running (all blocks while none has stopped)
         int grid = bp->nblocks;
         B.work = nullptr;
@@ -448,24 +475,26 @@ extern "C" nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, do
                                          cudaMemcpyHostToDevice, cs));
             B.work = bp->work;
         }
-        for (int q = 0; q < chunk && it < max_iter; ++q, ++it) {
-            // p0 holds z = M r at the start (beta = 0), then the directions alternate
-            const float* p_old = (it & 1) ? bp->p1 : bp->p0;
-            float* p_new = (it & 1) ? bp->p0 : bp->p1;
-            k_bpcg_dir_apply<<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap);
-            NN_CHECK_LAUNCH(ctx, "k_bpcg_dir_apply");
-            k_bpcg_update<<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter);
-            NN_CHECK_LAUNCH(ctx, "k_bpcg_update");
-        }
+        const int n = std::min(chunk, max_iter - *it);
+        NN_TRY(enqueue_iters(bp, B, d_x, *it, n, grid, max_iter, cs));
+        *it += n;
     }
+    return NN_OK;
+}
+
+// Per-instance iteration counts and convergence of the finished solve.
+nn_status collect(nn_bpcg* bp, cudaStream_t cs, int* h_iters, int* max_iters, int* unconverged)
+{
+    nn_ctx* ctx = bp->ctx;
     if (bp->timing) {
         NN_CUDA(ctx, cudaEventRecord(bp->ev1, cs));
         NN_CUDA(ctx, cudaEventSynchronize(bp->ev1));
         NN_CUDA(ctx, cudaEventElapsedTime(&bp->last_ms, bp->ev0, bp->ev1));
     }
     std::vector<int> its(bp->n_inst), fl(bp->n_inst);
-    NN_CUDA(ctx, nn_copy_sync(ctx, its.data(), bp->iters, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
-    NN_CUDA(ctx, nn_copy_sync(ctx, fl.data(), bp->flags, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost));
+    NN_CUDA(ctx, cudaMemcpyAsync(its.data(), bp->iters, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost, cs));
+    NN_CUDA(ctx, cudaMemcpyAsync(fl.data(), bp->flags, sizeof(int) * bp->n_inst, cudaMemcpyDeviceToHost, cs));
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
     int mx = 0, bad = 0;
     for (int b = 0; b < bp->n_inst; ++b) {
         mx = std::max(mx, its[(size_t)b]);
@@ -476,4 +505,53 @@ extern "C" nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, do
     if (unconverged) *unconverged = bad;
     bp->last_iters = mx;
     return NN_OK;
+}
+
+}  // namespace
+
+// Solve every instance (x holds the initial guesses).  *unconverged: the
+// instances that stopped before reaching rtol (0 on success); iters
+// (nullable, n_inst entries): per-instance iteration counts; *max_iters: the
+// batch's iteration count.
+extern "C" nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter,
+                                   int* h_iters, int* max_iters, int* unconverged)
+{
+    if (!bp || !d_b || !d_x || !(rtol > 0.0) || max_iter < 0) return NN_ERR_INVALID_ARG;
+    cudaStream_t cs = bp->ctx->stream;
+    const Batch B = batch_args(bp, rtol);
+    NN_TRY(enqueue_init(bp, B, d_b, d_x, cs));
+    int it = 0;
+    NN_TRY(iterate(bp, B, d_x, &it, max_iter, cs));
+    return collect(bp, cs, h_iters, max_iters, unconverged);
+}
+
+// Asynchronous solve on stream cs: the init and n iterations over all blocks
+// (blocks of converged instances return at once) are enqueued with no host
+// read; nn_bpcg_async_finish waits for the stream, completes the solve if n
+// was not enough and reports as nn_bpcg_solve does.  The arithmetic of every
+// instance is that of nn_bpcg_solve.
+nn_status nn_bpcg_async_begin(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter, int n,
+                              cudaStream_t cs)
+{
+    if (!bp || !d_b || !d_x || !(rtol > 0.0) || max_iter < 0) return NN_ERR_INVALID_ARG;
+    const Batch B = batch_args(bp, rtol);
+    NN_TRY(enqueue_init(bp, B, d_b, d_x, cs));
+    const int m = std::max(0, std::min(n, max_iter));
+    NN_TRY(enqueue_iters(bp, B, d_x, 0, m, bp->nblocks, max_iter, cs));
+    bp->as_active = true;
+    bp->as_x = d_x;
+    bp->as_rtol = rtol;
+    bp->as_max_iter = max_iter;
+    bp->as_it = m;
+    bp->as_cs = cs;
+    return NN_OK;
+}
+
+nn_status nn_bpcg_async_finish(nn_bpcg* bp, int* h_iters, int* max_iters, int* unconverged)
+{
+    if (!bp || !bp->as_active) return NN_ERR_INVALID_ARG;
+    bp->as_active = false;
+    int it = bp->as_it;
+    NN_TRY(iterate(bp, batch_args(bp, bp->as_rtol), bp->as_x, &it, bp->as_max_iter, bp->as_cs));
+    return collect(bp, bp->as_cs, h_iters, max_iters, unconverged);
 }

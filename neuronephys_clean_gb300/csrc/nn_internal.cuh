@@ -179,6 +179,10 @@ int64_t nn_bpcg_cells(const nn_bpcg* bp);
 const int64_t* nn_bpcg_offsets(const nn_bpcg* bp);
 void nn_bpcg_set_timing(nn_bpcg* bp, bool on);
 void nn_bpcg_last_timing(const nn_bpcg* bp, float* ms, int* iters);
+// asynchronous solve on a stream (no host read until finish)
+nn_status nn_bpcg_async_begin(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter, int n,
+                              cudaStream_t cs);
+nn_status nn_bpcg_async_finish(nn_bpcg* bp, int* h_iters, int* max_iters, int* unconverged);
 
 struct nn_cg_plan;
 nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, const float* D,

@@ -1843,7 +1843,8 @@ extern "C" nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out)
 
 static bool overlap_solve(const nn_sim* s)
 {
-    return s->cfg.par_overlap && s->cfg.hp.g_par == 0.0f && !s->bpcg && s->pcg && nn_pcg_async_supported(s->pcg);
+    return s->cfg.par_overlap && s->cfg.hp.g_par == 0.0f &&
+           (s->bpcg != nullptr || (s->pcg && nn_pcg_async_supported(s->pcg)));
 }
 
 // Complete an overlapped solve: wait for its stream, finish it if the
@@ -1854,11 +1855,19 @@ static nn_status finish_solve(nn_sim* s)
     s->solve_pending = false;
     int it = 0, conv = 0;
     double rel = 0.0;
-    NN_TRY(nn_pcg_async_finish(s->pcg, &it, &rel, &conv));
+    if (s->bpcg) {
+        int unconv = 0;
+        s->inst_iters.assign((size_t)s->n_inst, 0);
+        NN_TRY(nn_bpcg_async_finish(s->bpcg, s->inst_iters.data(), &it, &unconv));
+        conv = unconv == 0;
+        s->iter_estimate = it + 2;  // the batch stops with its slowest instance
+    } else {
+        NN_TRY(nn_pcg_async_finish(s->pcg, &it, &rel, &conv));
+        s->iter_estimate = it + 8;
+    }
     s->stats.iterations = it;
     s->stats.relres = rel;
     s->stats.converged = conv;
-    s->iter_estimate = it + 8;
     return NN_OK;
 }
 
@@ -1884,8 +1893,12 @@ static nn_status paracrine_solve(nn_sim* s)
     if (overlap) {
         NN_CUDA(ctx, cudaEventRecord(s->ev_rhs, cs));
         NN_CUDA(ctx, cudaStreamWaitEvent(s->par_stream, s->ev_rhs, 0));
-        NN_TRY(nn_pcg_async_begin(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, s->iter_estimate,
-                                  s->par_stream));
+        if (s->bpcg)
+            NN_TRY(nn_bpcg_async_begin(s->bpcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, s->iter_estimate,
+                                       s->par_stream));
+        else
+            NN_TRY(nn_pcg_async_begin(s->pcg, s->b, s->u, s->cfg.par_rtol, s->cfg.par_max_iter, s->iter_estimate,
+                                      s->par_stream));
         NN_CUDA(ctx, cudaEventRecord(s->ev_solved, s->par_stream));
         s->solve_pending = true;
         s->stats.solves += 1;
