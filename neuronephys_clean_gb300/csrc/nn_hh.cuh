@@ -228,12 +228,14 @@ __device__ __forceinline__ void nn_hh_rk4(const nn_hh_dev& p, const nn_vf<W>& ng
 }
 
 // Standard normals for the neuron pair (2k, 2k+1) at one step from the
-// counter-based stream: one Philox call and one Box-Muller transform per pair
-// (cos branch for the even neuron, sin branch for the odd one).
+// counter-based stream: one Philox2x32-10 draw (counter (k, low step word),
+// key nn_noise_key) and one Box-Muller transform per pair (cos branch for the
+// even neuron, sin branch for the odd one).
 __device__ __forceinline__ void nn_normal_pair(uint64_t seed, uint32_t k, uint64_t step, float& z0, float& z1)
 {
-    const nn_u4 r = nn_philox(seed, k, (uint32_t)step, (uint32_t)(step >> 32), NN_P_NOISE);
-    const float u1 = nn_u01f_open(r.x), u2 = nn_u01f(r.y);
+    uint32_t r0, r1;
+    nn_philox2(nn_noise_key(seed, step), k, (uint32_t)step, r0, r1);
+    const float u1 = nn_u01f_open(r0), u2 = nn_u01f(r1);
     // hardware approximations (absolute error ~1e-6 in the normal deviate, far
     // below the 1e-4 parity bound): log2 and sin/cos on [-pi, pi), with
     // (cos, sin)(2 pi u2) = -(cos, sin)(2 pi u2 - pi)

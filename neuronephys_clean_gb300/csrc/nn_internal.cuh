@@ -131,6 +131,29 @@ __host__ __device__ __forceinline__ nn_u4 nn_philox(uint64_t seed, uint32_t a, u
     return nn_u4{c0, c1, c2, c3};
 }
 
+// Philox2x32-10 (same paper): the neuron-update noise stream, one draw per
+// neuron pair and step.
+__host__ __device__ __forceinline__ void nn_philox2(uint32_t key, uint32_t c0, uint32_t c1, uint32_t& o0, uint32_t& o1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi, lo;
+        nn_mulhilo(0xD256D193u, c0, hi, lo);
+        const uint32_t n0 = hi ^ key ^ c1;
+        c1 = lo;
+        c0 = n0;
+        key += 0x9E3779B9u;
+    }
+    o0 = c0;
+    o1 = c1;
+}
+
+// its key: both seed words and the high step word mixed into one word
+__host__ __device__ __forceinline__ uint32_t nn_noise_key(uint64_t seed, uint64_t step)
+{
+    return (uint32_t)seed + 0x9E3779B9u * (uint32_t)(seed >> 32) + 0x85EBCA6Bu * (uint32_t)(step >> 32);
+}
+
 // uniform in [0,1) and (0,1] with 24 random bits (exact in float)
 __host__ __device__ __forceinline__ float nn_u01f(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 __host__ __device__ __forceinline__ float nn_u01f_open(uint32_t x) { return (float)((x >> 8) + 1u) * (1.0f / 16777216.0f); }

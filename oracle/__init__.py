@@ -42,6 +42,7 @@ class OrcSim(C.Structure):
 V = C.c_void_p
 _SIGS = {
     "orc_philox4x32_10": (None, [V, V, V]),
+    "orc_philox2x32_10": (None, [V, C.c_uint32, V]),
     "orc_normal_ctr": (C.c_double, [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32]),
     "orc_minstd_next": (C.c_uint32, [P(C.c_uint32)]),
     "orc_uniform_int": (C.c_int, [P(C.c_uint32), C.c_int, C.c_int]),
@@ -107,6 +108,13 @@ def philox(ctr, key) -> np.ndarray:
     k = np.asarray(key, np.uint32)
     out = np.zeros(4, np.uint32)
     lib().orc_philox4x32_10(ptr(c), ptr(k), ptr(out))
+    return out
+
+
+def philox2(ctr, key: int) -> np.ndarray:
+    c = np.asarray(ctr, np.uint32)
+    out = np.zeros(2, np.uint32)
+    lib().orc_philox2x32_10(ptr(c), key, ptr(out))
     return out
 
 

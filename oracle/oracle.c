@@ -46,6 +46,29 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
+/* Philox2x32-10, same paper: two counter words, one key word */
+void orc_philox2x32_10(const uint32_t ctr[2], uint32_t key, uint32_t out[2])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1];
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi, lo;
+        mulhilo32(0xD256D193u, c0, &hi, &lo);
+        const uint32_t n0 = hi ^ key ^ c1;
+        c1 = lo;
+        c0 = n0;
+        key += 0x9E3779B9u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+}
+
+/* the neuron-update noise key: both seed words and the high step word mixed
+ * into Philox2x32's single key word */
+static inline uint32_t noise_key(uint64_t seed, uint64_t step)
+{
+    return (uint32_t)seed + 0x9E3779B9u * (uint32_t)(seed >> 32) + 0x85EBCA6Bu * (uint32_t)(step >> 32);
+}
+
 static inline void philox(uint64_t seed, uint32_t a, uint32_t b, uint32_t c, uint32_t purpose, uint32_t out[4])
 {
     uint32_t ctr[4] = {a, b, c, purpose};
@@ -58,9 +81,13 @@ static inline double u01_open_closed(uint32_t x) { return (double)((x >> 8) + 1u
 
 double orc_normal_ctr(uint64_t seed, uint32_t i, uint64_t step, uint32_t purpose)
 {
-    /* one draw per neuron pair (i>>1): cos branch for even i, sin for odd i */
-    uint32_t r[4];
-    philox(seed, i >> 1, (uint32_t)step, (uint32_t)(step >> 32), purpose, r);
+    /* one Philox2x32-10 draw per neuron pair (i>>1) and step, counter
+     * (pair, low step word), key noise_key(seed, step): cos branch for even i,
+     * sin for odd i.  (purpose: the noise stream is the only user) */
+    (void)purpose;
+    const uint32_t ctr[2] = {i >> 1, (uint32_t)step};
+    uint32_t r[2];
+    orc_philox2x32_10(ctr, noise_key(seed, step), r);
     double u1 = u01_open_closed(r[0]);
     double u2 = u01_closed_open(r[1]);
     double rad = sqrt(-2.0 * log(u1));

@@ -47,6 +47,7 @@ extern "C" {
 /* ------------------------------------------------------------------ RNG -- */
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11). */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+void orc_philox2x32_10(const uint32_t ctr[2], uint32_t key, uint32_t out[2]);
 /* Standard normal of neuron i at a step: one Philox draw per neuron pair,
  * counter (i>>1, step, step>>32, purpose), Box-Muller with the cos branch for
  * even i and the sin branch for odd i. */

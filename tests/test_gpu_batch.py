@@ -137,10 +137,11 @@ def test_overlapped_batched_solve_matches_serial(ctx):
     """With no field feedback each period's batched solve runs on its own
     stream while the next period's steps run (its first iterations over all
     blocks, then the blocks of unconverged instances); the fields and the
-    per-instance iteration counts equal the in-line solve's bit for bit."""
+    per-instance iteration counts equal the in-line solve's bit for bit (pull
+    delivery: fixed-point sums independent of arrival order)."""
     out = []
     for overlap in (1, 0):
-        s, off = batch_sim(ctx, seed=13, overlap=overlap)
+        s, off = batch_sim(ctx, seed=13, delivery=1, overlap=overlap)
         s.step(250)
         s.step(150)
         out.append((s.get_density(), s.instance_iterations(), s.counters()))

@@ -14,6 +14,13 @@ def test_philox_known_answers(orc):
         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
 
 
+def test_philox2x32_known_answers(orc):
+    # Random123 known-answer vectors for Philox2x32-10 (the noise stream)
+    assert list(orc.philox2([0, 0], 0)) == [0xFF1DAE59, 0x6CD10DF2]
+    assert list(orc.philox2([0xFFFFFFFF, 0xFFFFFFFF], 0xFFFFFFFF)) == [0x2C3F628B, 0xAB4FD7AD]
+    assert list(orc.philox2([0x243F6A88, 0x85A308D3], 0x13198A2E)) == [0xDD7CE038, 0xF62A4C12]
+
+
 def test_stencil_sum_identity(orc):
     """The reference's sanity check (src/paracrine.cu:82-103): a delta on a 7^3
     grid convolved with A sums to sum(delta) * sum(A)."""
