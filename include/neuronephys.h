@@ -356,6 +356,8 @@ typedef struct nn_kernel_times {
     int samples;           /* launches averaged */
     float solve_ms;        /* last paracrine solve, all iterations */
     int solve_iterations;
+    float hh_step_median_ms;   /* median k_hh_step duration (a step without a burst of spikes) */
+    float deliver_median_ms;   /* median delivery-kernel duration */
 } nn_kernel_times;
 NN_API nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out);
 

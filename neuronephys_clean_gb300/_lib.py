@@ -59,7 +59,8 @@ class SolveStats(C.Structure):
 
 class KernelTimes(C.Structure):
     _fields_ = [("hh_step_ms", c_float), ("deliver_ms", c_float), ("samples", c_int),
-                ("solve_ms", c_float), ("solve_iterations", c_int)]
+                ("solve_ms", c_float), ("solve_iterations", c_int),
+                ("hh_step_median_ms", c_float), ("deliver_median_ms", c_float)]
 
 
 # name -> (restype, argtypes)

@@ -1822,6 +1822,7 @@ extern "C" nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out)
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     double hh = 0.0, dl = 0.0;
     int cnt = 0;
+    std::vector<float> hv, dv;
     for (size_t q = 0; q < s->ev_valid.size(); ++q) {
         if (!s->ev_valid[q]) continue;
         float a = 0.0f, b = 0.0f;
@@ -1829,11 +1830,20 @@ extern "C" nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out)
         NN_CUDA(ctx, cudaEventElapsedTime(&b, s->ev_b[q], s->ev_c[q]));
         hh += a;
         dl += b;
+        hv.push_back(a);
+        dv.push_back(b);
         ++cnt;
     }
     out->hh_step_ms = cnt ? (float)(hh / cnt) : 0.0f;
     out->deliver_ms = cnt ? (float)(dl / cnt) : 0.0f;
     out->samples = cnt;
+    auto median = [](std::vector<float>& v) {
+        if (v.empty()) return 0.0f;
+        std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+        return v[v.size() / 2];
+    };
+    out->hh_step_median_ms = median(hv);
+    out->deliver_median_ms = median(dv);
     out->solve_ms = 0.0f;
     out->solve_iterations = 0;
     if (s->pcg) nn_pcg_last_timing(s->pcg, &out->solve_ms, &out->solve_iterations);
@@ -1841,9 +1851,12 @@ extern "C" nn_status nn_sim_kernel_times(nn_sim* s, nn_kernel_times* out)
     return NN_OK;
 }
 
+// The field solve overlaps the next period's steps when the field does not
+// feed back into the neurons -- except while kernel timing is on, so that
+// each kernel is timed alone.
 static bool overlap_solve(const nn_sim* s)
 {
-    return s->cfg.par_overlap && s->cfg.hp.g_par == 0.0f &&
+    return s->cfg.par_overlap && s->cfg.hp.g_par == 0.0f && !s->timing &&
            (s->bpcg != nullptr || (s->pcg && nn_pcg_async_supported(s->pcg)));
 }
 
