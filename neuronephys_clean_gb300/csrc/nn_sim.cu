@@ -63,6 +63,7 @@ struct nn_sim {
     int32_t* dsl_cptr = nullptr;   // [block][j]: first chunk of the block with delay > j (j = 0: first chunk)
     uint32_t* dsl_ent = nullptr;   // entry words, chunk by chunk (each padded to a multiple of four)
     float* dsl_w = nullptr;        // their weights
+    uint2* dsl_hits = nullptr;     // per block, from its first entry: the step's hits {entry word, weight bits}
     int dsl_cols = 0;              // columns per block of the sliced pull kernel
     int dsl_ring = 0;              // bitmap slots in shared memory
     int dsl_slotw = 0;             // words per slot
@@ -134,6 +135,7 @@ struct PullArgs {
     const int32_t* dsl_cptr;
     const uint32_t* dsl_ent;
     const float* dsl_w;
+    uint2* dsl_hits;
     int dsl_cols, dsl_ring, dsl_slotw, dsl_cmax, dsl_dmax;
     int* err;
 };
@@ -207,16 +209,20 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
 // each chunk (16-byte reads; a warp reads consecutive words) against the
 // staged bitmap, all lookups before any use.  Hits go to a per-warp queue of
 // (entry, word) pairs in shared memory; a warp empties its queue when it could
-// overflow and at the end, every lane loading all its weights before it adds
-// any.  A warp done with a chunk arrives on the slot's "empty" mbarrier; one
-// producer warp waits for it and refills the slot with the chunk dsl_ring
-// places later.  Consumer warps drift apart by up to dsl_ring - 1 chunks, and
-// no block-wide barrier separates the delays.  Sums accumulate in
-// shared memory as 64-bit fixed point (weight x 2^32; integer addition does
-// not depend on order, so the result is deterministic, and exact for weights
-// >= 2^-8).  DRAM traffic per step: 4 B per synapse, the weights of the
-// sources that fired, the ring slot written (8 B per neuron); the bitmap words
-// come from L2.
+// overflow and at the end into the block's hit list in global memory (room
+// for every entry of the block), every lane loading all its weights before it
+// stores any.  A warp done with a chunk arrives on the slot's "empty"
+// mbarrier; one producer warp waits for it and refills the slot with the
+// chunk dsl_ring places later.  Consumer warps drift apart by up to
+// dsl_ring - 1 chunks, and no block-wide barrier separates the delays.  The
+// sums are not held during the sweep, so the slots get all the shared memory
+// (six at 1M neurons instead of three next to the sums): after the sweep the
+// block adds its hit list into 64-bit fixed-point sums in the slots' bytes
+// (weight x 2^32; integer addition does not depend on order, so the result is
+// deterministic, and exact for weights >= 2^-8).  DRAM traffic per step: 4 B
+// per synapse, per synapse whose source fired its weight and 16 B of hit
+// list (written, then read back, mostly from L2), the ring slot written (8 B
+// per neuron); the bitmap words come from L2.
 // Every wait is bounded: a thread that gives up sets error bit 2 and the
 // block's abort flag; the block then waits (bounded) for its copies in flight
 // and leaves without writing its columns.
@@ -248,10 +254,9 @@ __device__ __forceinline__ void dsl_issue(const PullArgs& a, int s1, int4 m, uin
     nn_bulk_g2s(dst + a.dsl_slotw, a.dsl_ent + m.x, be, bar);
 }
 
-// Add a warp's queued hits {entry, word}: each lane loads its weights, then
-// adds them to the columns' sums.
-__device__ __forceinline__ void dsl_drain(const uint2* q, int cnt, int lane, const float* w,
-                                          unsigned long long* acc_e, unsigned long long* acc_i)
+// Move a warp's queued hits {entry, word} to the block's hit list: each lane
+// loads its weights, then stores {word, weight bits} pairs at out[0, cnt).
+__device__ __forceinline__ void dsl_flush(const uint2* q, int cnt, int lane, const float* w, uint2* out)
 {
     constexpr int PER = DSL_HITCAP / 32;
     uint32_t ew[PER];
@@ -269,10 +274,7 @@ __device__ __forceinline__ void dsl_drain(const uint2* q, int cnt, int lane, con
     }
 #pragma unroll
     for (int k = 0; k < PER; ++k)
-        if (lane + 32 * k < cnt) {
-            const uint32_t col = (ew[k] >> 17) & 0x3fffu;
-            atomicAdd(((ew[k] >> 31) ? acc_i : acc_e) + col, (unsigned long long)llrintf(wv[k] * (float)DSL_FIX));
-        }
+        if (lane + 32 * k < cnt) out[lane + 32 * k] = make_uint2(ew[k], __float_as_uint(wv[k]));
 }
 
 __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(PullArgs a)
@@ -280,14 +282,17 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
     extern __shared__ __align__(128) unsigned char dsl_smem[];
     const int R = a.dsl_ring, SW = a.dsl_slotw, SL = a.dsl_slotw + DSL_CHUNK;  // slot: bitmap words, entries
     uint32_t* ring = reinterpret_cast<uint32_t*>(dsl_smem);
-    unsigned long long* acc_e = reinterpret_cast<unsigned long long*>(ring + (size_t)R * SL);
+    // after the sweep the slots hold the sums
+    unsigned long long* acc_e = reinterpret_cast<unsigned long long*>(dsl_smem);
     unsigned long long* acc_i = acc_e + a.dsl_cols;
-    uint2* hitq = reinterpret_cast<uint2*>(acc_i + a.dsl_cols);  // [DSL_WARPS][DSL_HITCAP]
+    uint2* hitq = reinterpret_cast<uint2*>(
+        dsl_smem + max((size_t)R * SL * 4, (size_t)a.dsl_cols * 16));  // [DSL_WARPS][DSL_HITCAP]
     int4* tab = reinterpret_cast<int4*>(hitq + DSL_WARPS * DSL_HITCAP);
     uint64_t* full = reinterpret_cast<uint64_t*>(tab + a.dsl_cmax);
     uint64_t* empty = full + R;
     int* last = reinterpret_cast<int*>(empty + R);  // last chunk issued into a slot
     __shared__ volatile int abort_flag;
+    __shared__ int hit_count;  // entries of the block's hit list
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint64_t t1 = *a.base + (uint64_t)a.q + 1;
     const int s1 = (int)(t1 % (uint64_t)a.D);
@@ -298,10 +303,12 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
     const int32_t* cp = a.dsl_cptr + (size_t)blockIdx.x * (a.dsl_dmax + 1);
     const int cfirst = cp[0];
     const int C = dlast >= 1 ? cp[dlast] - cfirst : 0;
-    for (int k = tid; k < a.dsl_cols; k += blockDim.x) acc_e[k] = acc_i[k] = 0ull;
     for (int c = tid; c < C; c += blockDim.x) tab[c] = a.dsl_chunk[cfirst + c];
+    // the block's hit list starts at its first entry: it has room for every entry
+    uint2* hits = a.dsl_hits + (C > 0 ? a.dsl_chunk[cfirst].x : 0);
     if (tid == 0) {
         abort_flag = 0;
+        hit_count = 0;
         for (int r = 0; r < R; ++r) {
             nn_mbar_init(&full[r], 1);
             nn_mbar_init(&empty[r], DSL_WARPS);
@@ -383,8 +390,11 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
                     const unsigned b = __ballot_sync(0xffffffffu, h);
                     if (!b) continue;
                     if (hcnt + __popc(b) > DSL_HITCAP) {
+                        int hb = 0;
+                        if (lane == 0) hb = atomicAdd(&hit_count, hcnt);
+                        hb = __shfl_sync(0xffffffffu, hb, 0);
                         __syncwarp();
-                        dsl_drain(hq, hcnt, lane, a.dsl_w, acc_e, acc_i);
+                        dsl_flush(hq, hcnt, lane, a.dsl_w, hits + hb);
                         __syncwarp();
                         hcnt = 0;
                     }
@@ -401,8 +411,11 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
             }
         }
         if (!abort_flag && hcnt > 0) {
+            int hb = 0;
+            if (lane == 0) hb = atomicAdd(&hit_count, hcnt);
+            hb = __shfl_sync(0xffffffffu, hb, 0);
             __syncwarp();
-            dsl_drain(hq, hcnt, lane, a.dsl_w, acc_e, acc_i);
+            dsl_flush(hq, hcnt, lane, a.dsl_w, hits + hb);
         }
     }
     __syncthreads();
@@ -414,6 +427,17 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
         }
         return;
     }
+    // every staged chunk was consumed, so no copy into the slots is pending:
+    // sum the hit list (written by this block, read back through L2) into
+    // the slots' bytes
+    for (int k = tid; k < a.dsl_cols; k += blockDim.x) acc_e[k] = acc_i[k] = 0ull;
+    __syncthreads();
+    for (int i = tid; i < hit_count; i += blockDim.x) {
+        const uint2 h = __ldcg(hits + i);
+        atomicAdd(((h.x >> 31) ? acc_i : acc_e) + ((h.x >> 17) & 0x3fffu),
+                  (unsigned long long)llrintf(__uint_as_float(h.y) * (float)DSL_FIX));
+    }
+    __syncthreads();
     float2* out = reinterpret_cast<float2*>(a.ring + (size_t)(t1 % (uint64_t)a.D) * a.n_pad * 2);
     for (int k = tid; k < k1 - k0; k += blockDim.x)
         out[k0 + k] = make_float2((float)((double)(long long)acc_e[k] / DSL_FIX),
@@ -474,25 +498,92 @@ __global__ void k_dsl_fill(const int64_t* col_ptr, const uint32_t* csc_src, cons
 
 // ... and packed chunk by chunk into entry words (each chunk padded with
 // zero entries to a multiple of four); ustart: the chunk's first entry in the
-// bucketed arrays.
-__global__ void k_dsl_pack(const int4* chunk, const int32_t* ustart, int nchunks, const uint32_t* src,
-                           const uint16_t* col, const float* w, uint32_t* ent, float* wout)
+// bucketed arrays.  Within a chunk the entries are dealt to positions so that
+// the 32 lanes of one lookup of k_deliver_pull_sliced read 32 different
+// shared-memory banks: entries are ranked within their bank (bank = bitmap
+// word & 31), the sequence "rank 0 of every bank, rank 1 of every bank, ..."
+// is formed, and its element j goes to the j-th position in lookup order
+// (dsl_lookup_rank).  While every bank still has entries, each lookup reads
+// one word per bank.  A warp's lookup q reads positions
+// 4 (32 h + lane) + c with h = warp + 16 (q / 4), c = q % 4.  The order of
+// entries does not change the fixed-point sums.
+__device__ __forceinline__ int dsl_lookup_rank(int p, int n)
 {
+    const int h = p >> 7, c = p & 3;
+    int r = 128 * h + ((p >> 2) & 31);
+    for (int cc = 0; cc < c; ++cc) r += min(max((n - 128 * h - cc + 3) >> 2, 0), 32);
+    return r;
+}
+
+constexpr int DSL_PACK_THREADS = 256;
+
+__global__ void __launch_bounds__(DSL_PACK_THREADS) k_dsl_pack(const int4* chunk, const int32_t* ustart,
+                                                               int nchunks, const uint32_t* src,
+                                                               const uint16_t* col, const float* w,
+                                                               uint32_t* ent, float* wout)
+{
+    constexpr int NW = DSL_PACK_THREADS / 32;
+    __shared__ uint32_t s_word[DSL_CHUNK];
+    __shared__ uint16_t s_rank[DSL_CHUNK];  // rank of the entry within its bank
+    __shared__ uint16_t s_pos[DSL_CHUNK];   // position of lookup-order index j
+    __shared__ int s_cw[NW][32];            // per warp: entries per bank, then the warp's first rank
+    __shared__ int s_cnt[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const int4 m = chunk[c];
         const int us = ustart[c];
-        const int padded = (m.y + 3) & ~3;
-        for (int i = threadIdx.x; i < padded; i += blockDim.x) {
-            uint32_t word = 0u;
-            float wv = 0.0f;
-            if (i < m.y) {
-                const uint32_t sw = src[us + i];
-                word = ((sw & 0x7fffffffu) - (uint32_t)m.z * 32u) | ((uint32_t)col[us + i] << 17) | (sw & 0x80000000u);
-                wv = w[us + i];
-            }
-            ent[m.x + i] = word;
-            wout[m.x + i] = wv;
+        const int n = m.y;
+        const int padded = (n + 3) & ~3;
+        for (int i = tid; i < n; i += DSL_PACK_THREADS) {
+            const uint32_t sw = src[us + i];
+            s_word[i] = ((sw & 0x7fffffffu) - (uint32_t)m.z * 32u) | ((uint32_t)col[us + i] << 17) |
+                        (sw & 0x80000000u);
         }
+        for (int p = tid; p < n; p += DSL_PACK_THREADS) s_pos[dsl_lookup_rank(p, n)] = (uint16_t)p;
+        if (tid < NW * 32) s_cw[tid >> 5][tid & 31] = 0;
+        __syncthreads();
+        // rank within the bank: warp k ranks entries [k per, (k + 1) per) in
+        // order, 32 at a time (peers with the same bank by __match_any_sync)
+        const int per = ((n + NW - 1) / NW + 31) & ~31;
+        for (int i0 = warp * per; i0 < min(n, (warp + 1) * per); i0 += 32) {
+            const int i = i0 + lane;
+            const uint32_t bank = i < n ? (s_word[i] >> 5) & 31u : 32u + (uint32_t)lane;
+            const unsigned peers = __match_any_sync(0xffffffffu, bank);
+            if (i < n) s_rank[i] = (uint16_t)(s_cw[warp][bank] + __popc(peers & ((1u << lane) - 1u)));
+            __syncwarp();
+            if (i < n && (__ffs(peers) - 1) == lane) s_cw[warp][bank] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        if (tid < 32) {
+            int acc = 0;
+            for (int k = 0; k < NW; ++k) {
+                const int t = s_cw[k][tid];
+                s_cw[k][tid] = acc;
+                acc += t;
+            }
+            s_cnt[tid] = acc;
+        }
+        __syncthreads();
+        for (int i = tid; i < n; i += DSL_PACK_THREADS) {
+            const uint32_t word = s_word[i];
+            const int bank = (int)((word >> 5) & 31u);
+            const int r = s_rank[i] + s_cw[i / per][bank];
+            int j = 0;
+#pragma unroll 8
+            for (int b = 0; b < 32; ++b) {
+                const int cb = s_cnt[b];
+                j += min(cb, r) + (b < bank && cb > r ? 1 : 0);
+            }
+            const int p = s_pos[j];
+            ent[m.x + p] = word;
+            wout[m.x + p] = w[us + i];
+        }
+        for (int p = n + tid; p < padded; p += DSL_PACK_THREADS) {
+            ent[m.x + p] = 0u;
+            wout[m.x + p] = 0.0f;
+        }
+        __syncthreads();
     }
 }
 
@@ -960,7 +1051,7 @@ static PullArgs pull_args(nn_sim* s, int q)
     a.q = q;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
     a.dsl_chunk = s->dsl_chunk; a.dsl_cptr = s->dsl_cptr;
-    a.dsl_ent = s->dsl_ent; a.dsl_w = s->dsl_w;
+    a.dsl_ent = s->dsl_ent; a.dsl_w = s->dsl_w; a.dsl_hits = s->dsl_hits;
     a.dsl_cols = s->dsl_cols; a.dsl_ring = s->dsl_ring; a.dsl_slotw = s->dsl_slotw;
     a.dsl_cmax = s->dsl_cmax; a.dsl_dmax = s->dsl_dmax;
     a.err = s->err;
@@ -968,12 +1059,12 @@ static PullArgs pull_args(nn_sim* s, int q)
 }
 
 // Dynamic shared memory of k_deliver_pull_sliced: the slots (slotw bitmap
-// words and a chunk of entries each), two 64-bit sums per column, the warps'
-// hit queues, the block's chunk table, and per slot two mbarriers (full,
-// empty) and the last chunk issued.
+// words and a chunk of entries each) during the sweep, the same bytes as two
+// 64-bit sums per column after it; the warps' hit queues, the block's chunk
+// table, and per slot two mbarriers (full, empty) and the last chunk issued.
 static size_t dsl_smem_bytes(int ring, int slotw, int cols, int cmax)
 {
-    return (size_t)ring * (slotw + DSL_CHUNK) * 4 + (size_t)cols * 16 + (size_t)DSL_WARPS * DSL_HITCAP * 8 +
+    return std::max((size_t)ring * (slotw + DSL_CHUNK) * 4, (size_t)cols * 16) + (size_t)DSL_WARPS * DSL_HITCAP * 8 +
            (size_t)cmax * 16 + (size_t)ring * 20;
 }
 
@@ -1088,7 +1179,7 @@ static void free_network(nn_sim* s)
 {
     nn_release(s->row_ptr); nn_release(s->col); nn_release(s->weight); nn_release(s->delay);
     nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
-    nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w);
+    nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w); nn_release(s->dsl_hits);
     s->nnz = 0;
 }
 
@@ -1126,7 +1217,7 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
 // |weight|).  The host cuts each (block, delay) run into chunks from the
 // bucket counts; the entries are first placed by bucket, then packed chunk by
 // chunk.  NN_PULL_UNSLICED=1 keeps the warp-per-column kernel (for
-// comparisons).
+// comparisons); NN_PULL_RING=r caps the slots at r (2 .. DSL_MAX_RING).
 static nn_status build_sliced(nn_sim* s)
 {
     nn_ctx* ctx = s->ctx;
@@ -1218,6 +1309,7 @@ static nn_status build_sliced(nn_sim* s)
     }
     // slots: as many as fit, up to DSL_MAX_RING (at least two)
     int ring = DSL_MAX_RING;
+    if (const char* r = std::getenv("NN_PULL_RING")) ring = std::max(2, std::min(DSL_MAX_RING, std::atoi(r)));
     while (ring >= 2 && dsl_smem_bytes(ring, slotw, cols, cmax) > (size_t)smem_max) --ring;
     if (st != NN_OK || pos > s->nnz || ppos >= INT32_MAX || chunks.empty() || ring < 2) {
         cudaFree(cnt);
@@ -1239,6 +1331,7 @@ static nn_status build_sliced(nn_sim* s)
     if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_cptr, cptr.size());
     if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_ent, (size_t)ppos);
     if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_w, (size_t)ppos);
+    if (st == NN_OK) st = nn_alloc(ctx, &s->dsl_hits, (size_t)ppos);
     if (st == NN_OK)
         st = nn_cuda_check(ctx, nn_copy_sync(ctx, s->dsl_chunk, chunks.data(), sizeof(int4) * chunks.size(),
                                              cudaMemcpyHostToDevice), "build_sliced");
@@ -1255,7 +1348,7 @@ static nn_status build_sliced(nn_sim* s)
     }
     if (st == NN_OK) {
         const int nc = (int)chunks.size();
-        k_dsl_pack<<<std::min(nc, ctx->num_sms * 16), 256, 0, ctx->stream>>>(s->dsl_chunk, d_ustart, nc, t_src, t_col,
+        k_dsl_pack<<<std::min(nc, ctx->num_sms * 8), DSL_PACK_THREADS, 0, ctx->stream>>>(s->dsl_chunk, d_ustart, nc, t_src, t_col,
                                                                             t_w, s->dsl_ent, s->dsl_w);
         st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_pack");
     }
@@ -1271,7 +1364,7 @@ static nn_status build_sliced(nn_sim* s)
     cudaFree(t_w);
     cudaFree(d_ustart);
     if (st != NN_OK) {
-        nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w);
+        nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w); nn_release(s->dsl_hits);
         return st;
     }
     s->dsl_cols = cols;
@@ -1313,7 +1406,7 @@ static nn_status after_network(nn_sim* s)
 {
     drop_graph(s);
     nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
-    nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w);
+    nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w); nn_release(s->dsl_hits);
     if (s->cfg.delivery == NN_DELIVERY_PULL) NN_TRY(build_csc(s));
     return NN_OK;
 }
