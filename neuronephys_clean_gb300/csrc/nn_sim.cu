@@ -505,8 +505,8 @@ __global__ void k_dsl_fill(const int64_t* col_ptr, const uint32_t* csc_src, cons
 // is formed, and its element j goes to the j-th position in lookup order
 // (dsl_lookup_rank).  While every bank still has entries, each lookup reads
 // one word per bank.  A warp's lookup q reads positions
-// 4 (32 h + lane) + c with h = warp + 16 (q / 4), c = q % 4.  The order of
-// entries does not change the fixed-point sums.
+// 4 (32 h + lane) + c with h = warp + DSL_WARPS (q / 4), c = q % 4.  The
+// order of entries does not change the fixed-point sums.
 __device__ __forceinline__ int dsl_lookup_rank(int p, int n)
 {
     const int h = p >> 7, c = p & 3;
