@@ -200,8 +200,8 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
 // ordered by delay and, within a delay, by source bucket (DSL_BUCKET_WORDS
 // bitmap words = 16,384 consecutive source neurons), and cut into chunks of
 // at most DSL_CHUNK entries that span at most DSL_SPAN buckets.  An entry is
-// one 32-bit word: the source's offset from the chunk's first bucket (17
-// bits), the column offset within the block (14 bits) and the inhibitory bit.
+// one 32-bit word: the source's offset from the chunk's first bucket (18
+// bits), the column offset within the block (13 bits) and the inhibitory bit.
 // A chunk of delay d needs only its buckets' words of the spike bitmap of step
 // t + 1 - d; two bulk copies stage those words (from L2) and the chunk's
 // entries (from DRAM) into one of dsl_ring shared-memory slots, completing on
@@ -228,17 +228,17 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
 // and leaves without writing its columns.
 constexpr int DSL_THREADS = 512;                  // consumer threads (plus one producer warp)
 constexpr int DSL_WARPS = DSL_THREADS / 32;
-constexpr int DSL_EPT = 8;                        // entries per consumer thread and chunk
+constexpr int DSL_EPT = 16;                       // entries per consumer thread and chunk
 constexpr int DSL_CHUNK = DSL_EPT * DSL_THREADS;  // entries per chunk at most
 constexpr int DSL_BUCKET_WORDS = 512;             // bitmap words per source bucket
-constexpr int DSL_SPAN = 8;                       // buckets per chunk at most: source offsets below 2^17
+constexpr int DSL_SPAN = 16;                      // buckets per chunk at most: source offsets below 2^18
 constexpr int DSL_MAX_RING = 6;                   // slots at most
 constexpr int DSL_HITCAP = 128;                   // hits a warp's queue holds
-constexpr int DSL_MAX_COLS = 16384;               // 14-bit column offsets
+constexpr int DSL_MAX_COLS = 8192;                // 13-bit column offsets
 constexpr int DSL_MAX_DELAY = 64;
 constexpr double DSL_FIX = 4294967296.0;  // 2^32
 constexpr uint32_t DSL_WAIT_LIMIT = 1u << 22;
-static_assert(DSL_SPAN * DSL_BUCKET_WORDS * 32 <= (1 << 17), "source offsets take 17 bits");
+static_assert(DSL_SPAN * DSL_BUCKET_WORDS * 32 <= (1 << 18), "source offsets take 18 bits");
 
 // Stage chunk m = {first entry, entries, first word, words << 8 | delay}: its
 // bitmap words of the row of step t + 1 - d, then its entries (a multiple of
@@ -367,7 +367,7 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
             if (m.y == DSL_CHUNK) {
 #pragma unroll
                 for (int q = 0; q < DSL_EPT; ++q) {
-                    const uint32_t wv = bm[(ew[q] >> 5) & 0xfffu];
+                    const uint32_t wv = bm[(ew[q] >> 5) & 0x1fffu];
                     hit |= __funnelshift_r(wv, wv, ew[q] - (uint32_t)q) & (1u << q);
                 }
             } else {
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
                     const int i = 4 * (tid + DSL_THREADS * (q / 4)) + (q % 4);
                     const bool in = i < m.y;
                     const uint32_t e = in ? ew[q] : 0u;
-                    const uint32_t wv = bm[(e >> 5) & 0xfffu];
+                    const uint32_t wv = bm[(e >> 5) & 0x1fffu];
                     hit |= __funnelshift_r(wv, wv, e - (uint32_t)q) & (in ? (1u << q) : 0u);
                 }
             }
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
     __syncthreads();
     for (int i = tid; i < hit_count; i += blockDim.x) {
         const uint2 h = __ldcg(hits + i);
-        atomicAdd(((h.x >> 31) ? acc_i : acc_e) + ((h.x >> 17) & 0x3fffu),
+        atomicAdd(((h.x >> 31) ? acc_i : acc_e) + ((h.x >> 18) & 0x1fffu),
                   (unsigned long long)llrintf(__uint_as_float(h.y) * (float)DSL_FIX));
     }
     __syncthreads();
@@ -516,6 +516,7 @@ __device__ __forceinline__ int dsl_lookup_rank(int p, int n)
 }
 
 constexpr int DSL_PACK_THREADS = 256;
+constexpr int DSL_PACK_SMEM = DSL_CHUNK * 8;
 
 __global__ void __launch_bounds__(DSL_PACK_THREADS) k_dsl_pack(const int4* chunk, const int32_t* ustart,
                                                                int nchunks, const uint32_t* src,
@@ -523,9 +524,12 @@ __global__ void __launch_bounds__(DSL_PACK_THREADS) k_dsl_pack(const int4* chunk
                                                                uint32_t* ent, float* wout)
 {
     constexpr int NW = DSL_PACK_THREADS / 32;
-    __shared__ uint32_t s_word[DSL_CHUNK];
-    __shared__ uint16_t s_rank[DSL_CHUNK];  // rank of the entry within its bank
-    __shared__ uint16_t s_pos[DSL_CHUNK];   // position of lookup-order index j
+    // dynamic shared memory (DSL_PACK_SMEM bytes): the chunk's words, the rank
+    // of each entry within its bank, the position of lookup-order index j
+    extern __shared__ __align__(16) unsigned char pack_smem[];
+    uint32_t* s_word = reinterpret_cast<uint32_t*>(pack_smem);
+    uint16_t* s_rank = reinterpret_cast<uint16_t*>(s_word + DSL_CHUNK);
+    uint16_t* s_pos = s_rank + DSL_CHUNK;
     __shared__ int s_cw[NW][32];            // per warp: entries per bank, then the warp's first rank
     __shared__ int s_cnt[32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -536,7 +540,7 @@ __global__ void __launch_bounds__(DSL_PACK_THREADS) k_dsl_pack(const int4* chunk
         const int padded = (n + 3) & ~3;
         for (int i = tid; i < n; i += DSL_PACK_THREADS) {
             const uint32_t sw = src[us + i];
-            s_word[i] = ((sw & 0x7fffffffu) - (uint32_t)m.z * 32u) | ((uint32_t)col[us + i] << 17) |
+            s_word[i] = ((sw & 0x7fffffffu) - (uint32_t)m.z * 32u) | ((uint32_t)col[us + i] << 18) |
                         (sw & 0x80000000u);
         }
         for (int p = tid; p < n; p += DSL_PACK_THREADS) s_pos[dsl_lookup_rank(p, n)] = (uint16_t)p;
@@ -1347,9 +1351,13 @@ static nn_status build_sliced(nn_sim* s)
         st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_fill");
     }
     if (st == NN_OK) {
+        st = nn_cuda_check(ctx, cudaFuncSetAttribute(k_dsl_pack, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     DSL_PACK_SMEM), "cudaFuncSetAttribute");
+    }
+    if (st == NN_OK) {
         const int nc = (int)chunks.size();
-        k_dsl_pack<<<std::min(nc, ctx->num_sms * 8), DSL_PACK_THREADS, 0, ctx->stream>>>(s->dsl_chunk, d_ustart, nc, t_src, t_col,
-                                                                            t_w, s->dsl_ent, s->dsl_w);
+        k_dsl_pack<<<std::min(nc, ctx->num_sms * 8), DSL_PACK_THREADS, DSL_PACK_SMEM, ctx->stream>>>(
+            s->dsl_chunk, d_ustart, nc, t_src, t_col, t_w, s->dsl_ent, s->dsl_w);
         st = nn_cuda_check(ctx, cudaGetLastError(), "k_dsl_pack");
     }
     const size_t smem = dsl_smem_bytes(ring, slotw, cols, cmax);
