@@ -8,15 +8,20 @@ weights, delays U{1..20} steps, 20 % inhibitory, drive U[6, 12] uA/cm^2,
 paracrine field on a 128^3 grid solved every 100 steps by Jacobi-PCG to a
 1e-6 relative residual.  All inputs are seeded synthetic data.
 
-One bench "step" is one paracrine period: 100 simulation timesteps (neuron
-update + spike delivery, replayed from a CUDA graph) plus one field solve, so
-``--steps 10`` covers the workload's 1,000 timesteps.
+One bench "step" is the workload's full run: 1,000 simulation timesteps
+(10 paracrine periods of 100 timesteps, each replayed from a CUDA graph, plus
+10 field solves).
 
 Output: one JSON line (rank 0).  ``value`` is neuron-steps/s of the device-
 resident path; ``e2e`` is the same metric through the C-ABI entry point that
 takes host state buffers (host<->device copies inside the timed region).
-``--impl reference`` times the CPU oracle port of the same step on the host
-cores instead (the reference has no runnable CPU implementation of the path).
+``parity`` compares the GPU with the FP64 oracle over 50 timesteps started
+from the GPU's state inside a population burst (after the timed region), and
+``cpu_baseline`` is that oracle's time on the host cores.
+``--impl reference`` times the CPU oracle port of the same workload on the
+host cores instead (the reference has no runnable CPU implementation of the
+path); it builds the network and initial state with the oracle's own
+generators (bit-exact to the device ones) and loads no GPU code.
 Multi-GPU (torchrun): replicas only -- every rank simulates its own copy, no
 data-path collective; value = all ranks' neuron-steps / max time.
 """
@@ -177,7 +182,7 @@ class ClockSampler:
 
 # --------------------------------------------------------------- our arm ---
 
-def build_sim(nn, ctx, wl: dict, seed: int = 1, delivery: int = 0):
+def build_sim(nn, ctx, wl: dict, seed: int = 1, delivery: int = 0, raster: int = 0):
     c = nn.default_config(wl["n"])
     c.delivery = delivery
     c.seed = seed
@@ -188,6 +193,7 @@ def build_sim(nn, ctx, wl: dict, seed: int = 1, delivery: int = 0):
     c.par_decay = wl["par_decay"]
     c.par_rtol = 1e-6
     c.par_max_iter = 5000
+    c.raster_capacity = raster
     s = nn.Simulation(ctx, c)
     if wl["kind"] == "gauss":
         sp = nn.default_net_spec(nn.NN_NET_GAUSS)
@@ -209,7 +215,8 @@ def build_sim(nn, ctx, wl: dict, seed: int = 1, delivery: int = 0):
 def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     import neuronephys_clean_gb300 as nn
     ctx = nn.Context(local_rank)
-    sim = build_sim(nn, ctx, wl)
+    # the raster records the parity window's spikes (restarted before it)
+    sim = build_sim(nn, ctx, wl, raster=2_000_000 if args.cpu_baseline else 0)
     P = wl["total_steps"]  # timesteps per bench step: one full run of the workload
     n = wl["n"]
     # settle: start the timed region in steady tonic firing, not at rest
@@ -301,10 +308,7 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded counter-based generators)",
-        "config": {"workload": wl["workload"], "neurons": n, "synapses": nnz, "timesteps_per_step": P,
-                   "dt_ms": 0.01, "grid": wl["grid"], "delivery": "push", "parallelism": "replicas",
-                   "l2": f"inputs larger than L2 (CSR {nnz * 9 / 1e9:.1f} GB, ring "
-                         f"{(wl['dmax'] + 1) * n * 8 / 1e6:.0f} MB, state {n * 28 / 1e6:.0f} MB per step)"},
+        "config": workload_config(wl, nnz),
         "synaptic_events_per_s": events / seconds if seconds else None,
         "spikes_in_timed_region": spikes,
         "cg": {"iterations_last_solve": st.iterations, "relres_last_solve": st.relres,
@@ -317,57 +321,69 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "e2e": e2e,
     }
     if args.cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sim, wl, args)
+        line["parity"], line["cpu_baseline"] = parity_and_cpu_baseline(sim, wl, args)
     sim.close()
     ctx.close()
     return line
 
 
+def workload_config(wl: dict, nnz: int) -> dict:
+    """The `config` object of both arms' lines for a single-network workload."""
+    n = wl["n"]
+    return {"workload": wl["workload"], "neurons": n, "synapses": int(nnz), "timesteps_per_step": wl["total_steps"],
+            "dt_ms": 0.01, "grid": wl["grid"], "delivery": "push", "parallelism": "replicas",
+            "l2": f"inputs larger than L2 (CSR {nnz * 9 / 1e9:.1f} GB, ring "
+                  f"{(wl['dmax'] + 1) * n * 8 / 1e6:.0f} MB, state {n * 28 / 1e6:.0f} MB per step)"}
+
+
 # ---------------------------------------------------------- CPU baseline ---
 
-def cpu_baseline_sample(wl: dict, net_arrays, state6, i_drive, is_inh, seed: int, steps: int,
-                        solve: bool, vox=None) -> dict:
-    """Time the FP64 oracle port of the same step (OpenMP over the host cores)."""
+def parity_and_cpu_baseline(sim, wl: dict, args) -> tuple[dict, dict]:
+    """The GPU against the FP64 oracle at the benchmarked configuration.
+
+    Both start from the GPU's state at a period boundary inside a population
+    burst (neuron fields, delay ring and step counter: the complete state a
+    step depends on) and advance args.parity_steps timesteps (>= 20, so that
+    spikes of the window arrive through the delay ring within it).  Reported:
+    raster equality (one-step shifts of crossings within 0.01 mV of the
+    threshold counted apart), the per-neuron trajectory criterion of
+    oracle/parity.py and the largest relative V error away from spikes.  The
+    oracle's time for the window is the CPU baseline (OpenMP over the host
+    cores), plus one PCG solve of the 128^3 field amortised over its period."""
     import oracle
-    rp, col, w, d = net_arrays
-    n = wl["n"]
-    net = oracle.CSR(rp, col, w, d)
+    from oracle.parity import find_burst, window_parity
+    n, k = wl["n"], args.parity_steps
+    P = wl["timescale"]
+    periods = find_burst(sim, P, n)
+    res = window_parity(sim, k)
+    o, t_steps, t0 = res.pop("_oracle"), res.pop("_t_oracle_s"), res["start_step"]
+    parity = dict(res, settle_periods_to_burst=periods,
+                  tolerance="V, m, h, n within 1e-4 relative (floors 1 mV / 1e-3) away from spikes, within a 1 us "
+                            "spike-time shift in a spike; rasters identical except one-step shifts of crossings "
+                            "within 0.01 mV of the threshold (their neurons and targets held to 5e-2 instead)",
+                  oracle="FP64 C restatement (oracle/oracle.c), started from the GPU's neuron fields, delay ring "
+                         "and step counter")
     g = wl["grid"]
-    sim = oracle.Sim(net, is_inh, i_drive, seed, max(1, wl["dmax"]) + 1, state6, vox=vox,
-                     grid_cells=g ** 3 if vox is not None else 0)
-    sim.step()  # touch memory
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        sim.step()
-    t_steps = time.perf_counter() - t0
     t_solve = 0.0
-    if solve:
+    if g:
+        # the period's field solve: b = u + deposits of the window's spikes,
+        # warm-started from u, as the simulation forms it
         dt_s = wl["timescale"] * 0.01 * 1e-3
         alpha, beta = dt_s * wl["par_D"] * g * g, dt_s * wl["par_decay"]
-        b = sim.src if sim.src is not None else np.zeros(g ** 3)
-        b = b + 1e-3
+        vox = oracle.voxels(sim.get_field("X"), sim.get_field("Y"), sim.get_field("Z"), g)
+        u = sim.density().astype(np.float64)
+        fired = np.fromiter((j for (_, j) in o.margins), np.int64, len(o.margins))
+        b = u + np.bincount(vox[fired], minlength=g ** 3)
         t1 = time.perf_counter()
-        oracle.pcg7(b, np.zeros(g ** 3), (g, g, g), alpha, beta, rtol=1e-6)
+        oracle.pcg7(b, u, (g, g, g), alpha, beta, rtol=1e-6)
         t_solve = time.perf_counter() - t1
-    P = wl["timescale"]
-    per_step = t_steps / steps + t_solve / P
-    return {"value": n / per_step, "unit": "neuron-steps/s", "cores": int(oracle.lib().orc_num_threads()),
-            "kind": "port", "t_steps_s": t_steps, "t_solve_s": t_solve,
-            "sample": f"{steps} timesteps of all {n} neurons (FP64 oracle, OpenMP) + one {g}^3 PCG solve "
-                      f"amortised over {P} timesteps"}
-
-
-def cpu_baseline(sim, wl: dict, args) -> dict:
-    rp, col, w, d, inh = sim.get_network()
-    state6 = np.stack([sim.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")])
-    x, y, z = (sim.get_field(k) for k in ("X", "Y", "Z"))
-    g = wl["grid"]
-    ix = np.clip((x * np.float32(g)).astype(np.int32), 0, g - 1)
-    iy = np.clip((y * np.float32(g)).astype(np.int32), 0, g - 1)
-    iz = np.clip((z * np.float32(g)).astype(np.int32), 0, g - 1)
-    vox = (ix + g * (iy + g * iz)).astype(np.int32)
-    return cpu_baseline_sample(wl, (rp, col, w, d), state6, sim.get_field("IDRIVE"), inh, 1, args.cpu_steps, True,
-                               vox)
+    per_step = t_steps / k + t_solve / P
+    cpu = {"value": n / per_step, "unit": "neuron-steps/s", "cores": int(oracle.lib().orc_num_threads()),
+           "kind": "port", "t_steps_s": t_steps, "t_solve_s": t_solve,
+           "sample": f"{k} timesteps of all {n} neurons from the GPU's state at step {t0} inside a population "
+                     f"burst ({parity['spikes_oracle']} spikes delivered; FP64 oracle, OpenMP) + one {g}^3 PCG "
+                     f"solve amortised over {P} timesteps"}
+    return parity, cpu
 
 
 def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | None:
@@ -786,43 +802,91 @@ def run_cg_reference(args, wl: dict, rank: int) -> dict | None:
             "e2e": {"value": ms_solve, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def oracle_network(wl: dict, seed: int):
+    """The workload's network, inhibitory flags, drive and voxels from the
+    oracle's generators, bit-exact to the device generators (tests
+    test_gauss_generator_bit_exact, test_block_generator_bit_exact,
+    test_er_generator_bit_exact, test_init_state_drive_and_types)."""
+    import oracle
+    n = wl["n"]
+    if wl["kind"] == "gauss":
+        net = oracle.gen_gauss(n, wl["k"], wl["sigma"], wl["w_mu"], wl["w_sigma"], wl["dmax"], seed)
+        inh = oracle.inh_flags(n, wl["inh"], True, seed)
+    elif wl["kind"] == "block":
+        net = oracle.gen_block(n, wl["k"], wl["n_regions"], wl["size_sigma"], wl["density_sigma"], wl["dmax"],
+                               wl["w_mu"], wl["w_sigma"], seed)
+        inh = oracle.inh_flags(n, wl["inh"], True, seed)
+    else:
+        net = oracle.gen_er(n, wl["p"], wl["w_max"], seed)
+        inh = oracle.inh_flags(n, wl["inh"], False, seed)
+    idr = oracle.init_drive(n, seed, wl["i_lo"], wl["i_hi"])
+    vox = oracle.voxels(*oracle.lattice_positions(n, seed), wl["grid"]) if wl["grid"] else None
+    return net, inh, idr, vox
+
+
 def run_reference(args, wl: dict, rank: int) -> dict | None:
-    """The reference arm: the CPU oracle port of the same workload, all host threads."""
+    """The reference arm: the CPU oracle port of the same workload on the host
+    cores (OpenMP over all of them).  It loads no GPU code: the network,
+    inhibitory flags, drive and positions come from the oracle's generators,
+    bit-exact to the device ones, and the state starts at rest as the GPU
+    arm's does.  One timed step is a bounded sample of the workload:
+    args.ref_sample_steps timesteps (one paracrine period) of all neurons with
+    spike delivery through the delay ring and the deposits, then the period's
+    PCG solve of the field (b = u + deposits, warm-started from u).  The
+    warm-up samples run on a copy of the initial state and are discarded, so
+    the timed samples simulate the workload from its first step; they contain
+    its first population burst (all neurons spike within a few ms, ~2 ms after
+    the start), the GPU arm's timed region contains later bursts."""
     if rank != 0:
         return None
-    import neuronephys_clean_gb300 as nn
-    # network + initial state come from the same generators (built on the GPU
-    # if one is present, else this arm is unavailable)
-    try:
-        ctx = nn.Context(0)
-    except Exception as e:  # pragma: no cover
-        return {"impl": "reference", "unavailable": f"no device to generate the seeded network: {e}"}
-    sim = build_sim(nn, ctx, wl)
-    rp, col, w, d, inh = sim.get_network()
-    state6 = np.stack([sim.get_field(k) for k in ("V", "M", "H", "N", "GE", "GI")])
-    idr = sim.get_field("IDRIVE")
-    x, y, z = (sim.get_field(k) for k in ("X", "Y", "Z"))
-    g = wl["grid"]
-    vox = (np.clip((x * np.float32(g)).astype(np.int32), 0, g - 1)
-           + g * (np.clip((y * np.float32(g)).astype(np.int32), 0, g - 1)
-                  + g * np.clip((z * np.float32(g)).astype(np.int32), 0, g - 1))).astype(np.int32)
-    sim.close()
-    ctx.close()
-    times = []
-    res = None
-    for i in range(args.warmup + args.steps):
-        res = cpu_baseline_sample(wl, (rp, col, w, d), state6, idr, inh, 1, args.cpu_steps, True, vox)
-        if i >= args.warmup:
-            times.append(wl["n"] / res["value"])
-    per_step = statistics.mean(times)
-    value = wl["n"] / per_step
-    cb = dict(res)
-    cb["value"] = value
+    import oracle
+    seed, n, S = 1, wl["n"], args.ref_sample_steps
+    t0 = time.perf_counter()
+    net, inh, idr, vox = oracle_network(wl, seed)
+    t_gen = time.perf_counter() - t0
+    g, D = wl["grid"], max(1, wl["dmax"]) + 1
+    dt_s = wl["timescale"] * 0.01 * 1e-3
+    alpha, beta = dt_s * wl["par_D"] * g * g, dt_s * wl["par_decay"]
+
+    def new_sim():
+        return oracle.Sim(net, inh, idr, seed, D, oracle.rest_state(n), vox=vox, grid_cells=g ** 3 if g else 0)
+
+    def sample(o, u):
+        spikes = events = 0
+        t = time.perf_counter()
+        for _ in range(S):
+            sp = o.step()
+            spikes += len(sp)
+            events += int((net.row_ptr[sp + 1] - net.row_ptr[sp]).sum()) if len(sp) else 0
+        if g:
+            x, _, _ = oracle.pcg7(u + o.src, u, (g, g, g), alpha, beta, rtol=1e-6)
+            u[:] = x
+            o.src[:] = 0.0
+        return time.perf_counter() - t, spikes, events
+
+    o, u = new_sim(), np.zeros(g ** 3 if g else 0)
+    for _ in range(args.warmup):
+        sample(o, u)
+    o, u = new_sim(), np.zeros(g ** 3 if g else 0)
+    times, spikes, events = [], 0, 0
+    for _ in range(args.steps):
+        dt, sp, ev = sample(o, u)
+        times.append(dt)
+        spikes += sp
+        events += ev
+    per_sample = statistics.mean(times)
+    value = n * S / per_sample
+    cb = {"value": value, "unit": "neuron-steps/s", "cores": int(oracle.lib().orc_num_threads()), "kind": "port",
+          "sample": f"{S} timesteps of all {n} neurons (FP64 oracle, OpenMP, spike delivery through the delay ring) "
+                    f"+ the period's {g}^3 PCG solve, per timed step; {args.steps} consecutive samples from the "
+                    f"initial state ({spikes} spikes, {events} synaptic events); network generation {t_gen:.1f} s "
+                    f"untimed"}
     return {"metric": "neuron-steps/s", "value": value, "unit": "neuron-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * wl["total_steps"] * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sample * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded counter-based generators)", "impl": "reference",
-            "config": {"workload": wl["workload"], "neurons": wl["n"], "timesteps_per_step": wl["total_steps"]},
+            "config": workload_config(wl, len(net.col)),
+            "spikes_in_timed_region": spikes, "synaptic_events_per_s": events / sum(times),
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "neuron-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -836,7 +900,11 @@ def main() -> None:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--settle", type=int, default=2000, help="untimed timesteps before the warm-up")
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=3, help="CG workload: FP64 PCG iterations per CPU sample unit")
+    ap.add_argument("--parity-steps", type=int, default=50,
+                    help="timesteps of the GPU-vs-oracle parity window (and the CPU baseline's sample)")
+    ap.add_argument("--ref-sample-steps", type=int, default=100,
+                    help="reference arm: timesteps per timed sample (one paracrine period)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--delivery-sweep", action="store_true",
                     help="time push / pull spike delivery alone over firing fractions (one JSON line)")
@@ -846,6 +914,11 @@ def main() -> None:
     rank, world, local_rank = dist_env()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
+        if wl.get("kind") == "batch":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the batched workload has no counterpart in "
+                                  "the reference and no CPU port here"}), flush=True)
+            return
         line = (run_cg_reference if wl.get("kind") == "cg" else run_reference)(args, wl, rank)
         if line is not None:
             print(json.dumps(line), flush=True)

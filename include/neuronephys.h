@@ -105,6 +105,13 @@ NN_API void nn_leapfrog_params_reference(nn_leapfrog_params* p, int variant);
  * stream. */
 NN_API nn_status nn_hh_leapfrog_step(nn_ctx* ctx, float* const* vars, int n, float dt,
                                      const nn_leapfrog_params* p, uint64_t seed, uint64_t step);
+/* The same step with the noise draws supplied by the caller: d_z (device,
+ * float[n]) holds one standard normal per neuron, so that white noise =
+ * noise_intensity * z + noise_mean as in src/ephys.cu:88, where z comes from
+ * curand_normal on the neuron's XORWOW state.  A caller that keeps the
+ * reference's curand stream passes its draws here. */
+NN_API nn_status nn_hh_leapfrog_step_z(nn_ctx* ctx, float* const* vars, int n, float dt,
+                                       const nn_leapfrog_params* p, const float* d_z);
 
 /* AtomicCoupling (src/coupling.cuh:17-38, src_wholebrain/coupling.cuh:26-43). */
 typedef struct nn_coupling nn_coupling;
@@ -333,6 +340,14 @@ NN_API nn_status nn_sim_run_host(nn_sim* s, const float* h_state_in, int nsteps,
                                  int64_t* h_spikes);
 /* Current step index and total spikes so far (synchronises). */
 NN_API nn_status nn_sim_counters(nn_sim* s, int64_t* step, int64_t* total_spikes);
+/* Download the delay ring: D = max_delay + 1 slots of n (excitatory,
+ * inhibitory) input pairs, h_ring float[D * n * 2]; slot (t mod D) holds the
+ * input the neurons take at step t.  With the step counter and the neuron
+ * fields it is the complete state a step depends on.  No counterpart in the
+ * reference (its inputs have a one-step delay and live in the SoA table). */
+NN_API nn_status nn_sim_get_ring(nn_sim* s, float* h_ring);
+/* Restart the spike raster: the next recorded spike is entry 0 again. */
+NN_API nn_status nn_sim_reset_raster(nn_sim* s);
 /* Recorded raster (ascending (step, neuron) after sorting on the host). */
 NN_API nn_status nn_sim_get_raster(nn_sim* s, int64_t cap, int32_t* h_step, int32_t* h_neuron,
                                    int64_t* count);

@@ -207,10 +207,16 @@ class HHEphys:
     def get(self, name: str) -> np.ndarray:
         return self.vars[SIM_PARAMS.index(name)].numpy()
 
-    def simulate_ephys(self) -> None:
+    def simulate_ephys(self, z: "DeviceArray | None" = None) -> None:
+        """One step; z (device float[n], optional) supplies the standard
+        normal draws of the noise term instead of the library's stream."""
         table = (C.c_void_p * len(self.vars))(*[v.value for v in self.vars])
-        _check(lib().nn_hh_leapfrog_step(self.ctx.handle, table, self.n, self.dt, C.byref(self.params),
-                                         self.seed, self.step), self.ctx, "SimulateEphys")
+        if z is None:
+            _check(lib().nn_hh_leapfrog_step(self.ctx.handle, table, self.n, self.dt, C.byref(self.params),
+                                             self.seed, self.step), self.ctx, "SimulateEphys")
+        else:
+            _check(lib().nn_hh_leapfrog_step_z(self.ctx.handle, table, self.n, self.dt, C.byref(self.params),
+                                               C.c_void_p(z.value)), self.ctx, "SimulateEphys")
         self.step += 1
 
 
@@ -523,6 +529,17 @@ class Simulation:
         _check(lib().nn_sim_run_host(self.handle, _ptr(state_in), nsteps, _ptr(state_out), C.byref(sp)), self.ctx,
                "run_host")
         return sp.value
+
+    def get_ring(self) -> np.ndarray:
+        """Delay ring as (D, n, 2) float32: slot t mod D holds the (E, I)
+        input of step t."""
+        D = int(self.config.max_delay) + 1
+        out = np.zeros((D, self.config.n, 2), np.float32)
+        _check(lib().nn_sim_get_ring(self.handle, _ptr(out)), self.ctx, "get_ring")
+        return out
+
+    def reset_raster(self) -> None:
+        _check(lib().nn_sim_reset_raster(self.handle), self.ctx, "reset_raster")
 
     def counters(self) -> tuple[int, int]:
         s, t = C.c_int64(), C.c_int64()

@@ -85,6 +85,7 @@ _SIGS = {
     "nn_leapfrog_params_reference": (None, [P(LeapfrogParams), c_int]),
     "nn_hh_leapfrog_step": (c_int, [c_void_p, P(c_void_p), c_int, c_float, P(LeapfrogParams),
                                     c_uint64, c_uint64]),
+    "nn_hh_leapfrog_step_z": (c_int, [c_void_p, P(c_void_p), c_int, c_float, P(LeapfrogParams), c_void_p]),
     "nn_coupling_create": (c_int, [c_void_p, c_int, P(c_void_p)]),
     "nn_coupling_destroy": (c_int, [c_void_p]),
     "nn_coupling_run": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, P(c_int)]),
@@ -120,6 +121,8 @@ _SIGS = {
     "nn_sim_init_state": (c_int, [c_void_p, c_float, c_float, c_float]),
     "nn_sim_step": (c_int, [c_void_p, c_int]),
     "nn_sim_run_host": (c_int, [c_void_p, c_void_p, c_int, c_void_p, P(c_int64)]),
+    "nn_sim_get_ring": (c_int, [c_void_p, c_void_p]),
+    "nn_sim_reset_raster": (c_int, [c_void_p]),
     "nn_sim_counters": (c_int, [c_void_p, P(c_int64), P(c_int64)]),
     "nn_sim_get_raster": (c_int, [c_void_p, c_int64, c_void_p, c_void_p, P(c_int64)]),
     "nn_sim_get_density": (c_int, [c_void_p, c_void_p]),

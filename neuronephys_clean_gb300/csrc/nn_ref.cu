@@ -31,79 +31,135 @@ extern "C" void nn_leapfrog_params_reference(nn_leapfrog_params* p, int variant)
 namespace {
 struct LFVars { float* v[NN_HH_NUM_VARS]; };
 
-// u / (1 - e^{-u}) with an accurate expm1 away from 0 and its series near 0.
-__device__ __forceinline__ float lf_xexprel(float u)
+// Leapfrog_HH (src/ephys.cu:28-96), evaluated in the precision the
+// reference's expressions have.  Its double literals (3.5, 0.1, 0.07, 0.125,
+// 1.0) promote alpha_m, alpha_n, beta_h, the products 0.07 * e^x and
+// 0.125 * e^x, and the output sigmoid to FP64, each rounded to float on
+// assignment; exponentials of float arguments (alpha_h, beta_m, beta_n, the
+// sigmoid's) are FP32 calls; the gate, synapse and membrane updates are FP32
+// (Float = float, src/defines.cuh:50-55).  The expressions keep the
+// reference's operand order, so each rounds as the reference's does.  The
+// removable singularities of alpha_m (V = -35) and alpha_n (V = -50), 0/0 in
+// the reference, take their limits (1 and 0.1) when the FP64 argument is
+// within 1e-9 of them, which no other input changes.
+__device__ __forceinline__ float lf_rate_am(float V)
 {
-    const float u2 = u * u;
-    const float series = 1.0f + u * 0.5f + u2 * (1.0f / 12.0f + u2 * (-1.0f / 720.0f + u2 * (1.0f / 30240.0f)));
-    return fabsf(u) < 0.5f ? series : u / (-expm1f(-u));
+    const double u = 3.5 + 0.1 * V;
+    if (fabs(u) < 1e-9) return 1.0f;
+    return (float)((3.5 + 0.1 * V) / (1 - exp(-3.5 - 0.1 * V)));
 }
 
-__device__ __forceinline__ float lf_cn(float A, float B, float x, float dt)
+__device__ __forceinline__ float lf_rate_an(float V)
 {
-    return (A * dt + (1.0f - dt * 0.5f * (A + B)) * x) / (dt * 0.5f * (A + B) + 1.0f);
+    const double u = -5 - 0.1 * V;
+    if (fabs(u) < 1e-9) return 0.1f;
+    return (float)((-0.5 - 0.01 * V) / (exp(-5 - 0.1 * V) - 1));
 }
 
-// Leapfrog_HH (src/ephys.cu:28-96).  The reference's (3.5+0.1V)/(1-e^{-3.5-0.1V})
-// and (-0.5-0.01V)/(e^{-5-0.1V}-1) are written as u/(1-e^{-u}) forms, which are
-// the same functions without the 0/0 at V = -35 and V = -50.
-__global__ void __launch_bounds__(256) k_leapfrog(LFVars s, int n, float dt, nn_leapfrog_params p, uint64_t seed,
-                                                  uint64_t step)
+template <bool EXT_Z>
+__global__ void __launch_bounds__(256) k_leapfrog(LFVars s, int n, float timestep, nn_leapfrog_params p,
+                                                  uint64_t seed, uint64_t step, const float* __restrict__ z)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float local_in = s.v[NN_HH_LOCAL_IN][i], local_num_in = s.v[NN_HH_LOCAL_COUNT][i];
+        const float Iin = s.v[NN_HH_IIN][i], Inum_in = s.v[NN_HH_ICOUNT][i];
+        const float Ein = s.v[NN_HH_EIN][i], Enum_in = s.v[NN_HH_ECOUNT][i];
+        const float appcur = s.v[NN_HH_APPCUR][i];
         const float V = s.v[NN_HH_V][i], M = s.v[NN_HH_M][i], N = s.v[NN_HH_N][i], H = s.v[NN_HH_H][i];
-        const float LY = s.v[NN_HH_LOCAL_Y][i], IY = s.v[NN_HH_IY][i], EY = s.v[NN_HH_EY][i];
-        const float Am = lf_xexprel(3.5f + 0.1f * V);
-        const float An = 0.1f * lf_xexprel(5.0f + 0.1f * V);
-        const float Ah = 0.07f * expf(-V / 20.0f - 3.0f);
-        const float Bm = 4.0f * expf(-(V + 60.0f) / 18.0f);
-        const float Bn = 0.125f * expf(-(V + 60.0f) / 80.0f);
-        const float Bh = 1.0f / (expf(-3.0f - 0.1f * V) + 1.0f);
-        const float nM = lf_cn(Am, Bm, M, dt), nN = lf_cn(An, Bn, N, dt), nH = lf_cn(Ah, Bh, H, dt);
-        const float lcnt = s.v[NN_HH_LOCAL_COUNT][i], icnt = s.v[NN_HH_ICOUNT][i], ecnt = s.v[NN_HH_ECOUNT][i];
-        const float lT = lcnt > 0.0f ? s.v[NN_HH_LOCAL_IN][i] / lcnt : 0.0f;
-        const float iT = icnt > 0.0f ? s.v[NN_HH_IIN][i] / icnt : 0.0f;
-        const float eT = ecnt > 0.0f ? s.v[NN_HH_EIN][i] / ecnt : 0.0f;
-        const float nLY = lf_cn(p.Ar * lT, p.Ad, LY, dt);
-        const float nIY = lf_cn(p.Ar * iT, p.Ad, IY, dt);
-        const float nEY = lf_cn(p.Ar * eT, p.Ad, EY, dt);
-        const float gna = p.gna * nM * nM * nM * nH;
-        const float n2 = nN * nN;
-        const float gk = p.gk * n2 * n2;
-        const float G = gna + gk + p.gl + p.g_local * nLY + p.g_gaba * nIY + p.g_exc * nEY;
-        const float E = gna * p.ena + gk * p.ek + p.gl * p.el + p.g_local * nLY * p.e_local +
-                        p.g_gaba * nIY * p.e_gaba + p.g_exc * nEY * p.e_exc;
-        const float noise = p.noise_intensity * nn_normal(seed, (uint32_t)i, step) + p.noise_mean;
-        const float app = s.v[NN_HH_APPCUR][i];
-        const float nV = ((noise + app) * dt + E * dt + (1.0f - dt * 0.5f * G) * V) / (1.0f + dt * 0.5f * G);
+        const float local_Y = s.v[NN_HH_LOCAL_Y][i], IY = s.v[NN_HH_IY][i], EY = s.v[NN_HH_EY][i];
+
+        const float Am = lf_rate_am(V);
+        const float An = lf_rate_an(V);
+        const float Ah = (float)(0.07 * expf(-V / 20 - 3));
+        const float Bm = 4 * expf(-(V + 60) / 18);
+        const float Bn = (float)(0.125 * expf(-(V + 60) / 80));
+        const float Bh = (float)(1 / (exp(-3 - 0.1 * V) + 1));
+
+        const float new_M = (Am * timestep + (1 - timestep / 2 * (Am + Bm)) * M) / (timestep / 2 * (Am + Bm) + 1);
+        const float new_N = (An * timestep + (1 - timestep / 2 * (An + Bn)) * N) / (timestep / 2 * (An + Bn) + 1);
+        const float new_H = (Ah * timestep + (1 - timestep / 2 * (Ah + Bh)) * H) / (timestep / 2 * (Ah + Bh) + 1);
+
+        const float Ar = p.Ar, Ad = p.Ad;
+        const float local_T = local_num_in > 0 ? local_in / local_num_in : 0;
+        const float new_local_Y = (Ar * local_T * timestep + (1 - timestep / 2 * (Ar * local_T + Ad)) * local_Y) /
+                                  (timestep / 2 * (Ar * local_T + Ad) + 1);
+        const float I_T = Inum_in > 0 ? Iin / Inum_in : 0;
+        const float new_IY = (Ar * I_T * timestep + (1 - timestep / 2 * (Ar * I_T + Ad)) * IY) /
+                             (timestep / 2 * (Ar * I_T + Ad) + 1);
+        const float E_T = Enum_in > 0 ? Ein / Enum_in : 0;
+        const float new_EY = (Ar * E_T * timestep + (1 - timestep / 2 * (Ar * E_T + Ad)) * EY) /
+                             (timestep / 2 * (Ar * E_T + Ad) + 1);
+
+        // G, E and the membrane update with every rounding explicit, in the
+        // order and fusion the reference kernel has when nvcc builds it for
+        // sm_103a (found by comparing the two kernels' outputs on the same
+        // states: the reference forms E * dt inside a fused multiply-add on
+        // top of the rounded (noise + I_app) * dt; left to the compiler, this
+        // source fused the other product and differed by an ulp in 19 % of
+        // the neurons).  The reference weights the local and excitatory
+        // synapses by g_ampa and the inhibitory one by g_gaba; the whole-brain
+        // variant sets them apart, hence g_local / g_exc.
+        const float gna_m3h = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(p.gna, new_M), new_M), new_M), new_H);
+        const float gk_n4 = __fmul_rn(p.gk, powf(new_N, 4));
+        float G = __fadd_rn(__fadd_rn(gna_m3h, gk_n4), p.gl);
+        G = __fadd_rn(G, __fmul_rn(p.g_local, new_local_Y));
+        G = __fadd_rn(G, __fmul_rn(p.g_gaba, new_IY));
+        G = __fadd_rn(G, __fmul_rn(p.g_exc, new_EY));
+        float E = __fmaf_rn(gna_m3h, p.ena, __fmul_rn(gk_n4, p.ek));
+        E = __fadd_rn(E, __fmul_rn(p.gl, p.el));
+        E = __fadd_rn(E, __fmul_rn(__fmul_rn(p.g_local, new_local_Y), p.e_local));
+        E = __fmaf_rn(__fmul_rn(p.g_gaba, new_IY), p.e_gaba, E);
+        E = __fadd_rn(E, __fmul_rn(__fmul_rn(p.g_exc, new_EY), p.e_exc));
+
+        const float zi = EXT_Z ? z[i] : nn_normal(seed, (uint32_t)i, step);
+        const float white_noise = __fmaf_rn(p.noise_intensity, zi, p.noise_mean);
+        const float half_dt = timestep / 2;
+        float num = __fmaf_rn(E, timestep, __fmul_rn(__fadd_rn(white_noise, appcur), timestep));
+        num = __fmaf_rn(__fmaf_rn(-half_dt, G, 1.0f), V, num);
+        const float nV = __fdiv_rn(num, __fmaf_rn(half_dt, G, 1.0f));
         s.v[NN_HH_V][i] = nV;
-        s.v[NN_HH_M][i] = nM;
-        s.v[NN_HH_N][i] = nN;
-        s.v[NN_HH_H][i] = nH;
-        s.v[NN_HH_LOCAL_Y][i] = nLY;
-        s.v[NN_HH_IY][i] = nIY;
-        s.v[NN_HH_EY][i] = nEY;
-        const float out = p.Tmax / (1.0f + expf(-(nV - p.Vt) / p.Kp));
+        s.v[NN_HH_M][i] = new_M;
+        s.v[NN_HH_N][i] = new_N;
+        s.v[NN_HH_H][i] = new_H;
+        s.v[NN_HH_LOCAL_Y][i] = new_local_Y;
+        s.v[NN_HH_IY][i] = new_IY;
+        s.v[NN_HH_EY][i] = new_EY;
+        const float out = (float)(p.Tmax / (1.0 + expf(-(nV - p.Vt) / p.Kp)));
         s.v[NN_HH_LOCAL_OUTPUT][i] = out;
         s.v[NN_HH_IOUTPUT][i] = out;
         s.v[NN_HH_EOUTPUT][i] = out;
     }
+}
+
+nn_status leapfrog_launch(nn_ctx* ctx, float* const* vars, int n, float dt, const nn_leapfrog_params* p,
+                          uint64_t seed, uint64_t step, const float* d_z, const char* what)
+{
+    if (!ctx || !vars || !p || n < 0) return nn_fail(ctx, NN_ERR_INVALID_ARG, "%s: bad argument", what);
+    if (n == 0) return NN_OK;
+    LFVars s;
+    for (int q = 0; q < NN_HH_NUM_VARS; ++q) {
+        if (!vars[q]) return nn_fail(ctx, NN_ERR_INVALID_ARG, "%s: sim_vars[%d] is NULL", what, q);
+        s.v[q] = vars[q];
+    }
+    const int grid = nn_grid_for(ctx, n, 256, 16);
+    if (d_z) k_leapfrog<true><<<grid, 256, 0, ctx->stream>>>(s, n, dt, *p, seed, step, d_z);
+    else k_leapfrog<false><<<grid, 256, 0, ctx->stream>>>(s, n, dt, *p, seed, step, nullptr);
+    NN_CHECK_LAUNCH(ctx, "k_leapfrog");
+    return NN_OK;
 }
 }  // namespace
 
 extern "C" nn_status nn_hh_leapfrog_step(nn_ctx* ctx, float* const* vars, int n, float dt,
                                          const nn_leapfrog_params* p, uint64_t seed, uint64_t step)
 {
-    if (!ctx || !vars || !p || n < 0) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_hh_leapfrog_step: bad argument");
-    if (n == 0) return NN_OK;
-    LFVars s;
-    for (int q = 0; q < NN_HH_NUM_VARS; ++q) {
-        if (!vars[q]) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_hh_leapfrog_step: sim_vars[%d] is NULL", q);
-        s.v[q] = vars[q];
-    }
-    k_leapfrog<<<nn_grid_for(ctx, n, 256, 16), 256, 0, ctx->stream>>>(s, n, dt, *p, seed, step);
-    NN_CHECK_LAUNCH(ctx, "k_leapfrog");
-    return NN_OK;
+    return leapfrog_launch(ctx, vars, n, dt, p, seed, step, nullptr, "nn_hh_leapfrog_step");
+}
+
+extern "C" nn_status nn_hh_leapfrog_step_z(nn_ctx* ctx, float* const* vars, int n, float dt,
+                                           const nn_leapfrog_params* p, const float* d_z)
+{
+    if (!d_z) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_hh_leapfrog_step_z: d_z is NULL");
+    return leapfrog_launch(ctx, vars, n, dt, p, 0, 0, d_z, "nn_hh_leapfrog_step_z");
 }
 
 // =============================================================== coupling ==

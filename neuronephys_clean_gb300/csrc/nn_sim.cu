@@ -2256,6 +2256,25 @@ extern "C" nn_status nn_sim_counters(nn_sim* s, int64_t* step, int64_t* total_sp
     return check_err(s);
 }
 
+extern "C" nn_status nn_sim_get_ring(nn_sim* s, float* h_ring)
+{
+    if (!s || !h_ring) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    // device rows are n_pad pairs long, host rows n
+    NN_CUDA(ctx, cudaMemcpy2DAsync(h_ring, sizeof(float2) * (size_t)s->n, s->ring, sizeof(float2) * (size_t)s->n_pad,
+                                   sizeof(float2) * (size_t)s->n, (size_t)s->D, cudaMemcpyDeviceToHost, ctx->stream));
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_err(s);
+}
+
+extern "C" nn_status nn_sim_reset_raster(nn_sim* s)
+{
+    if (!s) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    NN_CUDA(ctx, cudaMemsetAsync(s->rcount, 0, sizeof(unsigned long long), ctx->stream));
+    return NN_OK;
+}
+
 extern "C" nn_status nn_sim_get_raster(nn_sim* s, int64_t cap, int32_t* h_step, int32_t* h_neuron, int64_t* count)
 {
     if (!s || !count || cap < 0) return NN_ERR_INVALID_ARG;

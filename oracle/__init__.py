@@ -72,6 +72,8 @@ _SIGS = {
     "orc_gen_gauss": (None, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_uint64,
                              P(OrcCSR)]),
     "orc_lattice_positions": (None, [C.c_int, C.c_uint64, V, V, V]),
+    "orc_init_drive": (None, [C.c_int, C.c_uint64, C.c_float, C.c_float, V]),
+    "orc_inh_flags": (None, [C.c_int, C.c_double, C.c_int, C.c_uint64, V]),
     "orc_sim_step": (C.c_int, [P(OrcSim), C.c_uint64, V]),
     "orc_apply7": (None, [V, V, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, V]),
     "orc_pcg7": (C.c_int, [V, V, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, V, C.c_double, C.c_int,
@@ -278,6 +280,37 @@ def lattice_positions(n: int, seed: int):
     x, y, z = (np.zeros(n, np.float32) for _ in range(3))
     lib().orc_lattice_positions(n, seed, ptr(x), ptr(y), ptr(z))
     return x, y, z
+
+
+def init_drive(n: int, seed: int, lo: float, hi: float) -> np.ndarray:
+    """Drive currents of the device's initial state (nn_sim_init_state)."""
+    out = np.zeros(n, np.float32)
+    lib().orc_init_drive(n, seed, lo, hi, ptr(out))
+    return out
+
+
+def inh_flags(n: int, frac: float, random: bool, seed: int) -> np.ndarray:
+    """Inhibitory flags of the device generators (k_inh)."""
+    out = np.zeros(n, np.uint8)
+    lib().orc_inh_flags(n, frac, 1 if random else 0, seed, ptr(out))
+    return out
+
+
+def rest_state(n: int, v0: float = -65.0) -> np.ndarray:
+    """(6, n) state V, m, h, n, ge, gi at rest: gates at their steady state."""
+    m, h, nn_ = steady_state(v0)
+    st = np.zeros((6, n), np.float64)
+    st[0], st[1], st[2], st[3] = v0, np.float32(m), np.float32(h), np.float32(nn_)
+    return st
+
+
+def voxels(x, y, z, grid: int) -> np.ndarray:
+    """Voxel of each position on a grid^3 over the unit cube (k_init_state)."""
+    g = np.float32(grid)
+    ix = np.clip((np.asarray(x, np.float32) * g).astype(np.int32), 0, grid - 1)
+    iy = np.clip((np.asarray(y, np.float32) * g).astype(np.int32), 0, grid - 1)
+    iz = np.clip((np.asarray(z, np.float32) * g).astype(np.int32), 0, grid - 1)
+    return (ix + grid * (iy + grid * iz)).astype(np.int32)
 
 
 def csr_to_csc(a: CSR):

@@ -562,6 +562,38 @@ void orc_lattice_positions(int n, uint64_t seed, float* x, float* y, float* z)
     }
 }
 
+/* Per-neuron drive current lo + (hi - lo) u, u the 24-bit uniform of the
+ * neuron's P_DRIVE draw, in FP32 as the device's k_init_state forms it. */
+void orc_init_drive(int n, uint64_t seed, float lo, float hi, float* out)
+{
+    for (int i = 0; i < n; ++i) {
+        uint32_t r[4];
+        philox(seed, (uint32_t)i, 0u, 0u, P_DRIVE, r);
+        const float u = (float)(r[0] >> 8) * (1.0f / 16777216.0f);
+        const float span = hi - lo;
+        const float t = span * u;
+        out[i] = lo + t;
+    }
+}
+
+/* Inhibitory flags: the last round(frac * n) indices, or (random) each
+ * neuron's P_TYPE draw below floor(frac * 2^32), as the device's k_inh. */
+void orc_inh_flags(int n, double frac, int random, uint64_t seed, uint8_t* out)
+{
+    const int n_inh = (int)llround(frac * n);
+    const double tf = floor(frac * 4294967296.0);
+    const uint32_t thr = tf >= 4294967295.0 ? 0xffffffffu : (uint32_t)tf;
+    for (int i = 0; i < n; ++i) {
+        if (random) {
+            uint32_t r[4];
+            philox(seed, (uint32_t)i, 0u, 0u, P_TYPE, r);
+            out[i] = r[0] < thr ? 1 : 0;
+        } else {
+            out[i] = i >= n - n_inh ? 1 : 0;
+        }
+    }
+}
+
 void orc_gen_gauss(int n, int k, double sigma, double w_mu, double w_sigma, int dmax,
                    uint64_t seed, orc_csr* out)
 {

@@ -164,6 +164,8 @@ void orc_block_tables(int n, int R, double size_sigma, double density_sigma, int
                       int* start, int* size, uint32_t* cum, uint8_t* pdelay);
 void orc_gen_block(int n, int k, int R, double size_sigma, double density_sigma, int dmax, double w_mu,
                    double w_sigma, uint64_t seed, orc_csr* out);
+void orc_init_drive(int n, uint64_t seed, float lo, float hi, float* out);
+void orc_inh_flags(int n, double frac, int random, uint64_t seed, uint8_t* out);
 void orc_gen_gauss(int n, int k, double sigma, double w_mu, double w_sigma, int dmax,
                    uint64_t seed, orc_csr* out);
 void orc_lattice_positions(int n, uint64_t seed, float* x, float* y, float* z);

@@ -138,3 +138,26 @@ def test_init_state(ctx, orc):
     m, h, nn_ = orc.steady_state(-65.0)
     assert np.allclose(s.get_field("M"), m, rtol=1e-6) and np.allclose(s.get_field("N"), nn_, rtol=1e-6)
     assert np.all(s.get_field("V") == -65.0)
+
+
+@pytest.mark.parametrize("kind", ["er", "gauss"])
+def test_init_state_drive_and_types_match_oracle(ctx, orc, kind):
+    """The oracle's generators of the initial state (drive currents,
+    inhibitory flags, voxels), which the CPU reference arm of the benchmark
+    uses instead of the device: bit-exact against the device."""
+    n, seed, g = 5000, 1, 32
+    s = _sim(ctx, n, max_delay=20, seed=seed, grid=g)
+    if kind == "er":
+        spec = nn.default_net_spec(nn.NN_NET_ER)
+        spec.p = 0.002
+    else:
+        spec = nn.default_net_spec(nn.NN_NET_GAUSS)
+        spec.k, spec.dmax = 10, 20
+    s.generate_network(spec)
+    s.init_state(-65.0, 6.0, 12.0)
+    assert np.array_equal(s.get_field("IDRIVE"), orc.init_drive(n, seed, 6.0, 12.0))
+    assert np.array_equal(s.get_network()[4], orc.inh_flags(n, 0.2, kind == "gauss", seed))
+    assert np.array_equal(s.get_vox(), orc.voxels(*orc.lattice_positions(n, seed), g))
+    st = orc.rest_state(n)
+    for q, f in enumerate(("V", "M", "H", "N")):
+        np.testing.assert_allclose(s.get_field(f), st[q], rtol=1e-6)

@@ -92,6 +92,43 @@ def test_population_rate_50ms(ctx, orc):
     assert abs(total - nref) / nref < 0.01
 
 
+def test_benchmarked_configuration_parity(ctx, orc):
+    """The benchmarked 1M-neuron network (Gaussian connectivity, 100
+    out-edges per neuron = 1e8 synapses, lognormal(-1, 1) weights, delays
+    U{1..20}, 20 % inhibitory, drive U[6, 12]) against the FP64 oracle over
+    50 timesteps, started from the GPU's state (neuron fields, delay ring,
+    step counter) at a period boundary inside a population burst after 2,000
+    settling steps.  Tolerances as above (tests/tolerance.py), with the
+    cascade rule of oracle/parity.py: in a 50-step window a one-step shift
+    reaches its targets, whose inputs then arrive a step apart; differences
+    downstream of an accepted shift are counted (at most 1 % of the spikes)
+    and the neurons they reach (at most 1 % of the neurons) leave the
+    trajectory check."""
+    from oracle.parity import find_burst, window_parity
+    n = 1_000_000
+    c = nn.default_config(n)
+    c.seed, c.max_delay, c.raster_capacity, c.grid = 1, 20, 2_000_000, 0
+    s = nn.Simulation(ctx, c)
+    spec = nn.default_net_spec(nn.NN_NET_GAUSS)
+    spec.k, spec.sigma, spec.w_mu, spec.w_sigma, spec.dmax = 100, 0.1, -1.0, 1.0, 20
+    spec.inh_fraction, spec.inh_random = 0.2, 1
+    s.generate_network(spec)
+    assert s.nnz == 100 * n
+    s.init_state(-65.0, 6.0, 12.0)
+    s.step(2000)
+    find_burst(s, 50, n, max_periods=400)
+    r = window_parity(s, 50)
+    r.pop("_oracle")
+    print({k: v for k, v in r.items() if not k.startswith("_")})
+    assert r["spikes_oracle"] > 1000
+    assert r["unexplained_spikes"] == 0
+    assert r["shifted_spikes"] <= 0.005 * r["spikes_oracle"]
+    assert r["cascade_spikes"] <= 0.01 * r["spikes_oracle"]
+    assert r["excluded_neurons"] <= 0.01 * n
+    assert r["trajectory_violations"] == 0, r
+    s.close()
+
+
 def test_push_pull_agree_and_pull_is_deterministic(ctx):
     a = make_sim(ctx, delivery=0, seed=5)
     b = make_sim(ctx, delivery=1, seed=5)

@@ -45,3 +45,25 @@ def test_perturbed_neurons_are_held_to_the_wider_bound():
     got[0, 1] += 10.0                       # beyond the 5e-2 bound
     with pytest.raises(AssertionError):
         assert_trajectory(got, ref, ref, 0.01, exclude=mask)
+
+
+def test_cascade_of_a_root_shift_is_explained_only_downstream():
+    from oracle.parity import compare_rasters
+    # neuron 1 -> targets 2, 3; neuron 4 -> target 5
+    row_ptr = np.array([0, 0, 2, 2, 2, 3, 3])
+    col = np.array([2, 3, 5])
+    ref = {(10, 1): 0.001, (15, 2): 1.0, (15, 4): 1.0, (20, 5): 1.0}
+    got = {(11, 1), (16, 2), (15, 4), (20, 5)}
+    r = compare_rasters(got, ref, row_ptr=row_ptr, col=col)
+    assert r["shifted"] == [(10, 1)] and r["cascade"] == [(15, 2)]
+    assert not r["unexplained_oracle"] and not r["unexplained_device"]
+    assert r["perturbed"] == [1, 2, 3]
+    # without the network the downstream shift is unexplained
+    r = compare_rasters(got, ref)
+    assert r["unexplained_oracle"] == [(15, 2)]
+    # a shift of a neuron no difference reaches stays unexplained
+    r = compare_rasters({(11, 1), (15, 2), (16, 4), (20, 5)}, ref, row_ptr=row_ptr, col=col)
+    assert r["unexplained_oracle"] == [(15, 4)]
+    # a spike missing on the device entirely, downstream of the root shift
+    r = compare_rasters({(11, 1), (15, 4), (20, 5)}, ref, row_ptr=row_ptr, col=col)
+    assert r["cascade"] == [(15, 2)] and not r["unexplained_oracle"]
