@@ -53,6 +53,8 @@ NN_API const char* nn_ctx_last_error(const nn_ctx* ctx);
 NN_API nn_status nn_ctx_synchronize(nn_ctx* ctx);
 /* Number of kernels this context has launched (graph replays count their nodes). */
 NN_API int64_t nn_ctx_kernel_launches(const nn_ctx* ctx);
+/* Streaming multiprocessors of the context's device. */
+NN_API int nn_ctx_num_sms(const nn_ctx* ctx);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that interoperate. */
 NN_API void* nn_ctx_stream(nn_ctx* ctx);
@@ -426,10 +428,15 @@ NN_API nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, double
  * NN_ERR_UNSUPPORTED without launching anything.  Returns NN_ERR_NOT_CONVERGED
  * if rtol is not reached in max_iter iterations.
  * The first call on a device looks up the scratch's device address (which
- * also loads the library's kernels on that device): make that first call
- * before any stream capture.  All calls share the one scratch, so calls whose
- * work overlaps on the GPU (different streams, threads or processes' streams
- * of this library instance) race; serialise them. */
+ * also loads the library's kernels on that device) and keeps it for the
+ * process: make that first call before any stream capture, and do not call
+ * this entry point on a device after cudaDeviceReset there (the kept address
+ * would belong to the context the reset destroyed).  Each process has its
+ * own scratch; within a process, all calls on a device share the one
+ * scratch, so calls whose work overlaps on the GPU (from different streams or
+ * host threads) race: serialise them.  The call synchronises the caller's
+ * stream at each convergence check.  Only the status code reports a failure:
+ * no message is kept (there is no context to keep it in). */
 #define NN_PCG_NOALLOC_MAX_CELLS (64 * 64 * 64)
 NN_API nn_status nn_pcg_solve_noalloc(void* stream, int nx, int ny, int nz, double alpha, double beta,
                                       const float* d_Dcell, const float* d_b, float* d_x, double rtol,

@@ -97,6 +97,10 @@ class Context:
     def kernel_launches(self) -> int:
         return int(lib().nn_ctx_kernel_launches(self.handle))
 
+    @property
+    def num_sms(self) -> int:
+        return int(lib().nn_ctx_num_sms(self.handle))
+
     def time_begin(self) -> None:
         """Record a CUDA event on the context stream."""
         _check(lib().nn_ctx_time_begin(self.handle), self, "time_begin")

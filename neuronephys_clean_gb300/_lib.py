@@ -72,6 +72,7 @@ _SIGS = {
     "nn_ctx_last_error": (c_char_p, [c_void_p]),
     "nn_ctx_synchronize": (c_int, [c_void_p]),
     "nn_ctx_kernel_launches": (c_int64, [c_void_p]),
+    "nn_ctx_num_sms": (c_int, [c_void_p]),
     "nn_ctx_stream": (c_void_p, [c_void_p]),
     "nn_ctx_time_begin": (c_int, [c_void_p]),
     "nn_ctx_time_end": (c_int, [c_void_p, P(c_float)]),

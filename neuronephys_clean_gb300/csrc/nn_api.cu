@@ -108,6 +108,8 @@ extern "C" nn_status nn_ctx_synchronize(nn_ctx* ctx)
 
 extern "C" int64_t nn_ctx_kernel_launches(const nn_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+extern "C" int nn_ctx_num_sms(const nn_ctx* ctx) { return ctx ? ctx->num_sms : 0; }
+
 extern "C" void* nn_ctx_stream(nn_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 extern "C" nn_status nn_ctx_time_begin(nn_ctx* ctx)

@@ -544,7 +544,8 @@ nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol,
 // synchronisation of cudaMalloc/cudaFree).  Its work vectors, reduction
 // partials and flags live in the fixed file-scope array below, which every GPU
 // that loads this library holds until the process exits.  One scratch serves
-// all calls on a device, so calls whose work overlaps on the GPU race.
+// all calls on a device within a process, so calls whose work overlaps on the
+// GPU race (each process has its own copy of the array).
 
 namespace {
 constexpr size_t NA_ALIGN(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -565,7 +566,9 @@ static __device__ __align__(256) unsigned char g_pcg_noalloc_scratch[NA_BYTES];
 
 // Device address of the scratch on the current device, looked up once per
 // device (the first call on a device does this, which also loads the module on
-// that device; make that first call before any stream capture).
+// that device; make that first call before any stream capture).  The address
+// is kept for the life of the process; a cudaDeviceReset destroys the context
+// it belongs to, so the entry point is not for use on a device after a reset.
 static nn_status noalloc_scratch(int dev, unsigned char** out)
 {
     static std::mutex mu;
@@ -601,7 +604,8 @@ extern "C" nn_status nn_pcg_solve_noalloc(void* stream, int nx, int ny, int nz, 
     }
     unsigned char* base = nullptr;
     NN_TRY(noalloc_scratch(dev, &base));
-    // A context on the caller's stream that owns nothing.
+    // A context on the caller's stream that owns nothing (its error text is
+    // dropped on return: callers of this entry point get the status only).
     nn_ctx ctx;
     ctx.device = dev;
     ctx.stream = (cudaStream_t)stream;

@@ -11,12 +11,17 @@ namespace {
 //   the warp that found the spikes scatters their out-edges into ring slots
 //   (t+d)%D with red.global.add (d >= 1, so never the slot this launch reads).
 // Loop trip counts are warp-uniform so the warp collectives stay converged.
-// Resident blocks per SM the neuron update is compiled for: 3 (85 registers)
-// is the fastest of 1, 3 and 4 with packed pairs on the 1M-neuron workload.
+// Registers the neuron update is compiled for: 3 blocks of 256 threads per
+// SM (at most 85 registers; 80 used, with a few spilled words in the spike
+// path) is faster than 2 blocks without spills (21.3 vs 18.1 us per
+// 1M-neuron step) and than 4.
 #ifndef NN_HH_MIN_BLOCKS
 #define NN_HH_MIN_BLOCKS 3
 #endif
-template <int NPT>
+// UNI: no per-neuron gNa scale and no paracrine feedback (the common case),
+// so the step's constant current terms are launch constants
+// (nn_hh_drive_uniform) rather than registers.
+template <int NPT, bool UNI>
 __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
 {
     const uint64_t t = *a.base + (uint64_t)a.q;
@@ -92,7 +97,8 @@ __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
                 ngna.v[l] = -__fmul_rn(a.p.gNa, GS[q]);
                 ngpu.v[l] = -__fmul_rn(a.p.g_par, UP[q]);
             }
-            nn_hh_rk4<W>(a.p, ngna, iext, ngpu, y);
+            if (UNI) nn_hh_rk4<W>(a.p, nn_hh_make_drive_uniform<W>(a.p, iext), y);
+            else nn_hh_rk4<W>(a.p, nn_hh_make_drive<W>(a.p, ngna, iext, ngpu), y);
 #pragma unroll
             for (int l = 0; l < W; ++l) {
                 const int q = p0 + l;
@@ -194,10 +200,17 @@ __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
 
 cudaError_t nn_launch_hh_step(const StepArgs& a, int npt, int blocks, int tpb, cudaStream_t cs)
 {
-    switch (npt) {
-        case 1: k_hh_step<1><<<blocks, tpb, 0, cs>>>(a); break;
-        case 2: k_hh_step<2><<<blocks, tpb, 0, cs>>>(a); break;
-        default: k_hh_step<4><<<blocks, tpb, 0, cs>>>(a); break;
+    // uniform when no per-neuron gNa scale is loaded and the field does not
+    // feed back (g_par = 0 or no density input): then ngna = -gNa and
+    // ngpu = 0 (or -0) for every neuron, as the general form computes them
+    const bool uni = !a.gna_scale && (!a.upar || a.p.g_par == 0.0f);
+    switch (npt * 2 + (uni ? 1 : 0)) {
+        case 2: k_hh_step<1, false><<<blocks, tpb, 0, cs>>>(a); break;
+        case 3: k_hh_step<1, true><<<blocks, tpb, 0, cs>>>(a); break;
+        case 4: k_hh_step<2, false><<<blocks, tpb, 0, cs>>>(a); break;
+        case 5: k_hh_step<2, true><<<blocks, tpb, 0, cs>>>(a); break;
+        case 8: k_hh_step<4, false><<<blocks, tpb, 0, cs>>>(a); break;
+        default: k_hh_step<4, true><<<blocks, tpb, 0, cs>>>(a); break;
     }
     return cudaPeekAtLastError();
 }

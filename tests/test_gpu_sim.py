@@ -172,29 +172,51 @@ def test_sliced_pull_matches_warp_pull(ctx, monkeypatch):
 
 
 def test_chunked_pull_many_buckets(ctx, monkeypatch):
-    """The chunked pull on a network whose (block, delay) runs span several
-    source buckets and exceed one chunk (150k neurons, 100 synapses each,
-    delays 1..20: about 4,900 entries per run over ten 16,384-source
-    buckets; weights lognormal(-1, 1) nS), against the warp-per-column kernel:
-    same rasters, inputs within the spread of two summation orders."""
+    """The chunked pull where its (block, delay) runs fill whole chunks and
+    are split by source span: 300k neurons, 100 out-edges each to uniformly
+    random targets, delays U{1..3}, lognormal(-1, 1) weights.  Each gather
+    block then holds ~66k entries per delay (8 full chunks of 8,192 entries)
+    whose sources cover all 19 source buckets of 16,384 neurons, more than a
+    chunk may span (16).  The layout facts are checked on the host from the
+    network; the gather is compared with the warp-per-column kernel: same
+    rasters, inputs within the spread of two summation orders, and each
+    deterministic."""
+    n, k, dmax = 300_000, 100, 3
+    rng = np.random.default_rng(12)
+    col = rng.integers(0, n, n * k).astype(np.int32)
+    rp = (np.arange(n + 1, dtype=np.int64) * k)
+    w = np.exp(rng.normal(-1.0, 1.0, n * k)).astype(np.float32)
+    d = rng.integers(1, dmax + 1, n * k).astype(np.uint8)
+    inh = (rng.random(n) < 0.2).astype(np.uint8)
+
     def run(unsliced):
         if unsliced:
             monkeypatch.setenv("NN_PULL_UNSLICED", "1")
         else:
             monkeypatch.delenv("NN_PULL_UNSLICED", raising=False)
-        n = 150_000
         c = nn.default_config(n)
-        c.seed, c.max_delay, c.raster_capacity, c.delivery = 5, 20, 2_000_000, 1
+        c.seed, c.max_delay, c.raster_capacity, c.delivery = 5, dmax, 2_000_000, 1
         s = nn.Simulation(ctx, c)
-        spec = nn.default_net_spec(nn.NN_NET_GAUSS)
-        spec.k, spec.dmax, spec.w_mu = 100, 20, -1.0
-        s.generate_network(spec)
-        assert s.pull_info()[0] == (not unsliced)
+        s.set_network(rp, col, w, d, inh)
+        sliced, cols = s.pull_info()
+        assert sliced == (not unsliced)
         s.init_state(-65.0, 6.0, 12.0)
         s.set_field("V", np.random.default_rng(4).uniform(-65, -35, n).astype(np.float32))
-        s.step(45)
-        return raster_set(*s.raster()), np.stack([s.get_field("GE"), s.get_field("GI")])
-    a, b, u = run(False), run(False), run(True)
+        s.step(100)
+        return raster_set(*s.raster()), np.stack([s.get_field("GE"), s.get_field("GI")]), cols
+
+    a = run(False)
+    cols = a[2]
+    # layout facts of the gather: entries per (block, delay) and the source
+    # buckets they cover (the pull reads synapses by postsynaptic column)
+    src = np.repeat(np.arange(n), k)
+    key = (col // cols).astype(np.int64) * dmax + (d.astype(np.int64) - 1)
+    per_run = np.bincount(key)
+    assert per_run.min() > 8192 * 4
+    buckets = np.zeros((per_run.size, (n + 16383) // 16384), bool)
+    buckets[key, src // 16384] = True
+    assert buckets.sum(axis=1).max() > 16
+    b, u = run(False), run(True)
     assert len(a[0]) > 1000
     assert a[0] == b[0] and np.array_equal(a[1], b[1])
     assert a[0] == u[0]

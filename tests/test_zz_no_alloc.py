@@ -5,8 +5,10 @@ loop that cannot take cudaMalloc's device-wide synchronisation).
 Called through the C ABI; each result is compared with the allocating entry
 point (nn_pcg_create + nn_pcg_solve) on the same inputs, within the PCG tests'
 tolerance, on two calls in a row with different right-hand sides (the shared
-fixed scratch keeps the previous call's contents).  This file is collected
-last so that a run stopping at the first failure has run everything else.
+fixed scratch keeps the previous call's contents).  The device's free memory
+(cuMemGetInfo), taken after a warm-up call, is the same after those calls,
+which a single cudaMalloc would change.  This file is collected last so that
+a run stopping at the first failure has run everything else.
 """
 import ctypes as C
 
@@ -16,6 +18,14 @@ import pytest
 import neuronephys_clean_gb300 as nn
 
 pytestmark = pytest.mark.gpu
+
+
+def _free_device_bytes() -> int:
+    """Free memory of the current device (driver API, current context)."""
+    cuda = C.CDLL("libcuda.so.1")
+    free, total = C.c_size_t(0), C.c_size_t(0)
+    assert cuda.cuMemGetInfo_v2(C.byref(free), C.byref(total)) == 0
+    return free.value
 
 
 def _solve_noalloc(ctx, shape, alpha, beta, D, b, x):
@@ -35,14 +45,24 @@ def test_noalloc_matches_allocating_solver(ctx, hetero):
     D = ctx.to_device(np.exp(rng.normal(0.0, 0.5, G)).astype(np.float32)) if hetero else None
     alpha, beta = 6.0, 0.1
     pc = nn.PCG(ctx, shape[2], shape[1], shape[0], alpha, beta, D)
+    cases = []
     for call in range(2):
         b_h = rng.random(G).astype(np.float32)
         b_h[rng.integers(0, G, 50)] += 5.0
         b = ctx.to_device(b_h)
         x_ref = ctx.to_device(np.zeros(G, np.float32))
         it_ref, rel_ref = pc.solve(b, x_ref, rtol=1e-6, max_iter=5000)
-        x = ctx.to_device(np.zeros(G, np.float32))
-        st, it, rel = _solve_noalloc(ctx, shape, alpha, beta, D, b, x)
+        cases.append((b, x_ref, it_ref, ctx.to_device(np.zeros(G, np.float32))))
+    # a warm-up call does the per-device set-up (and loads the kernels it
+    # launches); the compared calls then must leave the free memory unchanged
+    warm = ctx.to_device(np.zeros(G, np.float32))
+    assert _solve_noalloc(ctx, shape, alpha, beta, D, cases[0][0], warm)[0] == 0
+    ctx.synchronize()
+    free0 = _free_device_bytes()
+    results = [_solve_noalloc(ctx, shape, alpha, beta, D, b, x) for (b, _, _, x) in cases]
+    ctx.synchronize()
+    assert _free_device_bytes() == free0
+    for call, ((st, it, rel), (_, x_ref, it_ref, x)) in enumerate(zip(results, cases)):
         assert st == 0, nn.lib().nn_status_string(st)
         assert rel <= 1e-6 and abs(it - it_ref) <= 1
         ref = x_ref.numpy().astype(np.float64)
