@@ -351,8 +351,91 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     if args.cpu_baseline:
         line["parity"], line["cpu_baseline"] = parity_and_cpu_baseline(sim, wl, args)
     sim.close()
+    if args.c5 and rank == 0 and args.gpus == 1 and wl["workload"] == WORKLOADS["c2"]["workload"]:
+        line["cg_256cube"] = c5_leg(nn, ctx, args)
     ctx.close()
     return line
+
+
+def c5_leg(nn, ctx, args) -> dict:
+    """The workload's third metric, CG time to a 1e-6 relative residual, on
+    the configuration-5 system (256^3 cells, lognormal D with sigma 1 and an
+    8-cell correlation length, uptake 0.1), in the default line:
+    * plain Jacobi-PCG (the judge), the classical multigrid FCG, and the
+      multigrid whose 32^3 level is solved by the learned U-Net (trained here
+      on the GPU, on the coarse problems of six training right-hand sides);
+    * each timed on the bench right-hand side and on four held-out ones
+      (spike-source fields of seeds not used in training);
+    * each bench solution's error against the FP64 oracle's CG solution of
+      the same system to a 1e-10 relative residual (16 host cores)."""
+    import oracle
+    from neuronephys_clean_gb300 import fields
+    wl = WORKLOADS["c5"]
+    shape, D, b, alpha, beta = cg_problem(wl)
+    G = int(np.prod(shape))
+    pc = nn.PCG(ctx, shape[2], shape[1], shape[0], alpha, beta, ctx.to_device(D.ravel()))
+    bench_rhs = ctx.to_device(b)
+    held_out = [ctx.to_device(fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=5000 + j))
+                for j in range(4)]
+    dx = ctx.empty((G,), np.float32)
+
+    def timed(solve, rhs, reps=2):
+        solve(rhs, dx)  # warm (graph capture, first touches)
+        ms, its = [], []
+        for _ in range(reps):
+            dx.zero()
+            ctx.time_begin()
+            it, rel = solve(rhs, dx)
+            ms.append(ctx.time_end())
+            its.append(it)
+        return statistics.mean(ms), statistics.mean(its), rel
+
+    def held(solve):
+        r = [timed(solve, h, reps=1) for h in held_out]
+        return {"ms_mean": statistics.mean(x[0] for x in r), "iterations_mean": statistics.mean(x[1] for x in r)}
+
+    out, sols = {}, {}
+    plain = lambda rb, x: pc.solve(rb, x, 1e-6, 20000)  # noqa: E731
+    ms, it, rel = timed(plain, bench_rhs)
+    sols["jacobi_pcg"] = dx.numpy().astype(np.float64)
+    out["jacobi_pcg"] = {"ms_to_tol": ms, "iterations": it, "relres": rel, "held_out": held(plain)}
+    mg = nn.MultigridPCG(pc)
+    classical = lambda rb, x: mg.solve(rb, x, 1e-6)  # noqa: E731
+    ms, it, rel = timed(classical, bench_rhs)
+    sols["multigrid"] = dx.numpy().astype(np.float64)
+    out["multigrid"] = {"ms_to_tol": ms, "iterations": it, "relres": rel, "levels": mg.levels,
+                        "held_out": held(classical)}
+    mg.close()
+    lm = nn.LearnedMultigrid(pc, level=3, seed=7)
+    t0 = time.perf_counter()
+    pairs = lm.add_solves([fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=2000 + j)
+                           for j in range(wl["train_rhs"])])
+    loss = lm.train(wl["lmg_train_steps"], 1e-3)
+    t_train = time.perf_counter() - t0
+    learned = lambda rb, x: lm.solve(rb, x, 1e-6)  # noqa: E731
+    ms, it, rel = timed(learned, bench_rhs)
+    sols["learned_multigrid"] = dx.numpy().astype(np.float64)
+    out["learned_multigrid"] = {"ms_to_tol": ms, "iterations": it, "relres": rel, "network_level_grid": 32,
+                                "held_out": held(learned),
+                                "training": {"right_hand_sides": wl["train_rhs"], "pairs": pairs,
+                                             "adam_steps": wl["lmg_train_steps"], "s": t_train, "final_loss": loss}}
+    lm.close()
+    pc.close()
+    t1 = time.perf_counter()
+    xs, it_o, rel_o = oracle.pcg7(b, np.zeros(G), shape, alpha, beta, D, rtol=1e-10, max_iter=5000)
+    t_oracle = time.perf_counter() - t1
+    nref = float(np.linalg.norm(xs))
+    for k, x in sols.items():
+        out[k]["error_vs_fp64"] = float(np.linalg.norm(x - xs) / nref)
+    plain_ms = out["jacobi_pcg"]["ms_to_tol"]
+    for k in ("multigrid", "learned_multigrid"):
+        out[k]["vs_plain_time"] = out[k]["ms_to_tol"] / plain_ms
+        out[k]["held_out"]["vs_plain_time"] = out[k]["held_out"]["ms_mean"] / out["jacobi_pcg"]["held_out"]["ms_mean"]
+    out["workload"] = wl["workload"]
+    out["fp64_oracle"] = {"iterations": it_o, "relres": rel_o, "s": t_oracle,
+                          "cores": int(oracle.lib().orc_num_threads())}
+    out["tolerance"] = "relative residual 1e-6 (FP64 reductions); error = |x - x_fp64| / |x_fp64|"
+    return out
 
 
 def workload_config(wl: dict, nnz: int) -> dict:
@@ -920,6 +1003,132 @@ def run_reference(args, wl: dict, rank: int) -> dict | None:
             "e2e": {"value": value, "unit": "neuron-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ------------------------------------------- reference kernels on GB300 ---
+
+# slots of the reference's HH struct-of-arrays (src/defines.cuh:57-78)
+REF_SOA = ["V", "M", "N", "H", "LOCAL_Y", "IY", "EY", "LOCAL_OUTPUT", "LOCAL_IN", "LOCAL_COUNT",
+           "EOUTPUT", "EIN", "ECOUNT", "IOUTPUT", "IIN", "ICOUNT", "APPCUR"]
+REFKERN = dict(workload="leapfrog_1M_dt0.4_coupling_count_1M_k100_fire1pct", n=1_000_000, k=100, fire=0.01,
+               dt=0.4, reps=20)
+
+
+def refkern_inputs(seed: int = 3):
+    """Shared inputs of the reference-kernel comparison: the reference SoA of
+    1M HH neurons in a physiological state (gates at their steady state,
+    src/ephys.cu:57-63 rates), and a 1M-neuron network of 100 uniformly random
+    out-edges per neuron (int32 CSR, as UniformRandomNetwork builds) with 1 %
+    of the neurons firing (output 0.5 > 0.1, the rest 0.05)."""
+    w = REFKERN
+    n, k = w["n"], w["k"]
+    rng = np.random.default_rng(seed)
+    V = rng.uniform(-75.0, -40.0, n)
+    am = (3.5 + 0.1 * V) / (1 - np.exp(-3.5 - 0.1 * V))
+    an = (-0.5 - 0.01 * V) / (np.exp(-5 - 0.1 * V) - 1)
+    ah, bm = 0.07 * np.exp(-V / 20 - 3), 4 * np.exp(-(V + 60) / 18)
+    bn, bh = 0.125 * np.exp(-(V + 60) / 80), 1 / (np.exp(-3 - 0.1 * V) + 1)
+    st = {q: np.zeros(n, np.float32) for q in REF_SOA}
+    st["V"], st["M"] = V.astype(np.float32), (am / (am + bm)).astype(np.float32)
+    st["N"], st["H"] = (an / (an + bn)).astype(np.float32), (ah / (ah + bh)).astype(np.float32)
+    for q in ("LOCAL", "E", "I"):
+        cnt = rng.integers(0, 12, n).astype(np.float32)
+        st["LOCAL_COUNT" if q == "LOCAL" else f"{q}COUNT"] = cnt
+        st["LOCAL_IN" if q == "LOCAL" else f"{q}IN"] = (cnt * rng.uniform(0, 1, n)).astype(np.float32)
+    st["APPCUR"] = rng.uniform(0.0, 5.0, n).astype(np.float32)
+    idx = rng.integers(0, n, n * k).astype(np.int32)
+    off = (np.arange(n + 1, dtype=np.int64) * k).astype(np.int32)
+    out = np.full(n, 0.05, np.float32)
+    fire = np.sort(rng.choice(n, int(w["fire"] * n), replace=False)).astype(np.int32)
+    out[fire] = 0.5
+    return [st[q] for q in REF_SOA], idx, off, out, fire
+
+
+def refkern_line(impl: str, rows: dict) -> dict:
+    w = REFKERN
+    return {"metric": "reference-semantics kernels on GB300 (leapfrog neuron-steps/s, count-coupling events/s)",
+            "impl": impl, "config": {"workload": w["workload"], "neurons": w["n"], "out_degree": w["k"],
+                                     "firing_fraction": w["fire"], "dt_ms": w["dt"], "launches_timed": w["reps"]},
+            "data": "synthetic (seeded)", **rows}
+
+
+def run_reference_kernels(args, rank: int) -> dict | None:
+    """The reference's own Leapfrog_HH and signal_spikes_kernel (compiled from
+    its sources, run by the driver-API harness in oracle/; no product code),
+    at the reference's launch shape <<<32, 64>>> (src/defines.cuh:81-82) and on
+    a grid that fills the GPU.  The thrust threshold/compaction of
+    AtomicCoupling::operator() is host glue the harness does not time: only
+    the kernels."""
+    if rank != 0:
+        return None
+    from oracle import refkern
+    if not refkern.RefKernels.available():
+        return {"impl": "reference", "unavailable": "reference kernel cubins not built (no reference checkout "
+                                                    "where oracle/build.py ran)"}
+    w = REFKERN
+    n, reps = w["n"], w["reps"]
+    vars17, idx, off, out, fire = refkern_inputs()
+    rk = refkern.RefKernels(0)
+    d_vars = [rk.to_device(a) for a in vars17]
+    d_table = rk.to_device(np.array(d_vars, np.uint64))
+    d_states = rk.zeros(n * refkern.XORWOW_DTYPE.itemsize)
+    rk.init_random(0, n, d_states)                       # Ephys::Ephys (src/ephys.cu:20-26)
+    full = (n + 255) // 256
+    rows = {"leapfrog": {}, "signal_spikes": {}}
+    for name, grid, block in (("reference_grid_32x64", 32, 64), ("full_grid", full, 256)):
+        rk.leapfrog(d_table, n, w["dt"], d_states, grid=grid, block=block)  # warm
+        ms = rk.time_leapfrog(d_table, n, w["dt"], d_states, grid, block, reps)
+        rows["leapfrog"][name] = {"grid": grid, "block": block, "ms_per_launch": ms,
+                                  "neuron_steps_per_s": n / (ms * 1e-3)}
+    d_idx, d_off, d_out, d_fire = rk.to_device(idx), rk.to_device(off), rk.to_device(out), rk.to_device(fire)
+    d_in = rk.zeros(4 * n)
+    events = len(fire) * w["k"]
+    for name, grid, block in (("reference_grid_32x64", 32, 64), ("full_grid", (len(fire) + 63) // 64, 64)):
+        rk.signal_spikes(len(fire), d_idx, d_off, d_fire, d_in, d_out, grid=grid, block=block)
+        ms = rk.time_signal_spikes(len(fire), d_idx, d_off, d_fire, d_in, d_out, grid, block, reps)
+        rows["signal_spikes"][name] = {"grid": grid, "block": block, "ms_per_launch": ms,
+                                       "synaptic_events_per_s": events / (ms * 1e-3)}
+    return refkern_line("reference", rows)
+
+
+def run_our_reference_kernels(args, rank: int, local_rank: int) -> dict | None:
+    """The library's drop-ins for the same calls on the same inputs:
+    nn_hh_leapfrog_step (HHEphys::SimulateEphys; same FP64 rate arithmetic, a
+    counter-based noise draw instead of curand) and nn_coupling_run in count
+    mode (AtomicCoupling::operator(): zeroing, threshold, ordered compaction
+    and the scatter, all timed)."""
+    if rank != 0:
+        return None
+    import neuronephys_clean_gb300 as nn
+    w = REFKERN
+    n, reps = w["n"], w["reps"]
+    vars17, idx, off, out, fire = refkern_inputs()
+    ctx = nn.Context(local_rank)
+    eph = nn.HHEphys(ctx, n, variant=0, dt=w["dt"])
+    assert list(nn.SIM_PARAMS) == REF_SOA
+    for q, a in zip(REF_SOA, vars17):
+        eph.set(q, a)
+    eph.simulate_ephys()
+    ctx.time_begin()
+    for _ in range(reps):
+        eph.simulate_ephys()
+    ms = ctx.time_end() / reps
+    rows = {"leapfrog": {"k_leapfrog": {"ms_per_launch": ms, "neuron_steps_per_s": n / (ms * 1e-3)}}}
+    coup = nn.AtomicCoupling(ctx, n)
+    lst = nn.AdjacencyList(ctx.to_device(idx), ctx.to_device(off))
+    d_out, d_in = ctx.to_device(out), ctx.empty((n,), np.float32)
+    nf = coup(lst, d_in, d_out)
+    assert nf == len(fire)
+    ctx.time_begin()
+    for _ in range(reps):
+        coup(lst, d_in, d_out, read_count=False)
+    ms = ctx.time_end() / reps
+    rows["signal_spikes"] = {"nn_coupling_run": {"ms_per_launch": ms,
+                                                 "synaptic_events_per_s": len(fire) * w["k"] / (ms * 1e-3),
+                                                 "includes": "zeroing of the inputs, threshold, compaction, scatter"}}
+    coup.close()
+    ctx.close()
+    return refkern_line("ours", rows)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -937,11 +1146,21 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--delivery-sweep", action="store_true",
                     help="time push / pull spike delivery alone over firing fractions (one JSON line)")
+    ap.add_argument("--reference-kernels", action="store_true",
+                    help="time the reference-semantics leapfrog and count coupling at 1M neurons: the reference's "
+                         "own kernels with --impl reference, the library's drop-ins otherwise (one JSON line)")
+    ap.add_argument("--no-c5", dest="c5", action="store_false",
+                    help="default workload: skip the 256^3 CG time-to-tolerance leg")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="CG workload: skip the learned-preconditioner comparison")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     wl = WORKLOADS[args.workload]
+    if args.reference_kernels and args.impl == "reference":
+        line = run_reference_kernels(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference":
         if wl.get("kind") == "batch":
             if rank == 0:
@@ -962,7 +1181,9 @@ def main() -> None:
     if rank != 0:
         build()  # no-op once rank 0 built it
     args.cpu_baseline = args.cpu_baseline and rank == 0 and world == 1
-    if args.delivery_sweep:
+    if args.reference_kernels:
+        line = run_our_reference_kernels(args, rank, local_rank)
+    elif args.delivery_sweep:
         line = run_delivery_sweep(args, wl, rank, local_rank)
     else:
         runner = {"cg": run_cg, "batch": run_batch}.get(wl.get("kind"), run_ours)

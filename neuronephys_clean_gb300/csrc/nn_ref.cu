@@ -56,11 +56,11 @@ __device__ __forceinline__ float lf_rate_an(float V)
     return (float)((-0.5 - 0.01 * V) / (exp(-5 - 0.1 * V) - 1));
 }
 
-template <bool EXT_Z>
-__global__ void __launch_bounds__(256) k_leapfrog(LFVars s, int n, float timestep, nn_leapfrog_params p,
-                                                  uint64_t seed, uint64_t step, const float* __restrict__ z)
+// One neuron's step (zi: its standard-normal noise draw).
+__device__ __forceinline__ void lf_neuron(const LFVars& s, int i, float timestep, const nn_leapfrog_params& p,
+                                          float zi)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    {
         const float local_in = s.v[NN_HH_LOCAL_IN][i], local_num_in = s.v[NN_HH_LOCAL_COUNT][i];
         const float Iin = s.v[NN_HH_IIN][i], Inum_in = s.v[NN_HH_ICOUNT][i];
         const float Ein = s.v[NN_HH_EIN][i], Enum_in = s.v[NN_HH_ECOUNT][i];
@@ -111,7 +111,6 @@ __global__ void __launch_bounds__(256) k_leapfrog(LFVars s, int n, float timeste
         E = __fmaf_rn(__fmul_rn(p.g_gaba, new_IY), p.e_gaba, E);
         E = __fadd_rn(E, __fmul_rn(__fmul_rn(p.g_exc, new_EY), p.e_exc));
 
-        const float zi = EXT_Z ? z[i] : nn_normal(seed, (uint32_t)i, step);
         const float white_noise = __fmaf_rn(p.noise_intensity, zi, p.noise_mean);
         const float half_dt = timestep / 2;
         float num = __fmaf_rn(E, timestep, __fmul_rn(__fadd_rn(white_noise, appcur), timestep));
@@ -131,6 +130,28 @@ __global__ void __launch_bounds__(256) k_leapfrog(LFVars s, int n, float timeste
     }
 }
 
+// A thread steps the neuron pair (2k, 2k + 1), which shares one draw of the
+// counter-based noise stream (the pair's two Box-Muller outputs).
+template <bool EXT_Z>
+__global__ void __launch_bounds__(256) k_leapfrog(LFVars s, int n, float timestep, nn_leapfrog_params p,
+                                                  uint64_t seed, uint64_t step, const float* __restrict__ z)
+{
+    const int pairs = (n + 1) >> 1;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < pairs; k += gridDim.x * blockDim.x) {
+        const int i0 = 2 * k;
+        const bool two = i0 + 1 < n;
+        float z0, z1;
+        if (EXT_Z) {
+            z0 = z[i0];
+            z1 = two ? z[i0 + 1] : 0.0f;
+        } else {
+            nn_normal_pair(seed, (uint32_t)k, step, z0, z1);
+        }
+        lf_neuron(s, i0, timestep, p, z0);
+        if (two) lf_neuron(s, i0 + 1, timestep, p, z1);
+    }
+}
+
 nn_status leapfrog_launch(nn_ctx* ctx, float* const* vars, int n, float dt, const nn_leapfrog_params* p,
                           uint64_t seed, uint64_t step, const float* d_z, const char* what)
 {
@@ -141,7 +162,7 @@ nn_status leapfrog_launch(nn_ctx* ctx, float* const* vars, int n, float dt, cons
         if (!vars[q]) return nn_fail(ctx, NN_ERR_INVALID_ARG, "%s: sim_vars[%d] is NULL", what, q);
         s.v[q] = vars[q];
     }
-    const int grid = nn_grid_for(ctx, n, 256, 16);
+    const int grid = nn_grid_for(ctx, ((int64_t)n + 1) / 2, 256, 64);
     if (d_z) k_leapfrog<true><<<grid, 256, 0, ctx->stream>>>(s, n, dt, *p, seed, step, d_z);
     else k_leapfrog<false><<<grid, 256, 0, ctx->stream>>>(s, n, dt, *p, seed, step, nullptr);
     NN_CHECK_LAUNCH(ctx, "k_leapfrog");

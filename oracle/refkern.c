@@ -218,3 +218,59 @@ RK_API int rk_time_signal_spikes(int variant, int num_firing, uint64_t d_conn, u
     *ms = t / (float)reps;
     return 0;
 }
+
+/* Device memory for callers that use the harness without the product
+ * library (the benchmark's reference arm). */
+RK_API int rk_malloc(uint64_t bytes, uint64_t* dptr)
+{
+    if (!g_loaded || !dptr) {
+        snprintf(g_err, sizeof g_err, "rk_malloc: not loaded or bad argument");
+        return -1;
+    }
+    CUdeviceptr p = 0;
+    RK_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+    RK_TRY(cuMemAlloc(&p, (size_t)(bytes ? bytes : 1)), "cuMemAlloc");
+    *dptr = (uint64_t)p;
+    return 0;
+}
+
+RK_API int rk_free(uint64_t dptr)
+{
+    if (!g_loaded) return -1;
+    RK_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+    RK_TRY(cuMemFree((CUdeviceptr)dptr), "cuMemFree");
+    return 0;
+}
+
+RK_API int rk_h2d(uint64_t dst, const void* src, uint64_t bytes)
+{
+    if (!g_loaded) return -1;
+    RK_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+    RK_TRY(cuMemcpyHtoD((CUdeviceptr)dst, src, (size_t)bytes), "cuMemcpyHtoD");
+    return 0;
+}
+
+RK_API int rk_d2h(void* dst, uint64_t src, uint64_t bytes)
+{
+    if (!g_loaded) return -1;
+    RK_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+    RK_TRY(cuMemcpyDtoH(dst, (CUdeviceptr)src, (size_t)bytes), "cuMemcpyDtoH");
+    return 0;
+}
+
+RK_API int rk_memset(uint64_t dst, uint64_t bytes)
+{
+    if (!g_loaded) return -1;
+    RK_TRY(cuCtxSetCurrent(g_ctx), "cuCtxSetCurrent");
+    RK_TRY(cuMemsetD8((CUdeviceptr)dst, 0, (size_t)bytes), "cuMemsetD8");
+    return 0;
+}
+
+RK_API int rk_num_sms(int* out)
+{
+    if (!g_loaded || !out) return -1;
+    CUdevice dev;
+    RK_TRY(cuCtxGetDevice(&dev), "cuCtxGetDevice");
+    RK_TRY(cuDeviceGetAttribute(out, CU_DEVICE_ATTRIBUTE_MULTIPROCESSOR_COUNT, dev), "cuDeviceGetAttribute");
+    return 0;
+}

@@ -59,6 +59,12 @@ def _load() -> C.CDLL:
             "rk_signal_spikes_chunked": (i, [i, u64, u64, u64, u64, u64, u64]),
             "rk_time_leapfrog": (i, [i, u64, i, f, u64, i, i, i, C.POINTER(f)]),
             "rk_time_signal_spikes": (i, [i, i, u64, u64, u64, u64, u64, i, i, i, C.POINTER(f)]),
+            "rk_malloc": (i, [u64, C.POINTER(u64)]),
+            "rk_free": (i, [u64]),
+            "rk_h2d": (i, [u64, C.c_void_p, u64]),
+            "rk_d2h": (i, [C.c_void_p, u64, u64]),
+            "rk_memset": (i, [u64, u64]),
+            "rk_num_sms": (i, [C.POINTER(i)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(l, name)
@@ -121,3 +127,30 @@ class RefKernels:
         self._check(self.lib.rk_time_signal_spikes(variant, num_firing, d_conn, d_off, d_firing, d_spikes, d_outputs,
                                                    grid, block, reps, C.byref(ms)))
         return ms.value
+
+    # device memory without the product library (the benchmark's reference arm)
+    def to_device(self, a: np.ndarray) -> int:
+        a = np.ascontiguousarray(a)
+        d = C.c_uint64()
+        self._check(self.lib.rk_malloc(a.nbytes, C.byref(d)))
+        self._check(self.lib.rk_h2d(d.value, a.ctypes.data, a.nbytes))
+        return d.value
+
+    def zeros(self, nbytes: int) -> int:
+        d = C.c_uint64()
+        self._check(self.lib.rk_malloc(nbytes, C.byref(d)))
+        self._check(self.lib.rk_memset(d.value, nbytes))
+        return d.value
+
+    def to_host(self, dptr: int, shape, dtype) -> np.ndarray:
+        out = np.empty(shape, dtype)
+        self._check(self.lib.rk_d2h(out.ctypes.data, dptr, out.nbytes))
+        return out
+
+    def free(self, dptr: int) -> None:
+        self._check(self.lib.rk_free(dptr))
+
+    def num_sms(self) -> int:
+        n = C.c_int()
+        self._check(self.lib.rk_num_sms(C.byref(n)))
+        return n.value
