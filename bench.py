@@ -234,6 +234,9 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     sim = build_sim(nn, ctx, wl, raster=2_000_000 if args.cpu_baseline else 0)
     P = wl["total_steps"]  # timesteps per bench step: one full run of the workload
     n = wl["n"]
+    el_info = None
+    if args.electrodes > 0:
+        el_info = set_knn_electrodes(sim, args.electrodes, 50, args.electrode_every)
     # settle: start the timed region in steady tonic firing, not at rest
     sim.step(args.settle)
     for _ in range(args.warmup):  # warm-up also captures the period graph
@@ -337,6 +340,7 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded counter-based generators)",
         "config": workload_config(wl, nnz),
+        "electrodes": el_info,
         "synaptic_events_per_s": events / seconds if seconds else None,
         "spikes_in_timed_region": spikes,
         "cg": {"iterations_last_solve": st.iterations, "relres_last_solve": st.relres,
@@ -436,6 +440,24 @@ def c5_leg(nn, ctx, args) -> dict:
                           "cores": int(oracle.lib().orc_num_threads())}
     out["tolerance"] = "relative residual 1e-6 (FP64 reductions); error = |x - x_fp64| / |x_fp64|"
     return out
+
+
+def set_knn_electrodes(sim, count: int, k: int, every: int = 1, seed: int = 11) -> dict:
+    """ElectrodeNet's regions (Morphology::GenSphericalRegions,
+    src/morphology.cpp:48-72): the k nearest neurons of each of `count`
+    randomly chosen electrode neurons, recorded every `every` steps by the
+    fused recording."""
+    x, y, z = (sim.get_field(f).astype(np.float64) for f in ("X", "Y", "Z"))
+    n = len(x)
+    centers = np.random.default_rng(seed).choice(n, count, replace=False)
+    regions = []
+    for c in centers:
+        d2 = (x - x[c]) ** 2 + (y - y[c]) ** 2 + (z - z[c]) ** 2
+        regions.append(np.argpartition(d2, k)[:k])
+    idx = np.concatenate(regions).astype(np.int32)
+    off = (np.arange(count + 1) * k).astype(np.int32)
+    sim.set_electrodes(idx, off, every=every, capacity=1024)
+    return {"regions": count, "neurons_per_region": k, "every_steps": every}
 
 
 def workload_config(wl: dict, nnz: int) -> dict:
@@ -1149,6 +1171,10 @@ def main() -> None:
     ap.add_argument("--reference-kernels", action="store_true",
                     help="time the reference-semantics leapfrog and count coupling at 1M neurons: the reference's "
                          "own kernels with --impl reference, the library's drop-ins otherwise (one JSON line)")
+    ap.add_argument("--electrodes", type=int, default=0,
+                    help="record this many KNN electrode regions (50 neurons each), fused into the update")
+    ap.add_argument("--electrode-every", type=int, default=1,
+                    help="electrode sampling interval in steps (40 = 0.4 ms, the reference's leapfrog step)")
     ap.add_argument("--no-c5", dest="c5", action="store_false",
                     help="default workload: skip the 256^3 CG time-to-tolerance leg")
     ap.add_argument("--no-learned", dest="learned", action="store_false",

@@ -342,6 +342,23 @@ NN_API nn_status nn_sim_run_host(nn_sim* s, const float* h_state_in, int nsteps,
                                  int64_t* h_spikes);
 /* Current step index and total spikes so far (synchronises). */
 NN_API nn_status nn_sim_counters(nn_sim* s, int64_t* step, int64_t* total_spikes);
+/* ElectrodeNet (src/electrode_net.cu:3-49; src_wholebrain/electrode_net.cu:3-54),
+ * fused into the step: regions as ElectrodeNet takes them (h_indices: the
+ * neurons of each region, h_offsets[n_regions + 1]; regions may overlap).
+ * On every step t with t % every == 0 (from the next such step on) the neuron
+ * update records the new membrane potential and the spike of step t of every
+ * neuron listed in a region; nn_sim_read_electrodes turns them into each
+ * region's mean potential (FP64 sum) and firing count after that step, as
+ * DoElectrodeMeasurements computes them.  Samples are kept in a ring of
+ * `capacity` slots (the oldest are overwritten).  every = 0 turns the
+ * recording off. */
+NN_API nn_status nn_sim_set_electrodes(nn_sim* s, const int* h_indices, const int* h_offsets, int n_regions,
+                                       int every, int capacity);
+/* The recorded samples, oldest first: h_avg / h_firing (host, [capacity]
+ * [n_regions], either may be NULL) get mean potentials and firing counts,
+ * *first_step the step of the first returned sample, *n_samples their number. */
+NN_API nn_status nn_sim_read_electrodes(nn_sim* s, float* h_avg, int* h_firing, int64_t* first_step,
+                                        int* n_samples);
 /* Download the delay ring: D = max_delay + 1 slots of n (excitatory,
  * inhibitory) input pairs, h_ring float[D * n * 2]; slot (t mod D) holds the
  * input the neurons take at step t.  With the step counter and the neuron

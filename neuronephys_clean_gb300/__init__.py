@@ -534,6 +534,29 @@ class Simulation:
                "run_host")
         return sp.value
 
+    def set_electrodes(self, regions_inds, regions_offsets, every: int = 1, capacity: int = 1024) -> None:
+        """ElectrodeNet fused into the step (nn_sim_set_electrodes): regions
+        as index lists (CSR), sampled every `every` steps into a ring of
+        `capacity` samples; every = 0 turns it off."""
+        ind = np.ascontiguousarray(regions_inds, np.int32)
+        off = np.ascontiguousarray(regions_offsets, np.int32)
+        self._el_regions = len(off) - 1
+        self._el_cap = capacity
+        _check(lib().nn_sim_set_electrodes(self.handle, _ptr(ind), _ptr(off), self._el_regions, every, capacity),
+               self.ctx, "set_electrodes")
+
+    def read_electrodes(self):
+        """(first step, mean potentials [samples, regions], firing counts
+        [samples, regions]) of the recorded samples, oldest first."""
+        R = getattr(self, "_el_regions", 0)
+        cap = max(getattr(self, "_el_cap", 1), 1)
+        avg = np.zeros((cap, max(R, 1)), np.float32)
+        fire = np.zeros((cap, max(R, 1)), np.int32)
+        first, k = C.c_int64(0), C.c_int(0)
+        _check(lib().nn_sim_read_electrodes(self.handle, _ptr(avg), _ptr(fire), C.byref(first), C.byref(k)),
+               self.ctx, "read_electrodes")
+        return int(first.value), avg[:k.value, :R], fire[:k.value, :R]
+
     def get_ring(self) -> np.ndarray:
         """Delay ring as (D, n, 2) float32: slot t mod D holds the (E, I)
         input of step t."""

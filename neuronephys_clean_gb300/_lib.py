@@ -122,6 +122,8 @@ _SIGS = {
     "nn_sim_init_state": (c_int, [c_void_p, c_float, c_float, c_float]),
     "nn_sim_step": (c_int, [c_void_p, c_int]),
     "nn_sim_run_host": (c_int, [c_void_p, c_void_p, c_int, c_void_p, P(c_int64)]),
+    "nn_sim_set_electrodes": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
+    "nn_sim_read_electrodes": (c_int, [c_void_p, c_void_p, c_void_p, P(c_int64), P(c_int)]),
     "nn_sim_get_ring": (c_int, [c_void_p, c_void_p]),
     "nn_sim_reset_raster": (c_int, [c_void_p]),
     "nn_sim_counters": (c_int, [c_void_p, P(c_int64), P(c_int64)]),

@@ -34,6 +34,7 @@
 #include <type_traits>
 
 #include "nn_internal.cuh"
+#include "nn_ptx.cuh"
 
 namespace {
 constexpr int CG_THREADS = 256;
@@ -81,32 +82,8 @@ struct CgArgs {
     int max_iter;
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase)
-{
-    const uint32_t addr = smem_u32(bar);
-    for (uint32_t it = 0; it < WAIT_LIMIT; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(addr), "r"(phase)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
+// Bounded mbarrier wait of this kernel (nn_ptx.cuh), WAIT_LIMIT polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) { return nn_mbar_wait(bar, phase, WAIT_LIMIT); }
 
 // Abort path: wait (bounded) for the copies of planes first .. last to land.
 __device__ __noinline__ void drain_planes(uint64_t* bars, int first, int last, int stages)
@@ -116,10 +93,7 @@ __device__ __noinline__ void drain_planes(uint64_t* bars, int first, int last, i
 
 __device__ __forceinline__ void tma_load_plane(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar)
 {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
+    nn_tma_load_3d(dst, map, x, y, z, bar);
 }
 
 __device__ __forceinline__ float warp_sumf(float v)
@@ -296,7 +270,7 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg_iter(const __grid_constant
 
     if (tid == 0) {
         abort_flag = 0;
-        for (int q = 0; q < STAGES; ++q) mbar_init(&bars[q], 1);
+        for (int q = 0; q < STAGES; ++q) nn_mbar_init(&bars[q], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -307,7 +281,7 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg_iter(const __grid_constant
         uint64_t* bar = &bars[j % STAGES];
         const int kz = z0 - 1 + j;
         const bool own = j >= 1 && j <= np - 2;
-        mbar_expect_tx(bar, L::NARR * PLANE_BYTES + (own ? 2 * PX_BYTES : 0));
+        nn_mbar_expect_tx(bar, L::NARR * PLANE_BYTES + (own ? 2 * PX_BYTES : 0));
         tma_load_plane(st, &tm_r, x0 - 4, y0 - 1, kz, bar);
         tma_load_plane(st + PLANE_STRIDE, &tm_w, x0 - 4, y0 - 1, kz, bar);
         tma_load_plane(st + 2 * PLANE_STRIDE, &tm_s, x0 - 4, y0 - 1, kz, bar);

@@ -54,6 +54,16 @@ __device__ __forceinline__ void nn_bulk_g2s(void* dst, const void* src, uint32_t
                  : "memory");
 }
 
+// Tiled tensor copy global -> shared by the bulk-copy engine (3D tensor map,
+// box origin {x, y, z}; x times the element size a multiple of 16 bytes).
+__device__ __forceinline__ void nn_tma_load_3d(void* dst, const void* map, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(nn_smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(nn_smem_u32(bar))
+        : "memory");
+}
+
 // ------------------------------------------------------------- tcgen05 --
 
 // Shared-memory matrix descriptor, no swizzle (canonical layout of 8-row x

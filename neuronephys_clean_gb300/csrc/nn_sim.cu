@@ -97,6 +97,13 @@ struct nn_sim {
     bool solve_pending = false;
     int iter_estimate = 64;
     nn_solve_stats stats{};
+    // fused electrode recording (nn_sim_set_electrodes)
+    uint2* el_group = nullptr;     // per 32-neuron group: member bits, members before it
+    float* el_val = nullptr;       // [cap][members] potentials
+    uint8_t* el_spk = nullptr;     // [cap][members] spike flags
+    int el_every = 0, el_cap = 0, el_members = 0;
+    int64_t el_first = 0;          // step of the first sample
+    std::vector<int> el_roff, el_rpos;  // regions as lists of member positions
     // host mirrors
     int64_t host_step = 0;
     bool gna_set = false;  // per-neuron gNa scale given (else the kernel skips the load)
@@ -1037,6 +1044,12 @@ static StepArgs step_args(nn_sim* s, int q)
     a.rcap = s->cfg.raster_capacity;
     a.vox = s->vox;
     a.src = has_field(s) ? s->src : nullptr;
+    a.el_group = s->el_group;
+    a.el_val = s->el_val;
+    a.el_spk = s->el_spk;
+    a.el_every = s->el_every;
+    a.el_cap = s->el_cap;
+    a.el_members = s->el_members;
     a.err = s->err;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
     a.zero_ring = push;
@@ -1197,6 +1210,7 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     drop_graph(s);
     for (int q = 0; q < NN_F_COUNT; ++q) nn_release(s->f[q]);
     nn_release(s->ring); nn_release(s->bitmap); nn_release(s->list); nn_release(s->counts); nn_release(s->step);
+    nn_release(s->el_group); nn_release(s->el_val); nn_release(s->el_spk);
     nn_release(s->total); nn_release(s->rcount); nn_release(s->raster); nn_release(s->err);
     nn_release(s->is_inh); nn_release(s->vox); nn_release(s->src); nn_release(s->u); nn_release(s->u_prev); nn_release(s->b);
     free_network(s);
@@ -2107,6 +2121,8 @@ extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, 
     if (st == NN_OK) st = save(s->total, sizeof(unsigned long long));
     if (st == NN_OK) st = save(s->rcount, sizeof(unsigned long long));
     if (st == NN_OK) st = save(s->src, has_field(s) ? (size_t)s->G * sizeof(float) : 0);
+    if (st == NN_OK) st = save(s->el_val, (size_t)s->el_cap * s->el_members * sizeof(float));
+    if (st == NN_OK) st = save(s->el_spk, (size_t)s->el_cap * s->el_members);
     const int old_tpb = s->tpb, old_npt = s->npt;
     const bool old_timing = s->timing;
     s->timing = false;
@@ -2255,6 +2271,94 @@ extern "C" nn_status nn_sim_counters(nn_sim* s, int64_t* step, int64_t* total_sp
     NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (step) *step = (int64_t)v[0];
     if (total_spikes) *total_spikes = (int64_t)v[1];
+    return check_err(s);
+}
+
+extern "C" nn_status nn_sim_set_electrodes(nn_sim* s, const int* h_indices, const int* h_offsets, int n_regions,
+                                           int every, int capacity)
+{
+    if (!s || n_regions < 0 || every < 0) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    drop_graph(s);  // the captured launches carry the recording's arguments
+    nn_release(s->el_group); nn_release(s->el_val); nn_release(s->el_spk);
+    s->el_every = s->el_cap = s->el_members = 0;
+    s->el_roff.clear();
+    s->el_rpos.clear();
+    if (every == 0 || n_regions == 0) return NN_OK;
+    if (!h_indices || !h_offsets || capacity < 1)
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_set_electrodes: regions and a capacity >= 1 needed");
+    if (h_offsets[0] != 0) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_set_electrodes: offsets[0] must be 0");
+    const int n = s->n;
+    // member positions in ascending neuron order; regions as lists of positions
+    std::vector<int> pos((size_t)n, -1);
+    for (int r = 0; r < n_regions; ++r) {
+        if (h_offsets[r + 1] < h_offsets[r])
+            return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_set_electrodes: offsets not monotone at %d", r);
+        for (int k = h_offsets[r]; k < h_offsets[r + 1]; ++k) {
+            const int i = h_indices[k];
+            if (i < 0 || i >= n) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_set_electrodes: index %d out of range", i);
+            pos[(size_t)i] = 0;
+        }
+    }
+    int members = 0;
+    std::vector<uint2> grp((size_t)s->n_pad / 32, make_uint2(0u, 0u));
+    for (int i = 0; i < n; ++i) {
+        if ((i & 31) == 0) grp[(size_t)i >> 5].y = (unsigned)members;
+        if (pos[(size_t)i] == 0) {
+            pos[(size_t)i] = members++;
+            grp[(size_t)i >> 5].x |= 1u << (i & 31);
+        }
+    }
+    s->el_roff.assign(h_offsets, h_offsets + n_regions + 1);
+    s->el_rpos.resize((size_t)h_offsets[n_regions]);
+    for (int k = 0; k < h_offsets[n_regions]; ++k) s->el_rpos[(size_t)k] = pos[(size_t)h_indices[k]];
+    const size_t cells = (size_t)capacity * members;
+    NN_TRY(nn_alloc(ctx, &s->el_group, grp.size()));
+    NN_TRY(nn_alloc(ctx, &s->el_val, cells));
+    NN_TRY(nn_alloc(ctx, &s->el_spk, cells));
+    NN_CUDA(ctx, nn_copy_sync(ctx, s->el_group, grp.data(), sizeof(uint2) * grp.size(), cudaMemcpyHostToDevice));
+    s->el_every = every;
+    s->el_cap = capacity;
+    s->el_members = members;
+    s->el_first = (s->host_step + every - 1) / every * every;
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_read_electrodes(nn_sim* s, float* h_avg, int* h_firing, int64_t* first_step,
+                                            int* n_samples)
+{
+    if (!s || !n_samples) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    *n_samples = 0;
+    if (first_step) *first_step = s->el_first;
+    if (s->el_every == 0) return NN_OK;
+    const int64_t E = s->el_every, M = s->el_members;
+    const int R = (int)s->el_roff.size() - 1;
+    const int64_t count = s->host_step > s->el_first ? (s->host_step - s->el_first - 1) / E + 1 : 0;
+    const int64_t kept = std::min<int64_t>(count, s->el_cap);
+    std::vector<float> val((size_t)s->el_cap * M);
+    std::vector<uint8_t> spk((size_t)s->el_cap * M);
+    NN_CUDA(ctx, cudaMemcpyAsync(val.data(), s->el_val, sizeof(float) * val.size(), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    NN_CUDA(ctx, cudaMemcpyAsync(spk.data(), s->el_spk, spk.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    NN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int64_t first_smp = s->el_first / E + (count - kept);
+    for (int64_t k = 0; k < kept; ++k) {
+        const size_t base = (size_t)((first_smp + k) % s->el_cap) * (size_t)M;
+        for (int r = 0; r < R; ++r) {
+            double v = 0.0;
+            int f = 0;
+            for (int q = s->el_roff[(size_t)r]; q < s->el_roff[(size_t)r + 1]; ++q) {
+                v += val[base + (size_t)s->el_rpos[(size_t)q]];
+                f += spk[base + (size_t)s->el_rpos[(size_t)q]];
+            }
+            const int sz = s->el_roff[(size_t)r + 1] - s->el_roff[(size_t)r];
+            if (h_avg) h_avg[k * R + r] = sz ? (float)(v / sz) : 0.0f;
+            if (h_firing) h_firing[k * R + r] = f;
+        }
+    }
+    if (first_step) *first_step = first_smp * E;
+    *n_samples = (int)kept;
     return check_err(s);
 }
 

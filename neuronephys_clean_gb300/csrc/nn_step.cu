@@ -21,12 +21,17 @@ namespace {
 // UNI: no per-neuron gNa scale and no paracrine feedback (the common case),
 // so the step's constant current terms are launch constants
 // (nn_hh_drive_uniform) rather than registers.
-template <int NPT, bool UNI>
+// EL: electrode recording compiled in (nn_sim_set_electrodes); without it
+// the update carries none of that code.
+template <int NPT, bool UNI, bool EL>
 __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
 {
     const uint64_t t = *a.base + (uint64_t)a.q;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.counts[(t + 1) & 1] = 0;  // next step's count
     const int slot = (int)(t % (uint64_t)a.D);
+    // electrode sample slot of this step (-1: no sample)
+    const int s_el =
+        (EL && t % (uint64_t)a.el_every == 0) ? (int)((t / (uint64_t)a.el_every) % (uint64_t)a.el_cap) : -1;
     float* ring_slot = a.ring + (size_t)slot * a.n_pad * 2;
     int* list = a.list + (size_t)(t & 1) * a.n_pad;
     int* cnt = a.counts + (t & 1);
@@ -35,6 +40,9 @@ __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int chunk = 32 * NPT;
+    // electrode sample of this step (nullptr: none)
+    float* el_v = EL && s_el >= 0 ? a.el_val + (size_t)s_el * a.el_members : nullptr;
+    uint8_t* el_s = EL && s_el >= 0 ? a.el_spk + (size_t)s_el * a.el_members : nullptr;
     const int nchunks = a.n_pad / chunk;
     for (int ch = warp; ch < nchunks; ch += nwarps) {
         const int i0 = ch * chunk + lane * NPT;
@@ -125,6 +133,24 @@ __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
             }
         }
         if (bad) atomicOr(a.err, 1);
+        // ElectrodeNet::DoElectrodeMeasurements fused: member neurons record
+        // their potential and spike.  A lane's NPT neurons lie in one 32-neuron
+        // group; its member bits and count of earlier members give the
+        // position (most groups hold no member).
+        if (EL && el_v) {
+            const uint2 gm = a.el_group[i0 >> 5];
+            if (gm.x) {
+#pragma unroll
+                for (int q = 0; q < NPT; ++q) {
+                    const int b = (i0 + q) & 31;
+                    if ((gm.x >> b) & 1u) {
+                        const int pos = (int)gm.y + __popc(gm.x & ((1u << b) - 1u));
+                        el_v[pos] = V[q];
+                        el_s[pos] = (mask >> q) & 1u;
+                    }
+                }
+            }
+        }
         // spike bitmap word of 32 consecutive neurons (pull delivery)
         if (bm) {
             uint32_t bits = mask << ((lane * NPT) & 31);
@@ -204,13 +230,20 @@ cudaError_t nn_launch_hh_step(const StepArgs& a, int npt, int blocks, int tpb, c
     // feed back (g_par = 0 or no density input): then ngna = -gNa and
     // ngpu = 0 (or -0) for every neuron, as the general form computes them
     const bool uni = !a.gna_scale && (!a.upar || a.p.g_par == 0.0f);
-    switch (npt * 2 + (uni ? 1 : 0)) {
-        case 2: k_hh_step<1, false><<<blocks, tpb, 0, cs>>>(a); break;
-        case 3: k_hh_step<1, true><<<blocks, tpb, 0, cs>>>(a); break;
-        case 4: k_hh_step<2, false><<<blocks, tpb, 0, cs>>>(a); break;
-        case 5: k_hh_step<2, true><<<blocks, tpb, 0, cs>>>(a); break;
-        case 8: k_hh_step<4, false><<<blocks, tpb, 0, cs>>>(a); break;
-        default: k_hh_step<4, true><<<blocks, tpb, 0, cs>>>(a); break;
+    const bool el = a.el_every > 0;
+    switch (npt * 4 + (uni ? 2 : 0) + (el ? 1 : 0)) {
+        case 4: k_hh_step<1, false, false><<<blocks, tpb, 0, cs>>>(a); break;
+        case 5: k_hh_step<1, false, true><<<blocks, tpb, 0, cs>>>(a); break;
+        case 6: k_hh_step<1, true, false><<<blocks, tpb, 0, cs>>>(a); break;
+        case 7: k_hh_step<1, true, true><<<blocks, tpb, 0, cs>>>(a); break;
+        case 8: k_hh_step<2, false, false><<<blocks, tpb, 0, cs>>>(a); break;
+        case 9: k_hh_step<2, false, true><<<blocks, tpb, 0, cs>>>(a); break;
+        case 10: k_hh_step<2, true, false><<<blocks, tpb, 0, cs>>>(a); break;
+        case 11: k_hh_step<2, true, true><<<blocks, tpb, 0, cs>>>(a); break;
+        case 16: k_hh_step<4, false, false><<<blocks, tpb, 0, cs>>>(a); break;
+        case 17: k_hh_step<4, false, true><<<blocks, tpb, 0, cs>>>(a); break;
+        case 18: k_hh_step<4, true, false><<<blocks, tpb, 0, cs>>>(a); break;
+        default: k_hh_step<4, true, true><<<blocks, tpb, 0, cs>>>(a); break;
     }
     return cudaPeekAtLastError();
 }

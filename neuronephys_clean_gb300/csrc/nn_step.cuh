@@ -30,6 +30,15 @@ struct StepArgs {
     long long rcap;
     const int32_t* vox;
     float* src;
+    // fused electrode recording (el_every > 0): on steps t with t % el_every
+    // == 0 each member neuron (a neuron of some region) writes its new
+    // potential and its spike flag to its member position (members in
+    // ascending neuron order) of sample slot
+    // (t / el_every) % el_cap; the host forms the region means and counts
+    const uint2* el_group;    // per 32-neuron group g (neurons 32g .. 32g+31): {member bits, members before g}
+    float* el_val;            // [el_cap][el_members]
+    uint8_t* el_spk;          // [el_cap][el_members]
+    int el_every, el_cap, el_members;
     int* err;
     int n, n_pad, D, words;
     int zero_ring;

@@ -6,6 +6,8 @@
     python -m neuronephys_clean_gb300.profile_cases conv128  # 3x3x3 convs (16->16, 48->16) + wgrad at 128^3
     python -m neuronephys_clean_gb300.profile_cases mg256    # multigrid FCG solve to 1e-6, 256^3, lognormal D
     python -m neuronephys_clean_gb300.profile_cases pull1m   # one pull gather, 1M neurons, 1e8 synapses, delays 1..20
+    python -m neuronephys_clean_gb300.profile_cases burst1m  # 200 steps of the 1M-neuron workload from rest: its first burst
+    python -m neuronephys_clean_gb300.profile_cases burst1m_steps  # its first 400 steps timed one by one (no ncu)
 
 Each case holds a few GB at most and launches a handful of kernels, so that
 an ncu capture of it ends by itself; every case also runs without ncu.
@@ -93,11 +95,57 @@ def pull1m(ctx):
     s.deliver_spikes(ctx.to_device(lst), len(lst), nn.NN_DELIVERY_PULL)
 
 
-CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128, "mg256": mg256, "pull1m": pull1m}
+def _burst_sim(ctx):
+    n = 1_000_000
+    c = nn.default_config(n)
+    c.seed, c.max_delay = 1, 20
+    s = nn.Simulation(ctx, c)
+    sp = nn.default_net_spec(nn.NN_NET_GAUSS)
+    sp.k, sp.sigma, sp.w_mu, sp.w_sigma, sp.dmax = 100, 0.1, -1.0, 1.0, 20
+    sp.inh_fraction, sp.inh_random = 0.2, 1
+    s.generate_network(sp)
+    s.init_state(-65.0, 6.0, 12.0)
+    return s
+
+
+def burst1m_steps(ctx):
+    """The same 400 steps one at a time, each timed with CUDA events, printed
+    as step time against spikes per step (JSON)."""
+    import json
+    s = _burst_sim(ctx)
+    ms, spk = [], []
+    _, t0 = s.counters()
+    for _ in range(400):
+        ctx.time_begin()
+        s.step(1)
+        ms.append(ctx.time_end())
+        _, t1 = s.counters()
+        spk.append(t1 - t0)
+        t0 = t1
+    ms, spk = np.array(ms), np.array(spk)
+    out = {"quiet_median_ms": float(np.median(ms[spk < 10]))}
+    for lo, hi in ((10, 1000), (1000, 5000), (5000, 20000), (20000, 10 ** 9)):
+        m = (spk >= lo) & (spk < hi)
+        if m.any():
+            out[f"spikes_{lo}_{hi}"] = {"steps": int(m.sum()), "mean_ms": float(ms[m].mean()),
+                                        "mean_spikes": float(spk[m].mean())}
+    print(json.dumps(out))
+
+
+def burst1m(ctx):
+    """The 1M-neuron workload (Gaussian network, 100 synapses per neuron,
+    delays 1..20, no field) for 200 steps from rest: its first population
+    burst (the neuron updates from step ~120 on carry thousands of spikes per
+    step, pushed inside the kernel)."""
+    _burst_sim(ctx).step(200)
+
+
+CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128, "mg256": mg256, "pull1m": pull1m,
+         "burst1m": burst1m, "burst1m_steps": burst1m_steps}
 
 
 def main(argv: list[str]) -> None:
-    names = argv or list(CASES)
+    names = argv or [c for c in CASES if c != "burst1m_steps"]
     ctx = nn.Context(0)
     for name in names:
         CASES[name](ctx)

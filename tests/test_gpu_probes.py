@@ -30,6 +30,56 @@ def test_electrodes(ctx):
     assert abs(m - V.astype(np.float64).mean()) <= 1e-5 * abs(V).max()
 
 
+def _electrode_sim(ctx, n=20000, seed=3):
+    c = nn.default_config(n)
+    c.seed, c.max_delay, c.raster_capacity = seed, 20, 1_000_000
+    s = nn.Simulation(ctx, c)
+    spec = nn.default_net_spec(nn.NN_NET_GAUSS)
+    spec.k, spec.dmax = 30, 20
+    s.generate_network(spec)
+    s.init_state(-65.0, 6.0, 12.0)
+    s.set_field("V", np.random.default_rng(seed).uniform(-65, -30, n).astype(np.float32))
+    return s
+
+
+@pytest.mark.parametrize("every,capacity,steps", [(3, 8, 22), (1, 4, 12)])
+def test_electrodes_fused_into_step(ctx, every, capacity, steps):
+    """nn_sim_set_electrodes: the recording fused into the neuron update
+    against the numpy restatement of ElectrodeNet::DoElectrodeMeasurements
+    (oracle/probes.py) on the states and spikes of the same steps: region
+    means within 1e-5 relative (FP64 sums here, the reference's sequential
+    FP32 sum there), firing counts exact.
+    Overlapping regions; a ring smaller than the run keeps the last
+    `capacity` samples."""
+    n, R = 20000, 30
+    rng = np.random.default_rng(7)
+    sizes = rng.integers(1, 200, R)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    idx = rng.integers(0, n, off[-1]).astype(np.int32)
+    s = _electrode_sim(ctx, n)
+    s.step(41)  # into the spiking
+    s.set_electrodes(idx, off, every=every, capacity=capacity)
+    want = {}
+    for t in range(41, 41 + steps):
+        s.step(1)
+        if t % every == 0:
+            want[t] = s.get_field("V")
+    st, ne = s.raster()
+    first, avg, fire = s.read_electrodes()
+    sample_steps = sorted(want)[-capacity:]
+    assert first == sample_steps[0] and len(avg) == len(sample_steps)
+    assert sum(len(ne[st == t]) for t in sample_steps) > 0
+    for k, t in enumerate(sample_steps):
+        spiked = np.zeros(n, np.int32)
+        spiked[ne[st == t]] = 1
+        ravg, rfire = P.electrodes_measure(idx, off, want[t], spiked)
+        np.testing.assert_allclose(avg[k], ravg, rtol=1e-5, atol=1e-4)
+        assert np.array_equal(fire[k], rfire), t
+    s.set_electrodes(idx, off, every=0)
+    assert s.read_electrodes()[1].shape[0] == 0
+    s.close()
+
+
 def test_synchrony(ctx):
     rng = np.random.default_rng(1)
     n = 4000
