@@ -231,7 +231,8 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     import neuronephys_clean_gb300 as nn
     ctx = nn.Context(local_rank)
     # the raster records the parity window's spikes (restarted before it)
-    sim = build_sim(nn, ctx, wl, raster=2_000_000 if args.cpu_baseline else 0)
+    sim = build_sim(nn, ctx, wl, raster=2_000_000 if args.cpu_baseline else 0,
+                    delivery=DELIVERY_MODES[args.delivery])
     P = wl["total_steps"]  # timesteps per bench step: one full run of the workload
     n = wl["n"]
     el_info = None
@@ -242,6 +243,8 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     for _ in range(args.warmup):  # warm-up also captures the period graph
         sim.step(P)
     ctx.synchronize()
+    if args.delivery == "auto":
+        sim.delivery_log(reset=True)
     launches0 = ctx.kernel_launches
     _, spikes_a = sim.counters()
     clocks = ClockSampler(local_rank)
@@ -255,6 +258,16 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     barrier(dist)
     launches = ctx.kernel_launches - launches0
     _, spikes_b = sim.counters()
+    delivery_info = {"mode": args.delivery}
+    if args.delivery == "auto":
+        modes, rates = sim.delivery_log(reset=True)
+        delivery_info.update({
+            "pull_rate": float(sim.config.pull_rate),
+            "periods_push": int((modes == 0).sum()), "periods_pull": int((modes == 1).sum()),
+            "modes": "".join("L" if m else "S" for m in modes.tolist()),
+            "max_measured_rate": float(rates.max()) if len(rates) else None,
+            "rule": "each period of the timed region: pull (L) when the latest measured period fired at least "
+                    "pull_rate spikes per neuron and step, else push (S)"})
     st = sim.solve_stats()
     seconds = ms / 1e3
     units = float(n) * P * args.steps
@@ -339,7 +352,8 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded counter-based generators)",
-        "config": workload_config(wl, nnz),
+        "config": workload_config(wl, nnz, args.delivery),
+        "delivery": delivery_info,
         "electrodes": el_info,
         "synaptic_events_per_s": events / seconds if seconds else None,
         "spikes_in_timed_region": spikes,
@@ -460,11 +474,14 @@ def set_knn_electrodes(sim, count: int, k: int, every: int = 1, seed: int = 11) 
     return {"regions": count, "neurons_per_region": k, "every_steps": every}
 
 
-def workload_config(wl: dict, nnz: int) -> dict:
+DELIVERY_MODES = {"push": 0, "pull": 1, "auto": 2}
+
+
+def workload_config(wl: dict, nnz: int, delivery: str) -> dict:
     """The `config` object of both arms' lines for a single-network workload."""
     n = wl["n"]
     return {"workload": wl["workload"], "neurons": n, "synapses": int(nnz), "timesteps_per_step": wl["total_steps"],
-            "dt_ms": 0.01, "grid": wl["grid"], "delivery": "push", "parallelism": "replicas",
+            "dt_ms": 0.01, "grid": wl["grid"], "delivery": delivery, "parallelism": "replicas",
             "l2": f"inputs larger than L2 (CSR {nnz * 9 / 1e9:.1f} GB, ring "
                   f"{(wl['dmax'] + 1) * n * 8 / 1e6:.0f} MB, state {n * 28 / 1e6:.0f} MB per step)"}
 
@@ -1019,7 +1036,7 @@ def run_reference(args, wl: dict, rank: int) -> dict | None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sample * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded counter-based generators)", "impl": "reference",
-            "config": workload_config(wl, len(net.col)),
+            "config": workload_config(wl, len(net.col), args.delivery),
             "spikes_in_timed_region": spikes, "synaptic_events_per_s": events / sum(times),
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": "neuron-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -1173,6 +1190,8 @@ def main() -> None:
                          "own kernels with --impl reference, the library's drop-ins otherwise (one JSON line)")
     ap.add_argument("--electrodes", type=int, default=0,
                     help="record this many KNN electrode regions (50 neurons each), fused into the update")
+    ap.add_argument("--delivery", choices=sorted(DELIVERY_MODES), default="auto",
+                    help="spike delivery: push, pull, or auto (per period by the measured firing rate)")
     ap.add_argument("--electrode-every", type=int, default=1,
                     help="electrode sampling interval in steps (40 = 0.4 ms, the reference's leapfrog step)")
     ap.add_argument("--no-c5", dest="c5", action="store_false",

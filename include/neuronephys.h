@@ -221,14 +221,18 @@ typedef struct nn_hh_params {
 } nn_hh_params;
 NN_API void nn_hh_params_standard(nn_hh_params* p);
 
-enum { NN_DELIVERY_PUSH = 0, NN_DELIVERY_PULL = 1 };
+/* Spike delivery (SignalSpikes / signal_spikes_kernel, src/coupling.cu:111-178,
+ * is push only).  NN_DELIVERY_AUTO chooses per period of steps: pull when the
+ * last measured period fired at least pull_rate of the neurons per step, else
+ * push; the spikes in flight are carried across a change of mode. */
+enum { NN_DELIVERY_PUSH = 0, NN_DELIVERY_PULL = 1, NN_DELIVERY_AUTO = 2 };
 
 typedef struct nn_sim_config {
     int n;                 /* neurons */
     int max_delay;         /* largest synaptic delay in steps (>= 1) */
     uint64_t seed;         /* master seed of every counter-based stream */
     nn_hh_params hp;
-    int delivery;          /* NN_DELIVERY_PUSH or NN_DELIVERY_PULL */
+    int delivery;          /* NN_DELIVERY_PUSH, NN_DELIVERY_PULL or NN_DELIVERY_AUTO */
     int64_t raster_capacity; /* spikes recorded as (step, neuron); 0 = off */
     /* paracrine field: grid^3 cells over the unit cube, solved every
      * `timescale` steps with dt_solve = timescale * dt */
@@ -245,6 +249,8 @@ typedef struct nn_sim_config {
     int par_extrapolate;   /* 1: initial guess 2 u_n - u_(n-1) from the second solve on; 0 (default): u_n.
                               Helps when the sources change slowly; with spike deposits that are new every
                               period it costs iterations (95 -> 103 on the 1M-neuron workload). */
+    float pull_rate;       /* NN_DELIVERY_AUTO: spikes per neuron and step at or above which a period runs
+                              pull delivery (default 0.025, the crossover measured on the 1M-neuron workload) */
 } nn_sim_config;
 NN_API void nn_sim_config_default(nn_sim_config* c, int n);
 
@@ -335,6 +341,15 @@ NN_API nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int count, 
  * shared memory; *cols = columns per block), 0 for the warp-per-column
  * kernel.  No counterpart in the reference. */
 NN_API nn_status nn_sim_pull_info(nn_sim* s, int* sliced, int* cols);
+/* NN_DELIVERY_AUTO: the delivery mode of each period run since the last call
+ * with reset != 0 (0 push, 1 pull) and the firing rate that chose it (spikes
+ * per neuron and step of the latest period measured when it was enqueued;
+ * -1 before the first measurement).  Up to cap entries are written, *count
+ * receives the number of periods logged. */
+NN_API nn_status nn_sim_delivery_log(nn_sim* s, int8_t* h_modes, float* h_rates, int cap, int* count, int reset);
+/* NN_DELIVERY_AUTO: change the pull threshold (config field pull_rate) for the
+ * periods enqueued from now on. */
+NN_API nn_status nn_sim_set_pull_rate(nn_sim* s, float pull_rate);
 /* End-to-end call: copy the state (6*n floats: V,m,h,n,ge,gi planes) from
  * host memory, advance nsteps, copy the state back and return the number of
  * spikes emitted. */

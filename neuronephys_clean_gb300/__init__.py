@@ -29,7 +29,7 @@ __all__ = ["NNError", "Context", "DeviceArray", "HHEphys", "AtomicCoupling", "Ad
            "lib", "NN_SIGNAL_COUNT", "NN_SIGNAL_OUTPUT", "FIELDS"]
 
 NN_SIGNAL_COUNT, NN_SIGNAL_OUTPUT = 0, 1
-NN_DELIVERY_PUSH, NN_DELIVERY_PULL = 0, 1
+NN_DELIVERY_PUSH, NN_DELIVERY_PULL, NN_DELIVERY_AUTO = 0, 1, 2
 NN_NET_ER, NN_NET_GAUSS, NN_NET_BLOCK = 1, 2, 3
 NN_ERR_NOT_CONVERGED = 4
 FIELDS = {name: i for i, name in enumerate(
@@ -527,6 +527,22 @@ class Simulation:
         a, b = C.c_int(0), C.c_int(0)
         _check(lib().nn_sim_pull_info(self.handle, C.byref(a), C.byref(b)), self.ctx, "sim_pull_info")
         return bool(a.value), b.value
+
+    def set_pull_rate(self, rate: float) -> None:
+        """Automatic delivery: pull threshold (spikes per neuron and step) for
+        the periods enqueued from now on."""
+        _check(lib().nn_sim_set_pull_rate(self.handle, rate), self.ctx, "sim_set_pull_rate")
+
+    def delivery_log(self, reset: bool = False) -> tuple[np.ndarray, np.ndarray]:
+        """Automatic delivery: (mode of each period since the last reset, 0 push
+        1 pull; the measured spikes per neuron and step that chose it)."""
+        cnt = C.c_int(0)
+        _check(lib().nn_sim_delivery_log(self.handle, None, None, 0, C.byref(cnt), 0), self.ctx, "sim_delivery_log")
+        modes = np.zeros(max(cnt.value, 1), np.int8)
+        rates = np.zeros(max(cnt.value, 1), np.float32)
+        _check(lib().nn_sim_delivery_log(self.handle, _ptr(modes), _ptr(rates), cnt.value, C.byref(cnt),
+                                         1 if reset else 0), self.ctx, "sim_delivery_log")
+        return modes[:cnt.value], rates[:cnt.value]
 
     def run_host(self, state_in: np.ndarray, nsteps: int, state_out: np.ndarray) -> int:
         sp = C.c_int64()

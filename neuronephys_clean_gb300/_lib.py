@@ -41,7 +41,8 @@ class SimConfig(C.Structure):
                 ("delivery", c_int), ("raster_capacity", c_int64), ("grid", c_int),
                 ("timescale", c_int), ("par_D", c_float), ("par_decay", c_float),
                 ("par_rtol", c_double), ("par_max_iter", c_int), ("threads_per_block", c_int),
-                ("neurons_per_thread", c_int), ("par_overlap", c_int), ("par_extrapolate", c_int)]
+                ("neurons_per_thread", c_int), ("par_overlap", c_int), ("par_extrapolate", c_int),
+                ("pull_rate", c_float)]
 
 
 class NetSpec(C.Structure):
@@ -140,6 +141,8 @@ _SIGS = {
     "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
     "nn_sim_deliver_spikes": (c_int, [c_void_p, c_void_p, c_int, c_int]),
     "nn_sim_pull_info": (c_int, [c_void_p, P(c_int), P(c_int)]),
+    "nn_sim_delivery_log": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_int), c_int]),
+    "nn_sim_set_pull_rate": (c_int, [c_void_p, c_float]),
     "nn_sim_set_instances": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "nn_sim_field_cells": (c_int, [c_void_p, P(c_int64)]),
     "nn_sim_get_vox": (c_int, [c_void_p, c_void_p]),

@@ -104,6 +104,22 @@ struct nn_sim {
     int el_every = 0, el_cap = 0, el_members = 0;
     int64_t el_first = 0;          // step of the first sample
     std::vector<int> el_roff, el_rpos;  // regions as lists of member positions
+    // automatic delivery (NN_DELIVERY_AUTO): the mode of the periods being
+    // enqueued (0 push, 1 pull), the ring rows' modes on the device, and the
+    // spike totals read back after each period (pinned, asynchronous)
+    int* rowflag = nullptr;        // [D]
+    int cur_mode = 0;
+    cudaGraphExec_t graph_pull = nullptr;
+    static constexpr int TOT_Q = 4;
+    unsigned long long* h_tot = nullptr;  // pinned [TOT_Q]
+    cudaEvent_t ev_tot[TOT_Q] = {};
+    int64_t tot_step[TOT_Q] = {};
+    int tot_head = 0, tot_pending = 0;
+    unsigned long long base_tot = 0;
+    int64_t base_step = -1;        // step of base_tot (-1: none yet)
+    float last_rate = -1.0f;       // spikes per neuron and step of the latest measured period
+    std::vector<int8_t> mode_log;
+    std::vector<float> rate_log;
     // host mirrors
     int64_t host_step = 0;
     bool gna_set = false;  // per-neuron gNa scale given (else the kernel skips the load)
@@ -144,6 +160,11 @@ struct PullArgs {
     const float* dsl_w;
     uint2* dsl_hits;
     int dsl_cols, dsl_ring, dsl_slotw, dsl_cmax, dsl_dmax;
+    // automatic delivery: only ring rows with rowflag set hold pull spikes
+    // (the others were pushed), and the gather adds to the ring slot, which
+    // pushed spikes may already have reached (null / 0: every row, overwrite)
+    const int* rowflag;
+    int add;
     int* err;
 };
 
@@ -178,9 +199,9 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
             for (int j = 0; j < 4; ++j) {
                 const int d = (int)((dv >> (8 * j)) & 0xffu);
                 const int64_t e = e0 + j;
-                if (e >= beg && e < end && d <= dlim) {
-                    int hs = s1 - d;
-                    if (hs < 0) hs += a.D;
+                int hs = s1 - d;
+                if (hs < 0) hs += a.D;
+                if (e >= beg && e < end && d <= dlim && (!a.rowflag || a.rowflag[hs])) {
                     const uint32_t sid = src[j] & 0x7fffffffu;
                     const uint32_t word = a.bitmap[(size_t)hs * a.words + (sid >> 5)];
                     hit |= ((word >> (sid & 31)) & 1u) << j;
@@ -198,7 +219,15 @@ __global__ void __launch_bounds__(DELIV_THREADS) k_deliver_pull(PullArgs a)
         }
         acc_e = nn_warp_sumf(acc_e);
         acc_i = nn_warp_sumf(acc_i);
-        if (lane == 0) reinterpret_cast<float2*>(out)[k] = make_float2(acc_e, acc_i);
+        if (lane == 0) {
+            float2* o = reinterpret_cast<float2*>(out) + k;
+            if (a.add) {
+                const float2 v = *o;
+                *o = make_float2(v.x + acc_e, v.y + acc_i);
+            } else {
+                *o = make_float2(acc_e, acc_i);
+            }
+        }
     }
 }
 
@@ -309,8 +338,41 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
     const int dlast = min(t1 < (uint64_t)(a.D - 1) ? (int)t1 : a.D - 1, a.dsl_dmax);
     const int32_t* cp = a.dsl_cptr + (size_t)blockIdx.x * (a.dsl_dmax + 1);
     const int cfirst = cp[0];
-    const int C = dlast >= 1 ? cp[dlast] - cfirst : 0;
-    for (int c = tid; c < C; c += blockDim.x) tab[c] = a.dsl_chunk[cfirst + c];
+    // the chunks of the live delays (all delays unless rowflag is given), in
+    // delay order: warp 0 scans their counts (two delays per lane)
+    __shared__ int s_off[DSL_MAX_DELAY + 1];
+    if (warp == 0) {
+        int len[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int d = lane + 1 + 32 * h;
+            len[h] = 0;
+            if (d <= dlast) {
+                int hs = s1 - d;
+                if (hs < 0) hs += a.D;
+                if (!a.rowflag || a.rowflag[hs]) len[h] = cp[d] - cp[d - 1];
+            }
+        }
+        int run = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            int v = len[h];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            s_off[lane + 1 + 32 * h] = run + v;  // live chunks of delays <= lane + 1 + 32 h
+            run += __shfl_sync(0xffffffffu, v, 31);
+        }
+        if (lane == 0) s_off[0] = 0;
+    }
+    __syncthreads();
+    const int C = dlast >= 1 ? s_off[dlast] : 0;
+    for (int d = 1; d <= dlast; ++d) {
+        const int o = s_off[d - 1], len = s_off[d] - o;
+        for (int c = tid; c < len; c += blockDim.x) tab[o + c] = a.dsl_chunk[cp[d - 1] + c];
+    }
     // the block's hit list starts at its first entry: it has room for every entry
     uint2* hits = a.dsl_hits + (C > 0 ? a.dsl_chunk[cfirst].x : 0);
     if (tid == 0) {
@@ -446,9 +508,48 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
     }
     __syncthreads();
     float2* out = reinterpret_cast<float2*>(a.ring + (size_t)(t1 % (uint64_t)a.D) * a.n_pad * 2);
-    for (int k = tid; k < k1 - k0; k += blockDim.x)
-        out[k0 + k] = make_float2((float)((double)(long long)acc_e[k] / DSL_FIX),
-                                  (float)((double)(long long)acc_i[k] / DSL_FIX));
+    for (int k = tid; k < k1 - k0; k += blockDim.x) {
+        const float2 v = make_float2((float)((double)(long long)acc_e[k] / DSL_FIX),
+                                     (float)((double)(long long)acc_i[k] / DSL_FIX));
+        if (a.add) {
+            const float2 o = out[k0 + k];
+            out[k0 + k] = make_float2(o.x + v.x, o.y + v.y);
+        } else {
+            out[k0 + k] = v;
+        }
+    }
+}
+
+// Automatic delivery, return from pull to push at step T (the pull gather
+// after step T - 1 delivered every arrival up to step T): the spikes of the
+// pull rows among steps T - D .. T - 1 scatter their out-edges that arrive at
+// step T + 1 or later, as the push would have.  Grid (word groups, D rows), a
+// warp per bitmap word.
+__global__ void __launch_bounds__(256) k_flush_pull(const uint32_t* bitmap, const int* rowflag, const int64_t* row_ptr,
+                                                    const int32_t* col, const float* weight, const uint8_t* delay,
+                                                    const uint8_t* is_inh, float* ring, int n, int n_pad, int D,
+                                                    int words, long long T)
+{
+    const int r = blockIdx.y;
+    if (!rowflag[r]) return;
+    // the step row r holds: the latest step <= T - 1 congruent to r mod D
+    const long long s = T - 1 - ((T - 1 - r) % D + D) % D;
+    if (s < 0) return;
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (w >= words) return;
+    uint32_t bits = bitmap[(size_t)r * words + w];
+    while (bits) {
+        const int j = 32 * w + __ffs(bits) - 1;
+        bits &= bits - 1;
+        if (j >= n) break;
+        const int64_t beg = row_ptr[j], end = row_ptr[j + 1];
+        const int chn = is_inh[j] ? 1 : 0;
+        for (int64_t e = beg + lane; e < end; e += 32) {
+            const long long arr = s + delay[e];
+            if (arr >= T + 1) atomicAdd(ring + 2 * ((size_t)(arr % D) * n_pad + col[e]) + chn, weight[e]);
+        }
+    }
 }
 
 // Bounds for the fixed-point sums: the longest column and the largest |weight|.
@@ -993,6 +1094,7 @@ extern "C" void nn_sim_config_default(nn_sim_config* c, int n)
     c->par_max_iter = 2000;
     c->par_extrapolate = 0;
     c->par_overlap = 1;
+    c->pull_rate = 0.025f;
 }
 
 extern "C" void nn_net_spec_default(nn_net_spec* sp, int kind)
@@ -1027,12 +1129,15 @@ static StepArgs step_args(nn_sim* s, int q)
     a.gna_scale = s->gna_set ? s->f[NN_F_GNA_SCALE] : nullptr;  // all ones unless set
     a.upar = (s->cfg.hp.g_par != 0.0f && has_field(s)) ? s->f[NN_F_UPAR] : nullptr;
     a.ring = reinterpret_cast<float*>(s->ring);
-    a.bitmap = s->bitmap;
+    const bool autod = s->cfg.delivery == NN_DELIVERY_AUTO;
+    // automatic delivery: push periods write no bitmap
+    a.bitmap = autod && s->cur_mode == 0 ? nullptr : s->bitmap;
+    a.rowflag = autod ? s->rowflag : nullptr;
     a.list = s->list;
     a.counts = s->counts;
     a.base = s->step;
     a.q = q;
-    const bool push = s->cfg.delivery == NN_DELIVERY_PUSH;
+    const bool push = s->cfg.delivery == NN_DELIVERY_PUSH || (autod && s->cur_mode == 0);
     a.row_ptr = push ? s->row_ptr : nullptr;
     a.col = s->col;
     a.weight = s->weight;
@@ -1052,15 +1157,17 @@ static StepArgs step_args(nn_sim* s, int q)
     a.el_members = s->el_members;
     a.err = s->err;
     a.n = s->n; a.n_pad = s->n_pad; a.D = s->D; a.words = s->words;
-    a.zero_ring = push;
+    a.zero_ring = push || autod;
     a.seed = s->cfg.seed;
     a.p = nn_hh_to_dev(s->cfg.hp);
     return a;
 }
 
-static PullArgs pull_args(nn_sim* s, int q)
+static PullArgs pull_args(nn_sim* s, int q, bool hybrid)
 {
     PullArgs a;
+    a.rowflag = hybrid ? s->rowflag : nullptr;
+    a.add = hybrid ? 1 : 0;
     a.col_ptr = s->col_ptr; a.csc_src = s->csc_src; a.csc_w = s->csc_w; a.csc_d = s->csc_d;
     a.bitmap = s->bitmap;
     a.ring = reinterpret_cast<float*>(s->ring);
@@ -1105,7 +1212,9 @@ static nn_status launch_pull(nn_sim* s, const PullArgs& d, cudaStream_t cs)
 static void drop_graph(nn_sim* s)
 {
     if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->graph_pull) cudaGraphExecDestroy(s->graph_pull);
     s->graph = nullptr;
+    s->graph_pull = nullptr;
     s->graph_steps = 0;
 }
 
@@ -1113,7 +1222,8 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
 {
     if (!ctx || !cfg || !out) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: NULL argument");
     if (cfg->n <= 0 || cfg->max_delay < 1 || cfg->max_delay > 254 ||
-        (cfg->delivery != NN_DELIVERY_PUSH && cfg->delivery != NN_DELIVERY_PULL) || cfg->grid < 0 ||
+        (cfg->delivery != NN_DELIVERY_PUSH && cfg->delivery != NN_DELIVERY_PULL &&
+         cfg->delivery != NN_DELIVERY_AUTO) || cfg->grid < 0 ||
         (cfg->grid > 0 && cfg->timescale < 1) || !(cfg->hp.dt > 0.0f) || cfg->raster_capacity < 0)
         return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_create: invalid configuration");
     if (cfg->neurons_per_thread != 0 && cfg->neurons_per_thread != 1 && cfg->neurons_per_thread != 2 &&
@@ -1141,7 +1251,18 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
     nn_status st = NN_OK;
     for (int q = 0; q < NN_F_COUNT && st == NN_OK; ++q) st = nn_alloc(ctx, &s->f[q], NP);
     if (st == NN_OK) st = nn_alloc(ctx, &s->ring, (size_t)s->D * NP);
-    if (st == NN_OK && cfg->delivery == NN_DELIVERY_PULL) st = nn_alloc(ctx, &s->bitmap, (size_t)s->D * s->words);
+    const bool autod = cfg->delivery == NN_DELIVERY_AUTO;
+    if (st == NN_OK && (cfg->delivery == NN_DELIVERY_PULL || autod))
+        st = nn_alloc(ctx, &s->bitmap, (size_t)s->D * s->words);
+    if (st == NN_OK && autod) {
+        if (!(cfg->pull_rate >= 0.0f)) s->cfg.pull_rate = 0.025f;
+        st = nn_alloc(ctx, &s->rowflag, (size_t)s->D);
+        if (st == NN_OK)
+            st = nn_cuda_check(ctx, cudaHostAlloc(&s->h_tot, sizeof(unsigned long long) * nn_sim::TOT_Q, 0),
+                               "cudaHostAlloc");
+        for (int k = 0; k < nn_sim::TOT_Q && st == NN_OK; ++k)
+            st = nn_cuda_check(ctx, cudaEventCreateWithFlags(&s->ev_tot[k], cudaEventDisableTiming), "event");
+    }
     if (st == NN_OK) st = nn_alloc(ctx, &s->list, 2 * NP);
     if (st == NN_OK) st = nn_alloc(ctx, &s->counts, 2);
     if (st == NN_OK) st = nn_alloc(ctx, &s->step, 1);
@@ -1173,6 +1294,7 @@ extern "C" nn_status nn_sim_create(nn_ctx* ctx, const nn_sim_config* cfg, nn_sim
     ctx->launches++;
     cudaMemsetAsync(s->ring, 0, (size_t)s->D * NP * sizeof(float2), cs);
     if (s->bitmap) cudaMemsetAsync(s->bitmap, 0, (size_t)s->D * s->words * sizeof(uint32_t), cs);
+    if (s->rowflag) cudaMemsetAsync(s->rowflag, 0, (size_t)s->D * sizeof(int), cs);
     cudaMemsetAsync(s->list, 0, 2 * NP * sizeof(int), cs);
     cudaMemsetAsync(s->counts, 0, 2 * sizeof(int), cs);
     cudaMemsetAsync(s->step, 0, sizeof(unsigned long long), cs);
@@ -1210,6 +1332,10 @@ extern "C" nn_status nn_sim_destroy(nn_sim* s)
     drop_graph(s);
     for (int q = 0; q < NN_F_COUNT; ++q) nn_release(s->f[q]);
     nn_release(s->ring); nn_release(s->bitmap); nn_release(s->list); nn_release(s->counts); nn_release(s->step);
+    nn_release(s->rowflag);
+    if (s->h_tot) cudaFreeHost(s->h_tot);
+    for (auto e : s->ev_tot)
+        if (e) cudaEventDestroy(e);
     nn_release(s->el_group); nn_release(s->el_val); nn_release(s->el_spk);
     nn_release(s->total); nn_release(s->rcount); nn_release(s->raster); nn_release(s->err);
     nn_release(s->is_inh); nn_release(s->vox); nn_release(s->src); nn_release(s->u); nn_release(s->u_prev); nn_release(s->b);
@@ -1431,7 +1557,7 @@ static nn_status after_network(nn_sim* s)
     drop_graph(s);
     nn_release(s->col_ptr); nn_release(s->csc_src); nn_release(s->csc_w); nn_release(s->csc_d);
     nn_release(s->dsl_chunk); nn_release(s->dsl_cptr); nn_release(s->dsl_ent); nn_release(s->dsl_w); nn_release(s->dsl_hits);
-    if (s->cfg.delivery == NN_DELIVERY_PULL) NN_TRY(build_csc(s));
+    if (s->cfg.delivery == NN_DELIVERY_PULL || s->cfg.delivery == NN_DELIVERY_AUTO) NN_TRY(build_csc(s));
     return NN_OK;
 }
 
@@ -1890,7 +2016,9 @@ static nn_status enqueue_step(nn_sim* s, int qk, int qe)
     NN_CHECK_LAUNCH(ctx, "k_hh_step");
     if (tm) NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_b[qe], cs, cudaEventRecordExternal));
     if (s->cfg.delivery == NN_DELIVERY_PULL) {
-        NN_TRY(launch_pull(s, pull_args(s, qk), cs));
+        NN_TRY(launch_pull(s, pull_args(s, qk, false), cs));
+    } else if (s->cfg.delivery == NN_DELIVERY_AUTO && s->cur_mode == 1) {
+        NN_TRY(launch_pull(s, pull_args(s, qk, true), cs));
     }
     if (tm) {
         NN_CUDA(ctx, cudaEventRecordWithFlags(s->ev_c[qe], cs, cudaEventRecordExternal));
@@ -1899,7 +2027,10 @@ static nn_status enqueue_step(nn_sim* s, int qk, int qe)
     return NN_OK;
 }
 
-static int launches_per_step(const nn_sim* s) { return s->cfg.delivery == NN_DELIVERY_PULL ? 2 : 1; }
+static int launches_per_step(const nn_sim* s)
+{
+    return s->cfg.delivery == NN_DELIVERY_PULL || (s->cfg.delivery == NN_DELIVERY_AUTO && s->cur_mode == 1) ? 2 : 1;
+}
 
 static nn_status enqueue_advance(nn_sim* s, int steps)
 {
@@ -2061,7 +2192,8 @@ static int period_steps(const nn_sim* s) { return has_field(s) ? s->cfg.timescal
 
 static nn_status ensure_graph(nn_sim* s)
 {
-    if (s->graph) return NN_OK;
+    cudaGraphExec_t* slot = s->cur_mode == 1 ? &s->graph_pull : &s->graph;
+    if (*slot) return NN_OK;
     nn_ctx* ctx = s->ctx;
     cudaStream_t cs = ctx->stream;
     const int P = period_steps(s);
@@ -2078,10 +2210,10 @@ static nn_status ensure_graph(nn_sim* s)
         return st;
     }
     if (e != cudaSuccess) return nn_cuda_check(ctx, e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&s->graph, g, 0);
+    e = cudaGraphInstantiate(slot, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
-        s->graph = nullptr;
+        *slot = nullptr;
         return nn_cuda_check(ctx, e, "cudaGraphInstantiate");
     }
     s->graph_steps = P;
@@ -2115,6 +2247,7 @@ extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, 
     for (int q = 0; q < NN_F_COUNT && st == NN_OK; ++q) st = save(s->f[q], NP * sizeof(float));
     if (st == NN_OK) st = save(s->ring, (size_t)s->D * NP * sizeof(float2));
     if (st == NN_OK) st = save(s->bitmap, s->bitmap ? (size_t)s->D * s->words * sizeof(uint32_t) : 0);
+    if (st == NN_OK) st = save(s->rowflag, s->rowflag ? (size_t)s->D * sizeof(int) : 0);
     if (st == NN_OK) st = save(s->list, 2 * NP * sizeof(int));
     if (st == NN_OK) st = save(s->counts, 2 * sizeof(int));
     if (st == NN_OK) st = save(s->step, sizeof(unsigned long long));
@@ -2174,6 +2307,87 @@ extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, 
     return st;
 }
 
+// Automatic delivery.  After each period the spike total is copied to
+// pinned memory behind an event; the periods whose events have completed
+// give the measured rate (spikes per neuron and step), without waiting for
+// the device unless TOT_Q periods are outstanding.
+static nn_status record_total(nn_sim* s)
+{
+    nn_ctx* ctx = s->ctx;
+    if (s->tot_pending == nn_sim::TOT_Q) {
+        NN_CUDA(ctx, cudaEventSynchronize(s->ev_tot[s->tot_head]));
+    }
+    // fold completed measurements
+    while (s->tot_pending > 0) {
+        const int k = s->tot_head;
+        const cudaError_t q = cudaEventQuery(s->ev_tot[k]);
+        if (q == cudaErrorNotReady) break;
+        NN_CUDA(ctx, q);
+        const unsigned long long tot = s->h_tot[k];
+        if (s->base_step >= 0 && s->tot_step[k] > s->base_step)
+            s->last_rate = (float)((double)(tot - s->base_tot) / ((double)(s->tot_step[k] - s->base_step) * s->n));
+        s->base_tot = tot;
+        s->base_step = s->tot_step[k];
+        s->tot_head = (k + 1) % nn_sim::TOT_Q;
+        --s->tot_pending;
+    }
+    const int k = (s->tot_head + s->tot_pending) % nn_sim::TOT_Q;
+    NN_CUDA(ctx, cudaMemcpyAsync(&s->h_tot[k], s->total, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    NN_CUDA(ctx, cudaEventRecord(s->ev_tot[k], ctx->stream));
+    s->tot_step[k] = s->host_step;
+    ++s->tot_pending;
+    return NN_OK;
+}
+
+// The next period's mode from the latest measured rate.  Leaving pull
+// delivery scatters the pull spikes still in flight (k_flush_pull) and clears
+// the row flags; entering it needs nothing (the pull gather skips the rows of
+// pushed steps).
+static nn_status choose_delivery(nn_sim* s)
+{
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    const int want = s->last_rate >= 0.0f && s->last_rate >= s->cfg.pull_rate ? 1 : 0;
+    if (s->cur_mode == 1 && want == 0) {
+        const dim3 grid((unsigned)((s->words + 7) / 8), (unsigned)s->D);
+        k_flush_pull<<<grid, 256, 0, cs>>>(s->bitmap, s->rowflag, s->row_ptr, s->col, s->weight, s->delay, s->is_inh,
+                                          reinterpret_cast<float*>(s->ring), s->n, s->n_pad, s->D, s->words,
+                                          (long long)s->host_step);
+        NN_CHECK_LAUNCH(ctx, "k_flush_pull");
+        NN_CUDA(ctx, cudaMemsetAsync(s->rowflag, 0, (size_t)s->D * sizeof(int), cs));
+    }
+    s->cur_mode = want;
+    s->mode_log.push_back((int8_t)want);
+    s->rate_log.push_back(s->last_rate);
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_delivery_log(nn_sim* s, int8_t* h_modes, float* h_rates, int cap, int* count, int reset)
+{
+    if (!s || !count || cap < 0) return NN_ERR_INVALID_ARG;
+    const int m = (int)s->mode_log.size();
+    for (int i = 0; i < std::min(cap, m); ++i) {
+        if (h_modes) h_modes[i] = s->mode_log[(size_t)i];
+        if (h_rates) h_rates[i] = s->rate_log[(size_t)i];
+    }
+    *count = m;
+    if (reset) {
+        s->mode_log.clear();
+        s->rate_log.clear();
+    }
+    return NN_OK;
+}
+
+extern "C" nn_status nn_sim_set_pull_rate(nn_sim* s, float pull_rate)
+{
+    if (!s || !(pull_rate >= 0.0f)) return NN_ERR_INVALID_ARG;
+    if (s->cfg.delivery != NN_DELIVERY_AUTO)
+        return nn_fail(s->ctx, NN_ERR_INVALID_ARG, "nn_sim_set_pull_rate: the simulation is not in automatic delivery");
+    s->cfg.pull_rate = pull_rate;
+    return NN_OK;
+}
+
 extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
 {
     if (!s || nsteps < 0) return NN_ERR_INVALID_ARG;
@@ -2181,14 +2395,17 @@ extern "C" nn_status nn_sim_step(nn_sim* s, int nsteps)
     nn_ctx* ctx = s->ctx;
     const int P = period_steps(s);
     int left = nsteps;
+    const bool autod = s->cfg.delivery == NN_DELIVERY_AUTO;
     while (left > 0) {
         const bool aligned = (s->host_step % P) == 0;
         if (aligned && left >= P) {
+            if (autod) NN_TRY(choose_delivery(s));
             NN_TRY(ensure_graph(s));
-            NN_CUDA(ctx, cudaGraphLaunch(s->graph, ctx->stream));
+            NN_CUDA(ctx, cudaGraphLaunch(s->cur_mode == 1 ? s->graph_pull : s->graph, ctx->stream));
             ctx->launches += (int64_t)launches_per_step(s) * P + 1;
             s->host_step += P;
             left -= P;
+            if (autod) NN_TRY(record_total(s));
         } else {
             NN_TRY(enqueue_step(s, 0, (int)(s->host_step % P)));
             NN_TRY(enqueue_advance(s, 1));
@@ -2237,7 +2454,7 @@ extern "C" nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int cou
                                                                        s->words);
         NN_CHECK_LAUNCH(ctx, "k_list_bitmap");
     }
-    return launch_pull(s, pull_args(s, 0), cs);
+    return launch_pull(s, pull_args(s, 0, false), cs);
 }
 
 extern "C" nn_status nn_sim_run_host(nn_sim* s, const float* h_in, int nsteps, float* h_out, int64_t* h_spikes)

@@ -27,8 +27,11 @@ template <int NPT, bool UNI, bool EL>
 __global__ void __launch_bounds__(256, NN_HH_MIN_BLOCKS) k_hh_step(StepArgs a)
 {
     const uint64_t t = *a.base + (uint64_t)a.q;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.counts[(t + 1) & 1] = 0;  // next step's count
     const int slot = (int)(t % (uint64_t)a.D);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.counts[(t + 1) & 1] = 0;  // next step's count
+        if (a.rowflag) a.rowflag[slot] = a.bitmap != nullptr;
+    }
     // electrode sample slot of this step (-1: no sample)
     const int s_el =
         (EL && t % (uint64_t)a.el_every == 0) ? (int)((t / (uint64_t)a.el_every) % (uint64_t)a.el_cap) : -1;

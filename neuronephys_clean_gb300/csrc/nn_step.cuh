@@ -39,6 +39,9 @@ struct StepArgs {
     float* el_val;            // [el_cap][el_members]
     uint8_t* el_spk;          // [el_cap][el_members]
     int el_every, el_cap, el_members;
+    // automatic delivery: rowflag[t % D] = 1 when step t's spikes go to the
+    // bitmap for the pull gather, 0 when they are pushed (null otherwise)
+    int* rowflag;
     int* err;
     int n, n_pad, D, words;
     int zero_ring;

@@ -243,6 +243,46 @@ def test_delays_parity(ctx, orc):
         assert_trajectory(gpu_state(s), o.state()[:4], prev, 0.01, exclude=perturbed(s, shifted))
 
 
+def test_automatic_delivery_switches_and_matches_oracle(ctx, orc):
+    """Automatic delivery with its threshold moved so that the periods alternate
+    between push and pull.  Each change of mode carries the spikes in flight:
+    the pull gather skips the ring rows of pushed steps, and leaving pull
+    scatters the pulled spikes that have yet to arrive.  Raster and state
+    against the oracle; raster and delay ring against a push-only run of the
+    same network (same spikes, the ring's sums in another order: 1e-5)."""
+    n, seed, periods = 2744, 31, 14
+    sims = {}
+    for delivery in (nn.NN_DELIVERY_PUSH, nn.NN_DELIVERY_AUTO):
+        c = nn.default_config(n)
+        c.seed, c.max_delay, c.raster_capacity, c.delivery = seed, 20, 100000, delivery
+        s = nn.Simulation(ctx, c)
+        spec = nn.default_net_spec(nn.NN_NET_GAUSS)
+        spec.k, spec.dmax, spec.w_mu = 30, 20, 0.0
+        s.generate_network(spec)
+        s.init_state(-65.0, 6.0, 12.0)
+        if delivery == nn.NN_DELIVERY_AUTO:
+            o = oracle_for(orc, s, seed)
+            ref, prev = run_oracle(o, 50 * periods)
+            for k in range(periods):  # periods of 50 steps (no field)
+                s.set_pull_rate(0.0 if k % 2 == 0 else 2.0)
+                s.step(50)
+                s.counters()  # the period's spike total is read back before the next choice
+            modes, rates = s.delivery_log()
+        else:
+            s.step(50 * periods)
+        sims[delivery] = s
+    auto, push = sims[nn.NN_DELIVERY_AUTO], sims[nn.NN_DELIVERY_PUSH]
+    # no rate measured for the first three periods (push); then the threshold decides
+    assert modes.tolist() == [0, 0, 0] + [1 - k % 2 for k in range(3, periods)], modes
+    assert (rates[:3] < 0).all() and (rates[3:] >= 0).all()
+    got = raster_set(*auto.raster())
+    assert len(ref) > 50
+    shifted = assert_rasters_match(got, o.margins)
+    assert_trajectory(gpu_state(auto), o.state()[:4], prev, 0.01, exclude=perturbed(auto, shifted))
+    assert got == raster_set(*push.raster())
+    np.testing.assert_allclose(auto.get_ring(), push.get_ring(), rtol=1e-5, atol=1e-5)
+
+
 def test_paracrine_field(ctx, orc):
     """Deposits of 100 steps, then one 7-point backward-Euler PCG solve.  The
     membrane potentials start spread over [-65, -35] mV so spikes (and hence
