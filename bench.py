@@ -235,6 +235,8 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
                     delivery=DELIVERY_MODES[args.delivery])
     P = wl["total_steps"]  # timesteps per bench step: one full run of the workload
     n = wl["n"]
+    # the field solver's tile depth from the autotuner (scratch vectors)
+    cg_tile = sim.autotune_solver(10) if wl["grid"] else (0, 0.0)
     el_info = None
     if args.electrodes > 0:
         el_info = set_knn_electrodes(sim, args.electrodes, 50, args.electrode_every)
@@ -354,6 +356,7 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "data": "synthetic (seeded counter-based generators)",
         "config": workload_config(wl, nnz, args.delivery),
         "delivery": delivery_info,
+        "autotuned": {"cg_tile": f"32 x 16 x {cg_tile[0]}", "cg_trial_ms_per_iteration": cg_tile[1]},
         "electrodes": el_info,
         "synaptic_events_per_s": events / seconds if seconds else None,
         "spikes_in_timed_region": spikes,
@@ -646,6 +649,7 @@ def run_batch(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     sim.set_field("IDRIVE", np.repeat(drive, sizes))
     sim.step(args.settle)
     tpb, npt, tune_ms = sim.autotune(20)
+    cpb, pcg_iter_ms = sim.autotune_solver(10)
     P = wl["total_steps"]
     for _ in range(args.warmup):
         sim.step(P)
@@ -696,11 +700,18 @@ def run_batch(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
         "config": {"workload": wl["workload"], "instances": int(wl["n_inst"]), "neurons": n, "synapses": int(nnz),
                    "timesteps_per_step": P, "grid_cells": int(sim.field_cells()),
                    "weights": "U[0, w_b], w_b = 2 * 2.5 nS / (p_b * size_b) per instance",
-                   "autotuned": {"threads_per_block": tpb, "neurons_per_thread": npt, "trial_ms_per_step": tune_ms},
+                   "autotuned": {"threads_per_block": tpb, "neurons_per_thread": npt, "trial_ms_per_step": tune_ms,
+                                 "pcg_cells_per_block": cpb, "pcg_trial_ms_per_iteration": pcg_iter_ms},
                    "network_generation_s": t_gen, "l2": "inputs larger than L2"},
         "spikes_in_timed_region": spikes_b - spikes_a,
         "cg": {"instances": int(wl["n_inst"]), "iterations_last_solve_max": int(iters.max()),
                "iterations_last_solve_median": float(np.median(iters)), "solve_ms": kt.solve_ms},
+        # one neuron-update launch per timestep for all instances, replayed from
+        # a graph: the timestep's wall time against the launch's own duration
+        # (events around each launch) shows what launching costs
+        "timestep": {"wall_us": tmax * 1e6 / (args.steps * P), "k_hh_step_mean_us": kt.hh_step_ms * 1e3,
+                     "k_hh_step_median_us": hh_ms * 1e3,
+                     "solve_us_per_timestep": kt.solve_ms * 1e3 / wl["timescale"]},
         "roofline": {"bound": "hbm", "kernel": "k_hh_step", "achieved": hh_ach, "peak": hbm_peak, "unit": "GB/s",
                      "frac": hh_ach / hbm_peak if hh_ach else None,
                      "traffic": NCU_TRAFFIC_PER_UNIT["hh_step"] * n, "algorithmic_bytes": n * HH_BYTES_PER_NEURON_STEP,

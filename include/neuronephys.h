@@ -301,6 +301,13 @@ NN_API nn_status nn_sim_set_instances(nn_sim* s, int n_inst, const int* h_offset
  * neurons per thread 1/2/4) candidate on the simulation's own network and
  * state, keeps the fastest and restores the state the trials touched. */
 NN_API nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, int* best_npt, float* best_ms);
+/* Autotuner of the field solver's block shape, on scratch vectors (the
+ * simulation's state is not touched): for a single grid the z-depth of the
+ * 32 x 16 tiles of the one-kernel PCG iteration (4 .. 32; NN_ERR_UNSUPPORTED
+ * when the grid runs the two-kernel PCG), for a batch the batched PCG's cells
+ * per block.  *shape: the chosen depth or cells per block; *ms_per_iter: its
+ * iteration time. */
+NN_API nn_status nn_sim_autotune_solver(nn_sim* s, int trial_iters, int* shape, float* ms_per_iter);
 /* Per-instance solver iteration counts of the last paracrine solve (n_inst entries). */
 NN_API nn_status nn_sim_instance_iterations(nn_sim* s, int* h_iters);
 NN_API nn_status nn_sim_network_size(nn_sim* s, int64_t* nnz);
@@ -445,6 +452,14 @@ NN_API nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides, dou
 NN_API nn_status nn_bpcg_destroy(nn_bpcg* bp);
 NN_API nn_status nn_bpcg_solve(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter, int* h_iters,
                                int* max_iters, int* unconverged);
+/* Block-size autotuner: times iterations with 512, 1,024, 2,048 and 4,096
+ * cells per block (2, 4, 8, 16 per thread) on the batch's own operators,
+ * right-hand side d_b and d_x as scratch (overwritten), and keeps the fastest
+ * layout for later solves. */
+NN_API nn_status nn_bpcg_autotune(nn_bpcg* bp, const float* d_b, float* d_x, int trial_iters, int* cells_per_block,
+                                  float* ms_per_iter);
+/* Fix the block layout instead: 512, 1024, 2048 (the default) or 4096 cells per block. */
+NN_API nn_status nn_bpcg_set_cells_per_block(nn_bpcg* bp, int cells_per_block);
 
 /* No counterpart in the reference.  The same solve as nn_pcg_create +
  * nn_pcg_solve + nn_pcg_destroy for callers that may not allocate device

@@ -514,6 +514,15 @@ class Simulation:
                "sim_autotune")
         return tpb.value, npt.value, ms.value
 
+    def autotune_solver(self, trial_iters: int = 20) -> tuple[int, float]:
+        """Field solver block shape (single grid: tile depth of the one-kernel
+        PCG iteration; batch: cells per block), timed on scratch vectors.
+        Returns (shape, ms per iteration)."""
+        shape, ms = C.c_int(0), C.c_float(0.0)
+        _check(lib().nn_sim_autotune_solver(self.handle, trial_iters, C.byref(shape), C.byref(ms)), self.ctx,
+               "sim_autotune_solver")
+        return shape.value, ms.value
+
     def instance_iterations(self) -> np.ndarray:
         out = np.empty(self.n_inst, np.int32)
         _check(lib().nn_sim_instance_iterations(self.handle, _ptr(out)), self.ctx, "sim_instance_iterations")
@@ -650,6 +659,17 @@ class BatchedPCG:
         _check(lib().nn_bpcg_solve(self.handle, b.ptr, x.ptr, rtol, max_iter, _ptr(its), C.byref(mx), C.byref(bad)),
                self.ctx, "bpcg_solve")
         return its, bad.value
+
+    def autotune(self, b: DeviceArray, x: DeviceArray, trial_iters: int = 20) -> tuple[int, float]:
+        """Time 512 .. 4,096 cells per block on right-hand side b (x: scratch,
+        overwritten); keeps the fastest.  Returns (cells per block, ms per iteration)."""
+        cpb, ms = C.c_int(0), C.c_float(0.0)
+        _check(lib().nn_bpcg_autotune(self.handle, b.ptr, x.ptr, trial_iters, C.byref(cpb), C.byref(ms)), self.ctx,
+               "bpcg_autotune")
+        return cpb.value, ms.value
+
+    def set_cells_per_block(self, cells: int) -> None:
+        _check(lib().nn_bpcg_set_cells_per_block(self.handle, cells), self.ctx, "bpcg_set_cells_per_block")
 
     def close(self):
         if self.handle:

@@ -143,6 +143,9 @@ _SIGS = {
     "nn_sim_pull_info": (c_int, [c_void_p, P(c_int), P(c_int)]),
     "nn_sim_delivery_log": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_int), c_int]),
     "nn_sim_set_pull_rate": (c_int, [c_void_p, c_float]),
+    "nn_sim_autotune_solver": (c_int, [c_void_p, c_int, P(c_int), P(c_float)]),
+    "nn_bpcg_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_int), P(c_float)]),
+    "nn_bpcg_set_cells_per_block": (c_int, [c_void_p, c_int]),
     "nn_sim_set_instances": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "nn_sim_field_cells": (c_int, [c_void_p, P(c_int64)]),
     "nn_sim_get_vox": (c_int, [c_void_p, c_void_p]),

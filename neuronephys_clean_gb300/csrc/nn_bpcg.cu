@@ -3,8 +3,9 @@
 // alpha_b = dt D g_b^2) solved together, each to its own relative residual.
 //
 // The instances' cells are concatenated (instance b at cell offset off_b,
-// x fastest).  A thread block covers CPB = 2,048 consecutive cells of one
-// instance (8 per thread, strided by the block size),
+// x fastest).  A thread block covers CPB = 256 VPT consecutive cells of one
+// instance (VPT per thread, strided by the block size; VPT = 8 unless the
+// autotuner, nn_bpcg_autotune, chose 2, 4 or 16),
 // so every reduction is per instance: a block writes its FP64 partials, and
 // the last block of an instance to arrive (a per-instance ticket) sums them in
 // fixed order and forms that instance's scalars.  Per iteration two kernels
@@ -24,8 +25,7 @@
 
 namespace {
 constexpr int BT = 256;
-constexpr int VPT = 8;            // cells per thread
-constexpr int CPB = BT * VPT;     // cells per block
+constexpr int VPT_MIN = 2;        // cells per thread: 2, 4, 8 or 16
 
 struct Batch {
     int n_inst;
@@ -143,13 +143,14 @@ __device__ bool instance_reduce(const Batch& B, int blk, int b, int nsum, const 
 }
 
 // r = b - A x, p = z = M r; partials (r, z), (b, b), (r, r)
+template <int VPT>
 __global__ void __launch_bounds__(BT) k_bpcg_init(Batch B, const float* rhs, const float* x, float* r, float* p)
 {
     const int blk = block_id(B);
     const int b = B.blk_inst[blk];
     const int g = B.side[b];
     const int64_t base = B.off[b], cells = B.off[b + 1] - base;
-    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * CPB + threadIdx.x;
+    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * (BT * VPT) + threadIdx.x;
     float rz = 0.0f, bb = 0.0f, rr = 0.0f;
 #pragma unroll
     for (int v = 0; v < VPT; ++v) {
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(BT) k_bpcg_init(Batch B, const float* rhs, con
 
 // p = z + beta p_old (z = M r; the first iteration has beta = 0 and p_old = z),
 // Ap = A p; partial (p, Ap) -> alpha = rz / pAp
+template <int VPT>
 __global__ void __launch_bounds__(BT) k_bpcg_dir_apply(Batch B, const float* r, const float* p_old, float* p_new,
                                                        float* Ap)
 {
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(BT) k_bpcg_dir_apply(Batch B, const float* r, 
     if (B.flags[b]) return;
     const int g = B.side[b];
     const int64_t base = B.off[b], cells = B.off[b + 1] - base;
-    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * CPB + threadIdx.x;
+    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * (BT * VPT) + threadIdx.x;
     const double* s = B.scal + (size_t)b * S_COUNT;
     const float beta = (float)s[S_BETA], md = B.invd[b];
     float pap = 0.0f;
@@ -218,6 +220,7 @@ __global__ void __launch_bounds__(BT) k_bpcg_dir_apply(Batch B, const float* r, 
 }
 
 // x += alpha p, r -= alpha Ap; partials (r, z), (r, r) -> beta, convergence
+template <int VPT>
 __global__ void __launch_bounds__(BT) k_bpcg_update(Batch B, float* x, float* r, const float* p, const float* Ap,
                                                     int max_iter)
 {
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(BT) k_bpcg_update(Batch B, float* x, float* r,
     const int b = B.blk_inst[blk];
     if (B.flags[b]) return;
     const int64_t base = B.off[b], cells = B.off[b + 1] - base;
-    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * CPB + threadIdx.x;
+    const int64_t c0 = (int64_t)(blk - B.blk_first[b]) * (BT * VPT) + threadIdx.x;
     const double* s = B.scal + (size_t)b * S_COUNT;
     const float alpha = (float)s[S_ALPHA];
     float rz = 0.0f, rr = 0.0f;
@@ -266,6 +269,8 @@ struct nn_bpcg {
     int n_inst = 0;
     int64_t G = 0;
     int nblocks = 0;
+    int vpt = 8;                   // cells per thread of the current block layout
+    int max_blocks = 0;            // blocks at VPT_MIN (the layout arrays' size)
     std::vector<int> h_side;
     std::vector<int64_t> h_off;
     int *side = nullptr, *blk_inst = nullptr, *blk_first = nullptr, *flags = nullptr, *iters = nullptr,
@@ -311,6 +316,27 @@ extern "C" nn_status nn_bpcg_destroy(nn_bpcg* bp)
     return NN_OK;
 }
 
+// Block layout for vpt cells per thread: blocks of each instance, block ->
+// instance table, first block of each instance.
+static nn_status set_layout(nn_bpcg* bp, int vpt)
+{
+    nn_ctx* ctx = bp->ctx;
+    const int64_t cpb = (int64_t)BT * vpt;
+    std::vector<int> first((size_t)bp->n_inst + 1, 0), binst;
+    for (int b = 0; b < bp->n_inst; ++b) {
+        const int64_t cells = bp->h_off[(size_t)b + 1] - bp->h_off[(size_t)b];
+        const int nb = (int)((cells + cpb - 1) / cpb);
+        first[(size_t)b + 1] = first[(size_t)b] + nb;
+        for (int q = 0; q < nb; ++q) binst.push_back(b);
+    }
+    NN_CUDA(ctx, nn_copy_sync(ctx, bp->blk_inst, binst.data(), sizeof(int) * binst.size(), cudaMemcpyHostToDevice));
+    NN_CUDA(ctx, nn_copy_sync(ctx, bp->blk_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
+    bp->vpt = vpt;
+    bp->nblocks = first.back();
+    bp->h_first = first;
+    return NN_OK;
+}
+
 // sides[b] >= 1; alpha_b = alpha_unit * side_b^2 (alpha_unit = dt D on the unit cube)
 extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides, double alpha_unit, double beta,
                                     nn_bpcg** out)
@@ -325,7 +351,6 @@ extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides,
     bp->h_side.assign(h_sides, h_sides + n_inst);
     bp->h_off.assign((size_t)n_inst + 1, 0);
     std::vector<float> al(n_inst), iv(n_inst);
-    std::vector<int> first((size_t)n_inst + 1, 0), binst;
     for (int b = 0; b < n_inst; ++b) {
         const int g = h_sides[b];
         if (g < 1 || g > 255) {
@@ -336,13 +361,9 @@ extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides,
         bp->h_off[(size_t)b + 1] = bp->h_off[(size_t)b] + cells;
         al[b] = (float)(alpha_unit * g * g);
         iv[b] = (float)(1.0 / (1.0 + beta + 6.0 * alpha_unit * g * g));
-        const int nb = (int)((cells + CPB - 1) / CPB);
-        first[(size_t)b + 1] = first[(size_t)b] + nb;
-        for (int q = 0; q < nb; ++q) binst.push_back(b);
+        bp->max_blocks += (int)((cells + BT * VPT_MIN - 1) / (BT * VPT_MIN));
     }
     bp->G = bp->h_off.back();
-    bp->nblocks = first.back();
-    bp->h_first = first;
     bp->onepb = (float)(1.0 + beta);
     nn_status st = NN_OK;
     const size_t G = (size_t)bp->G;
@@ -350,14 +371,14 @@ extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides,
     if (st == NN_OK) st = nn_alloc(ctx, &bp->off, (size_t)n_inst + 1);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->alpha, (size_t)n_inst);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->invd, (size_t)n_inst);
-    if (st == NN_OK) st = nn_alloc(ctx, &bp->blk_inst, (size_t)bp->nblocks);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->blk_inst, (size_t)bp->max_blocks);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->blk_first, (size_t)n_inst + 1);
-    if (st == NN_OK) st = nn_alloc(ctx, &bp->work, (size_t)bp->nblocks);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->work, (size_t)bp->max_blocks);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->flags, (size_t)n_inst);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->iters, (size_t)n_inst);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->running, 1);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->scal, (size_t)n_inst * S_COUNT);
-    if (st == NN_OK) st = nn_alloc(ctx, &bp->partials, (size_t)3 * bp->nblocks);
+    if (st == NN_OK) st = nn_alloc(ctx, &bp->partials, (size_t)3 * bp->max_blocks);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->ticket, (size_t)n_inst);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->r, G);
     if (st == NN_OK) st = nn_alloc(ctx, &bp->p0, G);
@@ -368,10 +389,7 @@ extern "C" nn_status nn_bpcg_create(nn_ctx* ctx, int n_inst, const int* h_sides,
         st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->off, bp->h_off.data(), sizeof(int64_t) * (n_inst + 1), cudaMemcpyHostToDevice), "copy");
     if (st == NN_OK) st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->alpha, al.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
     if (st == NN_OK) st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->invd, iv.data(), sizeof(float) * n_inst, cudaMemcpyHostToDevice), "copy");
-    if (st == NN_OK)
-        st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->blk_inst, binst.data(), sizeof(int) * binst.size(), cudaMemcpyHostToDevice), "copy");
-    if (st == NN_OK)
-        st = nn_cuda_check(ctx, nn_copy_sync(ctx, bp->blk_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice), "copy");
+    if (st == NN_OK) st = set_layout(bp, 8);
     if (st == NN_OK) st = nn_cuda_check(ctx, nn_zero_async(ctx, bp->ticket, sizeof(unsigned int) * n_inst), "memset");
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&bp->ev0), "event");
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&bp->ev1), "event");
@@ -424,7 +442,12 @@ nn_status enqueue_init(nn_bpcg* bp, const Batch& B, const float* d_b, const floa
     NN_CUDA(ctx, cudaMemsetAsync(bp->running, 0, sizeof(int), cs));
     NN_CUDA(ctx, cudaMemsetAsync(bp->ticket, 0, sizeof(unsigned int) * bp->n_inst, cs));
     if (bp->timing) NN_CUDA(ctx, cudaEventRecord(bp->ev0, cs));
-    k_bpcg_init<<<bp->nblocks, BT, 0, cs>>>(B, d_b, d_x, bp->r, bp->p0);
+    switch (bp->vpt) {
+        case 2: k_bpcg_init<2><<<bp->nblocks, BT, 0, cs>>>(B, d_b, d_x, bp->r, bp->p0); break;
+        case 4: k_bpcg_init<4><<<bp->nblocks, BT, 0, cs>>>(B, d_b, d_x, bp->r, bp->p0); break;
+        case 16: k_bpcg_init<16><<<bp->nblocks, BT, 0, cs>>>(B, d_b, d_x, bp->r, bp->p0); break;
+        default: k_bpcg_init<8><<<bp->nblocks, BT, 0, cs>>>(B, d_b, d_x, bp->r, bp->p0); break;
+    }
     NN_CHECK_LAUNCH(ctx, "k_bpcg_init");
     return NN_OK;
 }
@@ -438,9 +461,19 @@ nn_status enqueue_iters(nn_bpcg* bp, const Batch& B, float* d_x, int it, int n, 
         // p0 holds z = M r at the start (beta = 0), then the directions alternate
         const float* p_old = (it & 1) ? bp->p1 : bp->p0;
         float* p_new = (it & 1) ? bp->p0 : bp->p1;
-        k_bpcg_dir_apply<<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap);
+        switch (bp->vpt) {
+            case 2: k_bpcg_dir_apply<2><<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap); break;
+            case 4: k_bpcg_dir_apply<4><<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap); break;
+            case 16: k_bpcg_dir_apply<16><<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap); break;
+            default: k_bpcg_dir_apply<8><<<grid, BT, 0, cs>>>(B, bp->r, p_old, p_new, bp->Ap); break;
+        }
         NN_CHECK_LAUNCH(ctx, "k_bpcg_dir_apply");
-        k_bpcg_update<<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter);
+        switch (bp->vpt) {
+            case 2: k_bpcg_update<2><<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter); break;
+            case 4: k_bpcg_update<4><<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter); break;
+            case 16: k_bpcg_update<16><<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter); break;
+            default: k_bpcg_update<8><<<grid, BT, 0, cs>>>(B, d_x, bp->r, p_new, bp->Ap, max_iter); break;
+        }
         NN_CHECK_LAUNCH(ctx, "k_bpcg_update");
     }
     return NN_OK;
@@ -554,4 +587,70 @@ nn_status nn_bpcg_async_finish(nn_bpcg* bp, int* h_iters, int* max_iters, int* u
     int it = bp->as_it;
     NN_TRY(iterate(bp, batch_args(bp, bp->as_rtol), bp->as_x, &it, bp->as_max_iter, bp->as_cs));
     return collect(bp, bp->as_cs, h_iters, max_iters, unconverged);
+}
+
+// Block-size autotuner: time `iters` iterations over all blocks (after two
+// untimed ones) for 2, 4, 8 and 16 cells per thread on the batch's own
+// operators -- right-hand side d_b, d_x as scratch (overwritten), a residual
+// target no instance reaches -- and keep the fastest layout.
+extern "C" nn_status nn_bpcg_autotune(nn_bpcg* bp, const float* d_b, float* d_x, int iters, int* cells_per_block,
+                                      float* ms_per_iter)
+{
+    if (!bp || !d_b || !d_x || iters < 1) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = bp->ctx;
+    if (bp->as_active) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_bpcg_autotune: a solve is pending");
+    cudaStream_t cs = ctx->stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    NN_CUDA(ctx, cudaEventCreate(&e0));
+    NN_CUDA(ctx, cudaEventCreate(&e1));
+    const int vpt0 = bp->vpt;
+    const bool timing0 = bp->timing;
+    bp->timing = false;
+    int best_vpt = vpt0;
+    float best = 1e30f;
+    nn_status st = NN_OK;
+    const int max_iter = 1 << 30;
+    for (int vpt : {2, 4, 8, 16}) {
+        if (st != NN_OK) break;
+        st = set_layout(bp, vpt);
+        const Batch B = batch_args(bp, 1e-30);
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaMemsetAsync(d_x, 0, sizeof(float) * (size_t)bp->G, cs), "memset");
+        if (st == NN_OK) st = enqueue_init(bp, B, d_b, d_x, cs);
+        if (st == NN_OK) st = enqueue_iters(bp, B, d_x, 0, 2, bp->nblocks, max_iter, cs);
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e0, cs), "event");
+        if (st == NN_OK) st = enqueue_iters(bp, B, d_x, 2, iters, bp->nblocks, max_iter, cs);
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e1, cs), "event");
+        int running = 0;
+        if (st == NN_OK)
+            st = nn_cuda_check(ctx, cudaMemcpyAsync(&running, bp->running, sizeof(int), cudaMemcpyDeviceToHost, cs),
+                               "copy");
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(cs), "nn_bpcg_autotune");
+        float ms = 0.0f;
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventElapsedTime(&ms, e0, e1), "event");
+        // a layout under which instances stopped early did less work: no timing
+        if (st == NN_OK && running == bp->n_inst && ms / iters < best) {
+            best = ms / iters;
+            best_vpt = vpt;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    bp->timing = timing0;
+    const nn_status st2 = set_layout(bp, st == NN_OK ? best_vpt : vpt0);
+    if (st == NN_OK) st = st2;
+    if (cells_per_block) *cells_per_block = BT * bp->vpt;
+    if (ms_per_iter) *ms_per_iter = best < 1e30f ? best : 0.0f;
+    return st;
+}
+
+int nn_bpcg_cells_per_block(const nn_bpcg* bp) { return BT * bp->vpt; }
+
+extern "C" nn_status nn_bpcg_set_cells_per_block(nn_bpcg* bp, int cells_per_block)
+{
+    if (!bp) return NN_ERR_INVALID_ARG;
+    const int vpt = cells_per_block / BT;
+    if (cells_per_block != BT * vpt || (vpt != 2 && vpt != 4 && vpt != 8 && vpt != 16))
+        return nn_fail(bp->ctx, NN_ERR_INVALID_ARG, "nn_bpcg_set_cells_per_block: 512, 1024, 2048 or 4096");
+    if (bp->as_active) return nn_fail(bp->ctx, NN_ERR_INVALID_ARG, "nn_bpcg_set_cells_per_block: a solve is pending");
+    return set_layout(bp, vpt);
 }

@@ -827,3 +827,63 @@ nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, i
     if (converged) *converged = h_flags[0] == 1;
     return NN_OK;
 }
+
+// Tile-depth autotuner: time `iters` iterations (after two untimed ones) of
+// every candidate depth on this plan's own operator -- right-hand side d_b,
+// d_x as scratch (overwritten) -- and keep the fastest.  The residual target
+// is never reached, so every timed iteration does its full work.
+nn_status nn_cg_plan_autotune(nn_cg_plan* pl, const float* d_b, float* d_x, int iters, int* zc_out, float* ms_out)
+{
+    nn_ctx* ctx = pl->ctx;
+    cudaStream_t cs = ctx->stream;
+    if (iters < 1) return NN_ERR_INVALID_ARG;
+    CUtensorMap map_x;
+    if (((uintptr_t)d_x & 15) || !make_map(&map_x, d_x, pl->nx, pl->ny, pl->nz, false))
+        return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_cg_plan_autotune: x must be a 16-byte aligned device vector");
+    const int64_t cols = (int64_t)((pl->nx + TX - 1) / TX) * ((pl->ny + TY - 1) / TY);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    NN_CUDA(ctx, cudaEventCreate(&e0));
+    NN_CUDA(ctx, cudaEventCreate(&e1));
+    const int zc0 = pl->zc, tiles0 = pl->tiles;
+    int best_zc = zc0, best_tiles = tiles0;
+    float best = 1e30f;
+    nn_status st = NN_OK;
+    const double rtol = 1e-30;
+    const int max_iter = 1 << 30;
+    int prev_zc = 0;
+    for (int zc : {4, 6, 8, 12, 16, 24, 32}) {
+        if (st != NN_OK || prev_zc >= pl->nz) break;  // deeper tiles than the grid change nothing
+        prev_zc = zc;
+        pl->zc = zc;
+        pl->tiles = (int)(cols * ((pl->nz + zc - 1) / zc));
+        st = nn_cuda_check(ctx, cudaMemsetAsync(d_x, 0, sizeof(float) * (size_t)pl->G, cs), "memset");
+        if (st == NN_OK) st = enqueue_init(pl, d_b, d_x, rtol, max_iter, cs);
+        if (st == NN_OK) st = enqueue_iters(pl, d_x, map_x, rtol, max_iter, 0, 2, cs);
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e0, cs), "event");
+        if (st == NN_OK) st = enqueue_iters(pl, d_x, map_x, rtol, max_iter, 2, iters, cs);
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e1, cs), "event");
+        int h_flags[4] = {0, 0, 0, 0};
+        if (st == NN_OK)
+            st = nn_cuda_check(ctx, cudaMemcpyAsync(h_flags, pl->flags, sizeof h_flags, cudaMemcpyDeviceToHost, cs),
+                               "copy");
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(cs), "nn_cg_plan_autotune");
+        if (st == NN_OK && h_flags[2]) st = nn_fail(ctx, NN_ERR_TIMEOUT, "k_cg_iter: a TMA pipeline wait timed out");
+        float ms = 0.0f;
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventElapsedTime(&ms, e0, e1), "event");
+        // iterations that stopped early (exact solution, non-finite) are no timing
+        if (st == NN_OK && h_flags[0] == 0 && ms / iters < best) {
+            best = ms / iters;
+            best_zc = zc;
+            best_tiles = pl->tiles;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    pl->zc = st == NN_OK ? best_zc : zc0;
+    pl->tiles = st == NN_OK ? best_tiles : tiles0;
+    if (zc_out) *zc_out = pl->zc;
+    if (ms_out) *ms_out = best < 1e30f ? best : 0.0f;
+    return st;
+}
+
+int nn_cg_plan_tile_depth(const nn_cg_plan* pl) { return pl->zc; }

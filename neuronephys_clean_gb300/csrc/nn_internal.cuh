@@ -206,6 +206,7 @@ void nn_bpcg_last_timing(const nn_bpcg* bp, float* ms, int* iters);
 nn_status nn_bpcg_async_begin(nn_bpcg* bp, const float* d_b, float* d_x, double rtol, int max_iter, int n,
                               cudaStream_t cs);
 nn_status nn_bpcg_async_finish(nn_bpcg* bp, int* h_iters, int* max_iters, int* unconverged);
+int nn_bpcg_cells_per_block(const nn_bpcg* bp);
 
 struct nn_cg_plan;
 nn_status nn_cg_plan_create(nn_ctx* ctx, int nx, int ny, int nz, double alpha, double beta, const float* D,
@@ -223,6 +224,10 @@ nn_status nn_pcg_async_begin(nn_pcg* pc, const float* d_b, float* d_x, double rt
 nn_status nn_pcg_async_finish(nn_pcg* pc, int* iters, double* relres, int* converged);
 bool nn_pcg_async_supported(const nn_pcg* pc);
 void nn_cg_last_timing(const nn_cg_plan* pl, float* ms, int* iters);
+nn_status nn_cg_plan_autotune(nn_cg_plan* pl, const float* d_b, float* d_x, int iters, int* zc_out, float* ms_out);
+int nn_cg_plan_tile_depth(const nn_cg_plan* pl);
+struct nn_pcg;
+nn_status nn_pcg_autotune_tiles(nn_pcg* pc, int iters, int* tile_z, float* ms_per_iter);
 double nn_host_inv_phi(double p);
 void nn_host_gauss_table(double sigma_sites, int16_t* table4096);
 

@@ -537,6 +537,36 @@ nn_status nn_pcg_run_best(nn_pcg* pc, const float* d_b, float* d_x, double rtol,
     return nn_pcg_run(pc, d_b, d_x, rtol, max_iter, iters, relres, converged);
 }
 
+// Right-hand side for tile timing: values in [0.5, 1.5) from a hash of the
+// cell index (no solve reaches its residual target on it within a trial).
+__global__ void k_pcg_trial_rhs(float* b, int64_t G)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < G; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = 0.5f + (float)(((uint32_t)i * 2654435761u) >> 22) * (1.0f / 1024.0f);
+}
+
+// Tile autotuner of the single-kernel iteration (nn_cg_plan_autotune) on
+// scratch vectors; NN_ERR_UNSUPPORTED when the grid runs the two-kernel PCG.
+nn_status nn_pcg_autotune_tiles(nn_pcg* pc, int iters, int* tile_z, float* ms_per_iter)
+{
+    if (!pc || iters < 1) return NN_ERR_INVALID_ARG;
+    if (!pc->fast) return NN_ERR_UNSUPPORTED;
+    nn_ctx* ctx = pc->ctx;
+    const int64_t G = (int64_t)pc->nx * pc->ny * pc->nz;
+    float *b = nullptr, *x = nullptr;
+    NN_TRY(nn_alloc(ctx, &b, (size_t)G));
+    nn_status st = nn_alloc(ctx, &x, (size_t)G);
+    if (st == NN_OK) {
+        k_pcg_trial_rhs<<<nn_grid_for(ctx, G, 256, 8), 256, 0, ctx->stream>>>(b, G);
+        st = nn_cuda_check(ctx, cudaPeekAtLastError(), "k_pcg_trial_rhs");
+    }
+    if (st == NN_OK) st = nn_cg_plan_autotune(pc->fast, b, x, iters, tile_z, ms_per_iter);
+    cudaStreamSynchronize(ctx->stream);
+    nn_release(b);
+    nn_release(x);
+    return st;
+}
+
 // ========================================================= no allocation ==
 // nn_pcg_solve_noalloc: the same Jacobi-PCG as nn_pcg_create + nn_pcg_solve,
 // for callers that may not allocate device memory (a host framework that owns

@@ -2379,6 +2379,30 @@ extern "C" nn_status nn_sim_delivery_log(nn_sim* s, int8_t* h_modes, float* h_ra
     return NN_OK;
 }
 
+extern "C" nn_status nn_sim_autotune_solver(nn_sim* s, int trial_iters, int* shape, float* ms_per_iter)
+{
+    if (!s || trial_iters < 1) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = s->ctx;
+    if (!s->pcg && !s->bpcg) return nn_fail(ctx, NN_ERR_INVALID_ARG, "nn_sim_autotune_solver: no paracrine field");
+    // a pending overlapped solve owns the solver's work vectors
+    NN_TRY(finish_solve(s));
+    if (s->ev_solved) NN_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, s->ev_solved, 0));
+    if (s->pcg) return nn_pcg_autotune_tiles(s->pcg, trial_iters, shape, ms_per_iter);
+    float *b = nullptr, *x = nullptr;
+    const int64_t G = s->G;
+    NN_TRY(nn_alloc(ctx, &b, (size_t)G));
+    nn_status st = nn_alloc(ctx, &x, (size_t)G);
+    if (st == NN_OK) {
+        k_fill_f<<<nn_grid_for(ctx, G, 256), 256, 0, ctx->stream>>>(b, G, 1.0f);
+        st = nn_cuda_check(ctx, cudaPeekAtLastError(), "k_fill_f");
+    }
+    if (st == NN_OK) st = nn_bpcg_autotune(s->bpcg, b, x, trial_iters, shape, ms_per_iter);
+    cudaStreamSynchronize(ctx->stream);
+    nn_release(b);
+    nn_release(x);
+    return st;
+}
+
 extern "C" nn_status nn_sim_set_pull_rate(nn_sim* s, float pull_rate)
 {
     if (!s || !(pull_rate >= 0.0f)) return NN_ERR_INVALID_ARG;

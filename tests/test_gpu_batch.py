@@ -72,6 +72,79 @@ def test_batched_pcg_matches_single_solves(ctx, orc):
         assert abs(int(its[k]) - it1) <= 3, (k, its[k], it1)
 
 
+def test_batched_pcg_block_layouts_and_autotune(ctx, orc):
+    """Every block layout of the batched PCG (512 .. 4,096 cells per block)
+    solves each instance within 1e-5 of FP64 CG; the autotuner picks one of
+    them and leaves the solver correct."""
+    sides = [16, 24, 20, 32, 12]
+    alpha_unit, beta = 4e-3, 1e-4
+    bp = nn.BatchedPCG(ctx, sides, alpha_unit, beta)
+    rng = np.random.default_rng(1)
+    G = int(bp.offsets[-1])
+    b = np.zeros(G, np.float32)
+    b[rng.integers(0, G, 500)] += 1.0
+    b += 0.01 * rng.random(G).astype(np.float32)
+    db = ctx.to_device(b)
+    refs = []
+    for k, g in enumerate(sides):
+        lo, hi = bp.offsets[k], bp.offsets[k + 1]
+        refs.append(orc.pcg7(b[lo:hi], np.zeros(hi - lo), (g, g, g), alpha_unit * g * g, beta, rtol=1e-12)[0])
+
+    def check():
+        dx = ctx.to_device(np.zeros(G, np.float32))
+        its, bad = bp.solve(db, dx, 1e-6, 5000)
+        assert bad == 0
+        x = dx.numpy()
+        for k in range(len(sides)):
+            lo, hi = bp.offsets[k], bp.offsets[k + 1]
+            assert np.linalg.norm(x[lo:hi] - refs[k]) <= 1e-5 * np.linalg.norm(refs[k]), k
+        return its
+
+    its = [check() for cpb in (512, 1024, 2048, 4096) if bp.set_cells_per_block(cpb) is None]
+    assert all(np.abs(i.astype(int) - its[2]).max() <= 2 for i in its)
+    cpb, ms = bp.autotune(db, ctx.to_device(np.zeros(G, np.float32)), 8)
+    assert cpb in (512, 1024, 2048, 4096) and ms > 0
+    check()
+
+
+def test_solver_autotune_keeps_simulation(ctx):
+    """The field solver's autotuner (batched block size; single-grid tile
+    depth) works on scratch vectors: the neurons stay bit-identical to an
+    untuned twin's, the fields agree within the solves' tolerance."""
+    a, _ = batch_sim(ctx, seed=5)
+    b, _ = batch_sim(ctx, seed=5)
+    a.step(100)
+    b.step(100)
+    cpb, ms = a.autotune_solver(5)
+    assert cpb in (512, 1024, 2048, 4096) and ms > 0
+    a.step(200)
+    b.step(200)
+    for k in ("V", "M", "H", "N"):
+        assert np.array_equal(a.get_field(k), b.get_field(k)), k
+    ua, ub = a.get_density(), b.get_density()
+    assert np.linalg.norm(ua - ub) <= 1e-4 * np.linalg.norm(ub)
+    sims = []
+    for tune in (True, False):
+        c = nn.default_config(2000)
+        c.seed, c.grid, c.timescale = 7, 32, 50
+        s = nn.Simulation(ctx, c)
+        spec = nn.default_net_spec(nn.NN_NET_ER)
+        s.generate_network(spec)
+        s.init_state(-65.0, 5.0, 15.0)
+        s.set_field("V", np.random.default_rng(7).uniform(-65, -35, 2000).astype(np.float32))
+        s.step(50)
+        if tune:
+            zc, ms = s.autotune_solver(5)
+            assert zc in (4, 6, 8, 12, 16, 24, 32) and ms > 0
+        s.step(150)
+        sims.append(s)
+    for k in ("V", "M", "H", "N"):
+        assert np.array_equal(sims[0].get_field(k), sims[1].get_field(k)), k
+    ua, ub = sims[0].get_density(), sims[1].get_density()
+    assert np.linalg.norm(ub) > 0
+    assert np.linalg.norm(ua - ub) <= 1e-4 * np.linalg.norm(ub)
+
+
 def test_batch_simulation_matches_oracle(ctx, orc):
     s, off = batch_sim(ctx)
     rp, col, w, d, inh = s.get_network()
