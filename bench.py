@@ -17,7 +17,11 @@ resident path; ``e2e`` is the same metric through the C-ABI entry point that
 takes host state buffers (host<->device copies inside the timed region).
 ``parity`` compares the GPU with the FP64 oracle over 50 timesteps started
 from the GPU's state inside a population burst (after the timed region), and
-``cpu_baseline`` is that oracle's time on the host cores.
+``cpu_baseline`` is that oracle's time on the host cores.  Spike delivery is
+chosen per period by the measured firing rate (``delivery``).  Two more
+workloads ride along in the default line: ``cg_256cube`` (CG time to 1e-6 on
+the 256^3 heterogeneous grid: plain, multigrid, learned multigrid) and
+``batch256`` (256 independent networks in one simulation, both autotuners).
 ``--impl reference`` times the CPU oracle port of the same workload on the
 host cores instead (the reference has no runnable CPU implementation of the
 path); it builds the network and initial state with the oracle's own
@@ -375,7 +379,22 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     if args.c5 and rank == 0 and args.gpus == 1 and wl["workload"] == WORKLOADS["c2"]["workload"]:
         line["cg_256cube"] = c5_leg(nn, ctx, args)
     ctx.close()
+    if args.c4 and rank == 0 and args.gpus == 1 and wl["workload"] == WORKLOADS["c2"]["workload"]:
+        line["batch256"] = c4_leg(args, local_rank)
     return line
+
+
+def c4_leg(args, local_rank: int) -> dict:
+    """The batched configuration (256 networks of 1k-64k neurons, their own
+    32^3-64^3 grids) in the default line: the `--workload c4` measurement with
+    3 timed steps of 2,000 timesteps after 1 warm-up step, both autotuners run
+    first."""
+    a = argparse.Namespace(**vars(args))
+    a.steps, a.warmup, a.e2e_steps = 3, 1, 1
+    r = run_batch(a, WORKLOADS["c4"], None, 0, local_rank)
+    keep = ("value", "unit", "steps", "warmup", "ms_per_step", "config", "spikes_in_timed_region", "cg", "timestep",
+            "gpu_launches", "clocks", "e2e")
+    return {k: r[k] for k in keep if k in r}
 
 
 def c5_leg(nn, ctx, args) -> dict:
@@ -1205,6 +1224,8 @@ def main() -> None:
                     help="spike delivery: push, pull, or auto (per period by the measured firing rate)")
     ap.add_argument("--electrode-every", type=int, default=1,
                     help="electrode sampling interval in steps (40 = 0.4 ms, the reference's leapfrog step)")
+    ap.add_argument("--no-c4", dest="c4", action="store_false",
+                    help="default workload: skip the batched-networks leg")
     ap.add_argument("--no-c5", dest="c5", action="store_false",
                     help="default workload: skip the 256^3 CG time-to-tolerance leg")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
