@@ -48,7 +48,9 @@ struct ConvCfg {
     // 96 KB, else as many as fit (at least two); large grids use two, which
     // leaves room for more CTAs per SM
     static constexpr int STAGES = 96 * 1024 / STAGE_STRIDE >= 9 ? 9 : (96 * 1024 / STAGE_STRIDE < 2 ? 2 : 96 * 1024 / STAGE_STRIDE);
-    static constexpr int SMEM = 128 + STAGES * STAGE_STRIDE + NN_CONV_SMEM_SLACK;  // the most a launch uses
+    // grids of at most one tile per SM: as many stages as 200 KB hold
+    static constexpr int STAGES_BIG = 200 * 1024 / STAGE_STRIDE >= 9 ? 9 : (200 * 1024 / STAGE_STRIDE < 2 ? 2 : 200 * 1024 / STAGE_STRIDE);
+    static constexpr int SMEM = 128 + STAGES_BIG * STAGE_STRIDE + NN_CONV_SMEM_SLACK;  // the most a launch uses
     static int smem(int stages) { return 128 + stages * STAGE_STRIDE + NN_CONV_SMEM_SLACK; }
     static constexpr uint32_t TMEM_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
     static_assert(SMEM <= 227 * 1024, "shared memory");
@@ -64,7 +66,8 @@ struct ConvArgs {
     nn_act_geom g;
     int relu;
     int* err;
-    int stages;  // (dz, dy) stages in flight, 2 .. ConvCfg::STAGES
+    int stages;  // (dz, dy) stages in flight, 2 .. ConvCfg::STAGES_BIG
+    const double* y32_scale;
 };
 
 __device__ __forceinline__ unsigned char* align128(unsigned char* p)
@@ -110,7 +113,7 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
     extern __shared__ unsigned char smem_raw[];
     unsigned char* sm = align128(smem_raw);
     const int S = a.stages;
-    __shared__ uint64_t full[C::STAGES], done[C::STAGES], acc_bar;
+    __shared__ uint64_t full[C::STAGES_BIG], done[C::STAGES_BIG], acc_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -130,6 +133,8 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
     __syncthreads();
     nn_tc_fence_after();
     const uint32_t tmem = tmem_slot;
+    // the kernel before this one has finished with the activations
+    nn_grid_dep_wait();
 
     if (tid == 0) {
         int issued = 0;
@@ -179,6 +184,9 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
             for (int st = consumed; st < issued; ++st) nn_mbar_wait(&full[st % S], (st / S) & 1, CONV_WAIT_LIMIT);
         }
     }
+    // lanes 1-31 of warp 0 wait here for lane 0's issue loop: spinning on
+    // the mbarrier beside it would stall that loop at every wait
+    __syncwarp();
     if (!nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
     __syncthreads();
     nn_tc_fence_after();
@@ -204,7 +212,8 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
             }
             a.y[gb * a.g.S + a.g.GD + o] = pack_bf16x8(t);
             if (gb == 0 && a.y32 && in)
-                a.y32[((int64_t)(z - 1) * a.g.ny + (y - 1)) * a.g.nx + (x - 1)] = t[0];
+                a.y32[((int64_t)(z - 1) * a.g.ny + (y - 1)) * a.g.nx + (x - 1)] =
+                    a.y32_scale ? t[0] * (float)a.y32_scale[0] : t[0];
         }
     }
     nn_tc_fence_before();
@@ -350,6 +359,9 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad(const uint4* __restr
                 nn_mbar_wait(&full[j % S], (uint32_t)((j / S) & 1), CONV_WAIT_LIMIT);
         }
     }
+    // lanes 1-31 of warp 0 wait here for lane 0's issue loop: spinning on
+    // the mbarrier beside it would stall that loop at every wait
+    __syncwarp();
     if (!nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
     __syncthreads();
     nn_tc_fence_after();
@@ -468,9 +480,11 @@ nn_status launch_fwd(nn_ctx* ctx, const ConvArgs& a)
     // small grids (at most four tiles per SM) are latency-bound: all their
     // stages in flight; large ones keep two and more CTAs per SM
     ConvArgs b = a;
-    b.stages = a.g.tiles <= (int64_t)ctx->num_sms * 4 ? C::STAGES : 2;
-    k_conv3<CIN, COUT><<<(unsigned)a.g.tiles, CONV_THREADS, C::smem(b.stages), ctx->stream>>>(b);
-    NN_CHECK_LAUNCH(ctx, "k_conv3");
+    b.stages = a.g.tiles <= (int64_t)ctx->num_sms ? C::STAGES_BIG
+                                                  : (a.g.tiles <= (int64_t)ctx->num_sms * 4 ? C::STAGES : 2);
+    NN_CUDA(ctx, nn_launch_pdl(k_conv3<CIN, COUT>, dim3((unsigned)a.g.tiles), dim3(CONV_THREADS),
+                               (size_t)C::smem(b.stages), ctx->stream, b));
+    ctx->launches++;
     return NN_OK;
 }
 
@@ -515,9 +529,11 @@ bool nn_conv_supported(int cin, int cout)
 size_t nn_conv_packed_weight_bytes(int cin, int cout) { return (size_t)27 * cin * cout * 2; }
 
 nn_status nn_conv_forward(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, const void* x, const void* wpacked,
-                          const float* bias, int relu, const void* mask, void* y, float* y32, int* err)
+                          const float* bias, int relu, const void* mask, void* y, float* y32, int* err,
+                          const double* y32_scale)
 {
     ConvArgs a;
+    a.y32_scale = y32_scale;
     a.x = (const uint4*)x;
     a.w = (const unsigned char*)wpacked;
     a.bias = bias;

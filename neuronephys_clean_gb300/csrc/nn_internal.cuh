@@ -82,6 +82,29 @@ inline cudaError_t nn_copy_sync(nn_ctx* ctx, void* dst, const void* src, size_t 
 }
 inline cudaError_t nn_zero_async(nn_ctx* ctx, void* p, size_t bytes) { return cudaMemsetAsync(p, 0, bytes, ctx->stream); }
 
+// Programmatic dependent launch: the kernel may begin while the kernel before
+// it on the stream finishes (its launch and prologue overlap that kernel's
+// tail).  Such a kernel calls nn_grid_dep_wait() before it touches any memory
+// the kernels before it write or read; without a programmatic dependency the
+// wait returns at once.
+template <typename... KArgs, typename... Args>
+inline cudaError_t nn_launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                 Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+__device__ __forceinline__ void nn_grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 inline int nn_grid_for(const nn_ctx* ctx, int64_t work, int threads, int per_sm = 8)
 {
     int64_t b = (work + threads - 1) / threads;

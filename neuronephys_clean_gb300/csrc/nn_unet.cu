@@ -77,6 +77,7 @@ __device__ __forceinline__ int64_t vox(const nn_act_geom& g, int z, int y, int x
 // coarse(c) = mean of its 8 children, per 8-channel block
 __global__ void k_pool(const uint4* src, nn_act_geom gf, const uint4* dummy, uint4* dst, nn_act_geom gc, int groups)
 {
+    nn_grid_dep_wait();
     const int64_t G = (int64_t)gc.nz * gc.ny * gc.nx;
     GRID_LOOP(e, G * groups)
     {
@@ -100,6 +101,7 @@ __global__ void k_pool(const uint4* src, nn_act_geom gf, const uint4* dummy, uin
 // fine(c) = coarse(parent)            (nearest upsampling)
 __global__ void k_up(const uint4* src, nn_act_geom gc, uint4* dst, nn_act_geom gf, int groups)
 {
+    nn_grid_dep_wait();
     const int64_t G = (int64_t)gf.nz * gf.ny * gf.nx;
     GRID_LOOP(e, G * groups)
     {
@@ -153,14 +155,18 @@ __global__ void k_skip_grad(const uint4* a, const uint4* b, nn_act_geom gc, cons
 }
 
 // network input: channel 0 = r / s, channel 1 = log D (0 if absent), 2..15 = 0
-__global__ void k_net_input(const float* r, const float* logd, const double* s, uint4* in, nn_act_geom g)
+// (d given: the input is r / d, formed here)
+__global__ void k_net_input(const float* r, const float* d, const float* logd, const double* s, uint4* in,
+                            nn_act_geom g)
 {
+    nn_grid_dep_wait();
     const int64_t G = (int64_t)g.nz * g.ny * g.nx;
     const float inv = s[0] > 0.0 ? (float)(1.0 / s[0]) : 0.0f;
     GRID_LOOP(c, G)
     {
         const int x = (int)(c % g.nx), y = (int)((c / g.nx) % g.ny), z = (int)(c / ((int64_t)g.nx * g.ny));
-        float f[8] = {r[c] * inv, logd ? logd[c] : 0.0f, 0, 0, 0, 0, 0, 0};
+        const float rc = d ? r[c] / d[c] : r[c];
+        float f[8] = {rc * inv, logd ? logd[c] : 0.0f, 0, 0, 0, 0, 0, 0};
         in[g.GD + vox(g, z, y, x)] = pack8(f);
     }
 }
@@ -184,15 +190,49 @@ __global__ void k_net_loss(const float* y32, const float* t, const double* s, ui
 }
 
 // sum of squares -> s = sqrt(mean)
-__global__ void k_sumsq(const float* v, int64_t n, double* out)
+// s[0] = rms of v (of v / d with d given) in one launch: per-block FP64
+// partial sums; the last block to finish adds them in block order and resets
+// the ticket.  Its grid must be the partials' length.
+__global__ void __launch_bounds__(UT) k_rms(const float* v, const float* d, int64_t n, double* partials,
+                                            unsigned int* ticket, double* s)
 {
+    nn_grid_dep_wait();
+    __shared__ double ws[UT / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     double acc = 0.0;
-    GRID_LOOP(i, n) acc += (double)v[i] * v[i];
+    GRID_LOOP(i, n)
+    {
+        const float x = d ? v[i] / d[i] : v[i];
+        acc += (double)x * x;
+    }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+    if (lane == 0) ws[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int u = 0; u < UT / 32; ++u) t += ws[u];
+        partials[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const volatile double* pp = partials;
+    double t = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += UT) t += pp[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    __syncthreads();
+    if (lane == 0) ws[w] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int u = 0; u < UT / 32; ++u) tot += ws[u];
+        s[0] = sqrt(tot / (double)n);
+        *ticket = 0;
+    }
 }
-
-__global__ void k_rms_finish(double* s, int64_t n) { s[0] = sqrt(s[0] / (double)n); }
 
 __global__ void k_scale_out(const float* y, const double* s, float* z, int64_t n)
 {
@@ -385,6 +425,9 @@ struct nn_unet {
     void *gB2b = nullptr, *gB2a = nullptr, *gP2 = nullptr;
     float* y32 = nullptr;
     double* scal = nullptr;  // [0] s, [1] loss
+    double* partials = nullptr;  // k_rms block sums
+    unsigned int* ticket = nullptr;
+    int rms_blocks = 0;
     int* err = nullptr;
     int adam_t = 0;
     std::vector<void*> bufs;
@@ -501,6 +544,9 @@ nn_status nn_unet_make(nn_ctx* ctx, int nz, int ny, int nx, uint64_t seed, nn_un
     if (st == NN_OK) st = act_alloc(u, &u->gP2, 2, 32);
     if (st == NN_OK) st = buf_alloc(u, &u->y32, (size_t)u->G0);
     if (st == NN_OK) st = buf_alloc(u, &u->scal, 4);
+    u->rms_blocks = nn_grid_for(ctx, u->G0, UT, 8);
+    if (st == NN_OK) st = buf_alloc(u, &u->partials, (size_t)u->rms_blocks);
+    if (st == NN_OK) st = buf_alloc(u, &u->ticket, 1);
     if (st == NN_OK) st = buf_alloc(u, &u->err, 1);
     if (st != NN_OK) {
         nn_unet_free(u);
@@ -511,10 +557,10 @@ nn_status nn_unet_make(nn_ctx* ctx, int nz, int ny, int nx, uint64_t seed, nn_un
 }
 
 static nn_status conv(nn_unet* u, int l, const void* x, void* y, bool relu, const void* mask = nullptr,
-                      float* y32 = nullptr)
+                      float* y32 = nullptr, const double* y32_scale = nullptr)
 {
     return nn_conv_forward(u->ctx, u->g[LLEVEL[l]], LCIN[l], LCOUT[l], x, u->L[l].wp, u->L[l].b, relu ? 1 : 0, mask,
-                           y, y32, u->err);
+                           y, y32, u->err, y32_scale);
 }
 
 // input gradient of layer l (adjoint weights), masked by `mask` (> 0) if given
@@ -537,33 +583,47 @@ static nn_status launch(nn_ctx* ctx, int64_t work, const char* what, K kern, A..
     return NN_OK;
 }
 
-// forward pass; rc: dense level-0 input (already divided into s by k_net_input)
-static nn_status unet_forward(nn_unet* u, const float* rc, const float* logd)
+// the same as a programmatic dependent of the kernel before it (the kernel
+// starts with nn_grid_dep_wait)
+template <class... KA, class... A>
+static nn_status launch_pdl(nn_ctx* ctx, int64_t work, const char* what, void (*kern)(KA...), A... args)
+{
+    NN_CUDA(ctx, nn_launch_pdl(kern, dim3(nn_grid_for(ctx, work, UT, 8)), dim3(UT), 0, ctx->stream, args...));
+    NN_CHECK_LAUNCH(ctx, what);
+    return NN_OK;
+}
+
+// forward pass; rc: dense level-0 input (divided by d when d is given, then
+// by its rms s in k_net_input).  out (nullable): the result times s, written
+// by the output layer, instead of the unscaled y32.  Every kernel is a
+// programmatic dependent of the one before it.
+static nn_status unet_forward(nn_unet* u, const float* rc, const float* logd, const float* d = nullptr,
+                              float* out = nullptr)
 {
     nn_ctx* ctx = u->ctx;
     const nn_act_geom &g0 = u->g[0], &g1 = u->g[1], &g2 = u->g[2];
-    NN_CUDA(ctx, cudaMemsetAsync(u->scal, 0, sizeof(double), ctx->stream));
-    NN_TRY(launch(ctx, u->G0, "k_sumsq", k_sumsq, rc, u->G0, u->scal));
-    NN_TRY(launch(ctx, 1, "k_rms_finish", k_rms_finish, u->scal, u->G0));
-    NN_TRY(launch(ctx, u->G0, "k_net_input", k_net_input, rc, logd, (const double*)u->scal, (uint4*)u->I0, g0));
+    NN_CUDA(ctx, nn_launch_pdl(k_rms, dim3(u->rms_blocks), dim3(UT), 0, ctx->stream, rc, d, u->G0, u->partials,
+                               u->ticket, u->scal));
+    NN_CHECK_LAUNCH(ctx, "k_rms");
+    NN_TRY(launch_pdl(ctx, u->G0, "k_net_input", k_net_input, rc, d, logd, (const double*)u->scal, (uint4*)u->I0, g0));
     void* SK0 = blk(u->CAT0, g0, 4);  // skip0 = channels 32..47 of CAT0
     void* SK1 = blk(u->CAT1, g1, 8);  // skip1 = channels 64..95 of CAT1
     NN_TRY(conv(u, L_E0A, u->I0, u->E0a, true));
     NN_TRY(conv(u, L_E0B, u->E0a, SK0, true));
     const int64_t G1 = (int64_t)g1.nz * g1.ny * g1.nx, G2 = (int64_t)g2.nz * g2.ny * g2.nx;
-    NN_TRY(launch(ctx, G1 * 2, "k_pool", k_pool, (const uint4*)SK0, g0, (const uint4*)nullptr, (uint4*)u->P1, g1, 2));
+    NN_TRY(launch_pdl(ctx, G1 * 2, "k_pool", k_pool, (const uint4*)SK0, g0, (const uint4*)nullptr, (uint4*)u->P1, g1, 2));
     NN_TRY(conv(u, L_E1A, u->P1, u->E1a, true));
     NN_TRY(conv(u, L_E1B, u->E1a, SK1, true));
-    NN_TRY(launch(ctx, G2 * 4, "k_pool", k_pool, (const uint4*)SK1, g1, (const uint4*)nullptr, (uint4*)u->P2, g2, 4));
+    NN_TRY(launch_pdl(ctx, G2 * 4, "k_pool", k_pool, (const uint4*)SK1, g1, (const uint4*)nullptr, (uint4*)u->P2, g2, 4));
     NN_TRY(conv(u, L_B2A, u->P2, u->B2a, true));
     NN_TRY(conv(u, L_B2B, u->B2a, u->B2b, true));
-    NN_TRY(launch(ctx, G1 * 8, "k_up", k_up, (const uint4*)u->B2b, g2, (uint4*)u->CAT1, g1, 8));
+    NN_TRY(launch_pdl(ctx, G1 * 8, "k_up", k_up, (const uint4*)u->B2b, g2, (uint4*)u->CAT1, g1, 8));
     NN_TRY(conv(u, L_D1A, u->CAT1, u->D1a, true));
     NN_TRY(conv(u, L_D1B, u->D1a, u->D1b, true));
-    NN_TRY(launch(ctx, u->G0 * 4, "k_up", k_up, (const uint4*)u->D1b, g1, (uint4*)u->CAT0, g0, 4));
+    NN_TRY(launch_pdl(ctx, u->G0 * 4, "k_up", k_up, (const uint4*)u->D1b, g1, (uint4*)u->CAT0, g0, 4));
     NN_TRY(conv(u, L_D0A, u->CAT0, u->D0a, true));
     NN_TRY(conv(u, L_D0B, u->D0a, u->D0b, true));
-    NN_TRY(conv(u, L_OUT, u->D0b, u->OUT, false, nullptr, u->y32));
+    NN_TRY(conv(u, L_OUT, u->D0b, u->OUT, false, nullptr, out ? out : u->y32, out ? (const double*)u->scal : nullptr));
     return NN_OK;
 }
 
@@ -973,10 +1033,9 @@ struct nn_lmg {
 static nn_status lmg_level_solve(void* user, const float* b, float* x)
 {
     nn_lmg* lm = static_cast<nn_lmg*>(user);
-    NN_TRY(launch(lm->ctx, lm->Gc, "k_div", k_div, b, lm->diag, lm->bs, lm->Gc));
-    NN_TRY(unet_forward(lm->net, lm->bs, lm->feat));
-    return launch(lm->ctx, lm->Gc, "k_scale_out", k_scale_out, (const float*)lm->net->y32,
-                  (const double*)lm->net->scal, x, lm->Gc);
+    // x = s N(D^-1 b / s, f): the division, the rms and the final scaling run
+    // inside the network's first and last kernels
+    return unet_forward(lm->net, b, lm->feat, lm->diag, x);
 }
 
 static nn_status lmg_record(void* user, const float* b)

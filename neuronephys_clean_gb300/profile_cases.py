@@ -5,6 +5,7 @@
     python -m neuronephys_clean_gb300.profile_cases cghet    # 3 PCG iterations, 128^3, lognormal D
     python -m neuronephys_clean_gb300.profile_cases conv128  # 3x3x3 convs (16->16, 48->16) + wgrad at 128^3
     python -m neuronephys_clean_gb300.profile_cases mg256    # multigrid FCG solve to 1e-6, 256^3, lognormal D
+    python -m neuronephys_clean_gb300.profile_cases lmg256   # the same with the learned 32^3 level (20 training steps)
     python -m neuronephys_clean_gb300.profile_cases pull1m   # one pull gather, 1M neurons, 1e8 synapses, delays 1..20
     python -m neuronephys_clean_gb300.profile_cases burst1m  # 200 steps of the 1M-neuron workload from rest: its first burst
     python -m neuronephys_clean_gb300.profile_cases burst1m_steps  # its first 400 steps timed one by one (no ncu)
@@ -81,6 +82,19 @@ def mg256(ctx):
     mg.solve(b, x, rtol=1e-6)
 
 
+def lmg256(ctx):
+    from neuronephys_clean_gb300 import fields
+    n = 256
+    D = ctx.to_device(fields.lognormal_diffusivity((n, n, n), 1.0, 8.0, seed=1).ravel())
+    b = fields.spike_sources((n, n, n), 20000, 2.0, seed=2)
+    pc = nn.PCG(ctx, n, n, n, 1e-3 * n * n, 1e-4, D)
+    lm = nn.LearnedMultigrid(pc, level=3)
+    lm.add_solves([fields.spike_sources((n, n, n), 20000, 2.0, seed=3)])
+    lm.train(20)
+    x = ctx.to_device(np.zeros(n ** 3, np.float32))
+    lm.solve(ctx.to_device(b), x, rtol=1e-6)
+
+
 def pull1m(ctx):
     n = 1_000_000
     c = nn.default_config(n)
@@ -140,7 +154,8 @@ def burst1m(ctx):
     _burst_sim(ctx).step(200)
 
 
-CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128, "mg256": mg256, "pull1m": pull1m,
+CASES = {"hh1m": hh1m, "cg128": cg128, "cghet": cghet, "conv128": conv128, "mg256": mg256, "lmg256": lmg256,
+         "pull1m": pull1m,
          "burst1m": burst1m, "burst1m_steps": burst1m_steps}
 
 
