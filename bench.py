@@ -452,11 +452,15 @@ def c5_leg(nn, ctx, args) -> dict:
                            for j in range(wl["train_rhs"])])
     loss = lm.train(wl["lmg_train_steps"], 1e-3)
     t_train = time.perf_counter() - t0
+    # Jacobi sweeps after the network's correction, chosen by timing a solve
+    # of one training right-hand side
+    post_sweeps, _ = lm.autotune_post_sweeps(
+        [ctx.to_device(fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=2000 + j)) for j in range(3)])
     learned = lambda rb, x: lm.solve(rb, x, 1e-6)  # noqa: E731
     ms, it, rel = timed(learned, bench_rhs)
     sols["learned_multigrid"] = dx.numpy().astype(np.float64)
     out["learned_multigrid"] = {"ms_to_tol": ms, "iterations": it, "relres": rel, "network_level_grid": 32,
-                                "held_out": held(learned),
+                                "post_sweeps": post_sweeps, "held_out": held(learned),
                                 "training": {"right_hand_sides": wl["train_rhs"], "pairs": pairs,
                                              "adam_steps": wl["lmg_train_steps"], "s": t_train, "final_loss": loss}}
     lm.close()
@@ -880,6 +884,7 @@ def learned_multigrid_cg(nn, ctx, pc, wl, shape, G, db, plain_ms, plain_iters, a
     t0 = time.perf_counter()
     loss = lm.train(wl["lmg_train_steps"], 1e-3)
     t_train = time.perf_counter() - t0
+    post_sweeps, _ = lm.autotune_post_sweeps([ctx.to_device(r) for r in rhs[:3]])
     dx = ctx.empty((G,), np.float32)
 
     def timed(solve):
@@ -904,6 +909,7 @@ def learned_multigrid_cg(nn, ctx, pc, wl, shape, G, db, plain_ms, plain_iters, a
     cut.close()
     return {"ms_to_tol": ms, "iterations": it, "relres": rel, "vs_plain_time": ms / plain_ms,
             "vs_plain_iterations": it / plain_iters, "network_level_grid": shape[0] >> level,
+            "post_sweeps": post_sweeps,
             "classical_hierarchy": {"ms_to_tol": ms_c, "iterations": it_c},
             "cut_at_network_level": {"ms_to_tol": ms_t, "iterations": it_t},
             "training": {"pairs": pairs, "pair_generation_s": t_pairs, "adam_steps": wl["lmg_train_steps"],

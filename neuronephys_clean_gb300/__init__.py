@@ -801,6 +801,20 @@ class LearnedMultigrid:
     def use_network(self, on: bool = True) -> None:
         _check(lib().nn_lmg_use_network(self.handle, int(on)), self.ctx, "nn_lmg_use_network")
 
+    def set_post_sweeps(self, sweeps: int) -> None:
+        """Jacobi sweeps on the network's level after its correction (default 2)."""
+        _check(lib().nn_lmg_set_post_sweeps(self.handle, sweeps), self.ctx, "nn_lmg_set_post_sweeps")
+
+    def autotune_post_sweeps(self, rhs, rtol: float = 1e-6) -> tuple[int, float]:
+        """Pick the post-network sweeps (2 .. 16) by timing solves of the device
+        right-hand sides `rhs` (a list); returns (sweeps, total ms of its solves)."""
+        x = self.ctx.empty((int(np.prod(rhs[0].shape)),), np.float32)
+        ptrs = (C.c_void_p * len(rhs))(*[r.ptr for r in rhs])
+        best, ms = C.c_int(0), C.c_float(0)
+        _check(lib().nn_lmg_autotune_post_sweeps(self.handle, ptrs, len(rhs), x.ptr, rtol, C.byref(best),
+                                                 C.byref(ms)), self.ctx, "nn_lmg_autotune_post_sweeps")
+        return best.value, ms.value
+
     def solve(self, b: DeviceArray, x: DeviceArray, rtol: float = 1e-6, max_iter: int = 1000) -> tuple[int, float]:
         it, rel = C.c_int(0), C.c_double(0)
         _check(lib().nn_lmg_solve(self.handle, b.ptr, x.ptr, rtol, max_iter, C.byref(it), C.byref(rel)), self.ctx,

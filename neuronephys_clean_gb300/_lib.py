@@ -186,6 +186,8 @@ _SIGS = {
     "nn_lmg_pairs": (c_int, [c_void_p, P(c_int)]),
     "nn_lmg_train": (c_int, [c_void_p, c_int, c_float, P(c_float)]),
     "nn_lmg_use_network": (c_int, [c_void_p, c_int]),
+    "nn_lmg_set_post_sweeps": (c_int, [c_void_p, c_int]),
+    "nn_lmg_autotune_post_sweeps": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_double, P(c_int), P(c_float)]),
     "nn_lmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_int, P(c_int), P(c_double)]),
     "nn_learned_create": (c_int, [c_void_p, c_uint64, P(c_void_p)]),
     "nn_learned_destroy": (c_int, [c_void_p]),

@@ -215,6 +215,7 @@ typedef nn_status (*nn_mg_level_fn)(void* user, const float* d_b, float* d_x);
 typedef nn_status (*nn_mg_record_fn)(void* user, const float* d_b);
 nn_status nn_mg_set_level_solver(nn_mg* mg, int level, nn_mg_level_fn fn, void* user);  // fn null: classical
 nn_status nn_mg_set_recorder(nn_mg* mg, int level, nn_mg_record_fn fn, void* user);    // fn null: off
+nn_status nn_mg_set_level_sweeps(nn_mg* mg, int sweeps);  // smoothing sweeps after the level solver (default 2)
 // dims and diagonal of level >= 1
 nn_status nn_mg_level_dims(const nn_mg* mg, int level, int* nx, int* ny, int* nz, const float** diag);
 // Jacobi-PCG on level >= 1 from x = 0 to rtol (synchronising; for training targets)

@@ -825,6 +825,7 @@ struct nn_mg {
     int hook_level = -1;
     nn_mg_level_fn hook_fn = nullptr;
     void* hook_user = nullptr;
+    int hook_sweeps = 2;  // smoothing sweeps after the level solver
     // optional recorder of the right-hand sides that reach one level (solves
     // then run without the captured graph)
     int rec_level = -1;
@@ -900,12 +901,12 @@ nn_status vlevel(nn_mg* mg, int l, const Op& op, const float* b, float* out, con
     MgLevel& L = mg->lv[l];
     if (mg->rec_fn && l == mg->rec_level) NN_TRY(mg->rec_fn(mg->rec_user, b));
     if (mg->hook_fn && l == mg->hook_level) {
-        // the caller's solver for this level, then nu smoothing sweeps
+        // the caller's solver for this level, then hook_sweeps smoothing sweeps
         float* cur = L.x;
         float* oth = L.t;
         NN_TRY(mg->hook_fn(mg->hook_user, b, cur));
-        for (int s = 0; s < mg->nu; ++s) {
-            float* dst = (s == mg->nu - 1 && out != cur) ? out : oth;
+        for (int s = 0; s < mg->hook_sweeps; ++s) {
+            float* dst = (s == mg->hook_sweeps - 1 && out != cur) ? out : oth;
             NN_TRY((launch_jacobi<V, false>(mg, op, b, cur, dst, flags)));
             oth = cur;
             cur = dst;
@@ -1215,6 +1216,14 @@ nn_status nn_mg_set_level_solver(nn_mg* mg, int level, nn_mg_level_fn fn, void* 
     mg->hook_fn = fn;
     mg->hook_user = user;
     mg->last_iters = 0;
+    return NN_OK;
+}
+
+nn_status nn_mg_set_level_sweeps(nn_mg* mg, int sweeps)
+{
+    if (!mg || sweeps < 0) return NN_ERR_INVALID_ARG;
+    drop_graph(mg);
+    mg->hook_sweeps = sweeps;
     return NN_OK;
 }
 

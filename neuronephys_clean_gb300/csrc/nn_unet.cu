@@ -1207,6 +1207,12 @@ extern "C" nn_status nn_lmg_use_network(nn_lmg* lm, int enable)
     return lmg_apply_mode(lm);
 }
 
+extern "C" nn_status nn_lmg_set_post_sweeps(nn_lmg* lm, int sweeps)
+{
+    if (!lm) return NN_ERR_INVALID_ARG;
+    return nn_mg_set_level_sweeps(lm->mg, sweeps);
+}
+
 extern "C" nn_status nn_lmg_pairs(nn_lmg* lm, int* n)
 {
     if (!lm || !n) return NN_ERR_INVALID_ARG;
@@ -1221,5 +1227,51 @@ extern "C" nn_status nn_lmg_solve(nn_lmg* lm, const float* d_b, float* d_x, doub
     NN_CUDA(lm->ctx, cudaMemsetAsync(lm->net->err, 0, sizeof(int), lm->ctx->stream));
     const nn_status st = nn_mg_solve(lm->mg, d_b, d_x, rtol, max_iter, iters, relres);
     const nn_status st2 = check_err(lm->net);
+    return st != NN_OK ? st : st2;
+}
+
+// The number of Jacobi sweeps after the network's correction, chosen by time:
+// each candidate solves the nb right-hand sides d_bs[k] from zero (d_x:
+// scratch) to rtol, once to warm (graph capture) and once timed; the smallest
+// total time is kept.
+extern "C" nn_status nn_lmg_autotune_post_sweeps(nn_lmg* lm, const float* const* d_bs, int nb, float* d_x, double rtol,
+                                                 int* best, float* best_ms)
+{
+    if (!lm || !d_bs || nb < 1 || !d_x) return NN_ERR_INVALID_ARG;
+    nn_ctx* ctx = lm->ctx;
+    cudaStream_t cs = ctx->stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    NN_CUDA(ctx, cudaEventCreate(&e0));
+    NN_CUDA(ctx, cudaEventCreate(&e1));
+    int bsw = 2;
+    float bms = 1e30f;
+    nn_status st = NN_OK;
+    for (int sw : {2, 4, 8, 12, 16}) {
+        if (st != NN_OK) break;
+        st = nn_mg_set_level_sweeps(lm->mg, sw);
+        int it = 0;
+        double rel = 0.0;
+        float ms = 0.0f;
+        for (int k = 0; k < nb && st == NN_OK; ++k)
+            for (int rep = 0; rep < 2 && st == NN_OK; ++rep) {
+                st = nn_cuda_check(ctx, cudaMemsetAsync(d_x, 0, sizeof(float) * (size_t)lm->G, cs), "memset");
+                if (st == NN_OK && rep == 1) st = nn_cuda_check(ctx, cudaEventRecord(e0, cs), "event");
+                if (st == NN_OK) st = nn_lmg_solve(lm, d_bs[k], d_x, rtol, 1000, &it, &rel);
+                if (st == NN_OK && rep == 1) st = nn_cuda_check(ctx, cudaEventRecord(e1, cs), "event");
+                float m = 0.0f;
+                if (st == NN_OK && rep == 1) st = nn_cuda_check(ctx, cudaEventSynchronize(e1), "event");
+                if (st == NN_OK && rep == 1) st = nn_cuda_check(ctx, cudaEventElapsedTime(&m, e0, e1), "event");
+                ms += m;
+            }
+        if (st == NN_OK && ms < bms) {
+            bms = ms;
+            bsw = sw;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const nn_status st2 = nn_mg_set_level_sweeps(lm->mg, bsw);
+    if (best) *best = bsw;
+    if (best_ms) *best_ms = bms < 1e30f ? bms : 0.0f;
     return st != NN_OK ? st : st2;
 }

@@ -66,3 +66,12 @@ def test_learned_coarse_solver(ctx, orc):
     x = dx.numpy().astype(np.float64)
     ref, _, _ = orc.pcg7(b, np.zeros(G), shape, alpha, beta, D, rtol=1e-12)
     assert np.linalg.norm(x - ref) <= 1e-5 * np.linalg.norm(ref)
+    # Jacobi sweeps after the network's correction, chosen by time: the
+    # solve keeps its tolerance and its FP64 agreement
+    sw, ms = lm.autotune_post_sweeps([ctx.to_device(sources(shape, np.random.default_rng(100 + j))) for j in range(2)])
+    assert sw in (2, 4, 8, 12, 16) and ms > 0
+    dx.zero()
+    it_tuned, rel = lm.solve(db, dx)
+    assert rel <= 1e-6 and it_tuned <= it_trained + 1
+    x = dx.numpy().astype(np.float64)
+    assert np.linalg.norm(x - ref) <= 1e-5 * np.linalg.norm(ref)
