@@ -110,9 +110,10 @@ def test_batched_pcg_block_layouts_and_autotune(ctx, orc):
 def test_solver_autotune_keeps_simulation(ctx):
     """The field solver's autotuner (batched block size; single-grid tile
     depth) works on scratch vectors: the neurons stay bit-identical to an
-    untuned twin's, the fields agree within the solves' tolerance."""
-    a, _ = batch_sim(ctx, seed=5)
-    b, _ = batch_sim(ctx, seed=5)
+    untuned twin's, the fields agree within the solves' tolerance (pull
+    delivery: sums independent of arrival order)."""
+    a, _ = batch_sim(ctx, seed=5, delivery=1)
+    b, _ = batch_sim(ctx, seed=5, delivery=1)
     a.step(100)
     b.step(100)
     cpb, ms = a.autotune_solver(5)
@@ -126,7 +127,7 @@ def test_solver_autotune_keeps_simulation(ctx):
     sims = []
     for tune in (True, False):
         c = nn.default_config(2000)
-        c.seed, c.grid, c.timescale = 7, 32, 50
+        c.seed, c.grid, c.timescale, c.delivery = 7, 32, 50, nn.NN_DELIVERY_PULL
         s = nn.Simulation(ctx, c)
         spec = nn.default_net_spec(nn.NN_NET_ER)
         s.generate_network(spec)
