@@ -338,40 +338,47 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
     const int dlast = min(t1 < (uint64_t)(a.D - 1) ? (int)t1 : a.D - 1, a.dsl_dmax);
     const int32_t* cp = a.dsl_cptr + (size_t)blockIdx.x * (a.dsl_dmax + 1);
     const int cfirst = cp[0];
-    // the chunks of the live delays (all delays unless rowflag is given), in
-    // delay order: warp 0 scans their counts (two delays per lane)
+    // the chunks of the live delays, in delay order: all of them, or with
+    // rowflag given those whose source row was a pull step (warp 0 scans their
+    // counts, two delays per lane)
     __shared__ int s_off[DSL_MAX_DELAY + 1];
-    if (warp == 0) {
-        int len[2];
+    int C = 0;
+    if (!a.rowflag) {
+        C = dlast >= 1 ? cp[dlast] - cfirst : 0;
+        for (int c = tid; c < C; c += blockDim.x) tab[c] = a.dsl_chunk[cfirst + c];
+    } else {
+        if (warp == 0) {
+            int len[2];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int d = lane + 1 + 32 * h;
-            len[h] = 0;
-            if (d <= dlast) {
-                int hs = s1 - d;
-                if (hs < 0) hs += a.D;
-                if (!a.rowflag || a.rowflag[hs]) len[h] = cp[d] - cp[d - 1];
+            for (int h = 0; h < 2; ++h) {
+                const int d = lane + 1 + 32 * h;
+                len[h] = 0;
+                if (d <= dlast) {
+                    int hs = s1 - d;
+                    if (hs < 0) hs += a.D;
+                    if (a.rowflag[hs]) len[h] = cp[d] - cp[d - 1];
+                }
             }
-        }
-        int run = 0;
+            int run = 0;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            int v = len[h];
+            for (int h = 0; h < 2; ++h) {
+                int v = len[h];
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int u = __shfl_up_sync(0xffffffffu, v, o);
-                if (lane >= o) v += u;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int u = __shfl_up_sync(0xffffffffu, v, o);
+                    if (lane >= o) v += u;
+                }
+                s_off[lane + 1 + 32 * h] = run + v;  // live chunks of delays <= lane + 1 + 32 h
+                run += __shfl_sync(0xffffffffu, v, 31);
             }
-            s_off[lane + 1 + 32 * h] = run + v;  // live chunks of delays <= lane + 1 + 32 h
-            run += __shfl_sync(0xffffffffu, v, 31);
+            if (lane == 0) s_off[0] = 0;
         }
-        if (lane == 0) s_off[0] = 0;
-    }
-    __syncthreads();
-    const int C = dlast >= 1 ? s_off[dlast] : 0;
-    for (int d = 1; d <= dlast; ++d) {
-        const int o = s_off[d - 1], len = s_off[d] - o;
-        for (int c = tid; c < len; c += blockDim.x) tab[o + c] = a.dsl_chunk[cp[d - 1] + c];
+        __syncthreads();
+        C = dlast >= 1 ? s_off[dlast] : 0;
+        for (int d = 1; d <= dlast; ++d) {
+            const int o = s_off[d - 1], len = s_off[d] - o;
+            for (int c = tid; c < len; c += blockDim.x) tab[o + c] = a.dsl_chunk[cp[d - 1] + c];
+        }
     }
     // the block's hit list starts at its first entry: it has room for every entry
     uint2* hits = a.dsl_hits + (C > 0 ? a.dsl_chunk[cfirst].x : 0);
