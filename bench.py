@@ -612,6 +612,16 @@ def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | Non
                 nbytes = nnz * PULL_CSC_BYTES_PER_SYNAPSE + n * 8 + n // 8
             res[name] = {"ms": ms, "GBs": nbytes / (ms * 1e-3) / 1e9, "frac_of_peak": nbytes / (ms * 1e-3) / 1e9 / hbm_peak}
             if mode == nn.NN_DELIVERY_PULL:
+                # the gather kernel alone (the bitmap built above stays): the
+                # simulation's pull mode runs only this kernel, its bitmap
+                # written by the neuron update
+                sim.pull_gather()
+                ctx.time_begin()
+                for _ in range(reps):
+                    sim.pull_gather()
+                gms = ctx.time_end() / reps
+                res[name]["gather_ms"] = gms
+                res[name]["gather_frac_of_peak"] = nbytes / (gms * 1e-3) / 1e9 / hbm_peak
                 csc = nnz * PULL_CSC_BYTES_PER_SYNAPSE + n * 8 + n // 8
                 res[name]["bytes"] = nbytes
                 # the rate at which a sweep over the 9-byte CSC entries would
@@ -622,6 +632,8 @@ def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | Non
     cross = next((r["fraction"] for r in rows if r["pull"]["ms"] < r["push"]["ms"]), None)
     sim.close()
     ctx.close()
+    # "ms": list in, delivery out (the pull rebuilds the bitmap from the list
+    # first); "gather_ms": the pull gather kernel by itself
     return {"metric": "spike delivery GB/s vs firing fraction", "workload": wl["workload"], "neurons": n,
             "synapses": nnz, "peak_GBs": hbm_peak, "peak_source": peak_kind,
             "pull_kernel": (f"k_deliver_pull_sliced (chunked entries and bitmap ranges staged by bulk copies, "

@@ -348,6 +348,10 @@ NN_API nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int count, 
  * shared memory; *cols = columns per block), 0 for the warp-per-column
  * kernel.  No counterpart in the reference. */
 NN_API nn_status nn_sim_pull_info(nn_sim* s, int* sliced, int* cols);
+/* The pull gather alone, from the spike bitmap as it stands (for example
+ * after nn_sim_deliver_spikes with NN_DELIVERY_PULL): the input of the next
+ * step rewritten.  For timing the gather kernel by itself; asynchronous. */
+NN_API nn_status nn_sim_pull_gather(nn_sim* s);
 /* NN_DELIVERY_AUTO: the delivery mode of each period run since the last call
  * with reset != 0 (0 push, 1 pull) and the firing rate that chose it (spikes
  * per neuron and step of the latest period measured when it was enqueued;

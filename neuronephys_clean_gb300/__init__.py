@@ -531,6 +531,10 @@ class Simulation:
     def deliver_spikes(self, d_list: "DeviceArray", count: int, mode: int = NN_DELIVERY_PUSH) -> None:
         _check(lib().nn_sim_deliver_spikes(self.handle, d_list.ptr, count, mode), self.ctx, "sim_deliver_spikes")
 
+    def pull_gather(self) -> None:
+        """The pull gather kernel alone, from the current spike bitmap."""
+        _check(lib().nn_sim_pull_gather(self.handle), self.ctx, "sim_pull_gather")
+
     def pull_info(self) -> tuple[bool, int]:
         """(shared-memory sliced pull kernel in use, columns per block)."""
         a, b = C.c_int(0), C.c_int(0)

@@ -141,6 +141,7 @@ _SIGS = {
     "nn_pcg_set_kernel_timing": (c_int, [c_void_p, c_int]),
     "nn_sim_deliver_spikes": (c_int, [c_void_p, c_void_p, c_int, c_int]),
     "nn_sim_pull_info": (c_int, [c_void_p, P(c_int), P(c_int)]),
+    "nn_sim_pull_gather": (c_int, [c_void_p]),
     "nn_sim_delivery_log": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_int), c_int]),
     "nn_sim_set_pull_rate": (c_int, [c_void_p, c_float]),
     "nn_sim_autotune_solver": (c_int, [c_void_p, c_int, P(c_int), P(c_float)]),

@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
     // the chunks of the live delays, in delay order: all of them, or with
     // rowflag given those whose source row was a pull step (warp 0 scans their
     // counts, two delays per lane)
-    __shared__ int s_off[DSL_MAX_DELAY + 1];
+    __shared__ int s_off[DSL_MAX_DELAY + 1], s_cp[DSL_MAX_DELAY + 1];
     int C = 0;
     if (!a.rowflag) {
         C = dlast >= 1 ? cp[dlast] - cfirst : 0;
@@ -356,7 +356,9 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
                 if (d <= dlast) {
                     int hs = s1 - d;
                     if (hs < 0) hs += a.D;
-                    if (a.rowflag[hs]) len[h] = cp[d] - cp[d - 1];
+                    const int c0 = cp[d - 1];
+                    s_cp[d] = c0;  // first chunk of delay d
+                    if (a.rowflag[hs]) len[h] = cp[d] - c0;
                 }
             }
             int run = 0;
@@ -375,9 +377,16 @@ __global__ void __launch_bounds__(DSL_THREADS + 32, 1) k_deliver_pull_sliced(Pul
         }
         __syncthreads();
         C = dlast >= 1 ? s_off[dlast] : 0;
-        for (int d = 1; d <= dlast; ++d) {
-            const int o = s_off[d - 1], len = s_off[d] - o;
-            for (int c = tid; c < len; c += blockDim.x) tab[o + c] = a.dsl_chunk[cp[d - 1] + c];
+        // one pass over the live chunks: live chunk c belongs to the delay d
+        // with s_off[d - 1] <= c < s_off[d] (binary search)
+        for (int c = tid; c < C; c += blockDim.x) {
+            int lo = 1, hi = dlast;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (s_off[mid] > c) hi = mid;
+                else lo = mid + 1;
+            }
+            tab[c] = a.dsl_chunk[s_cp[lo] + (c - s_off[lo - 1])];
         }
     }
     // the block's hit list starts at its first entry: it has room for every entry
@@ -2486,6 +2495,14 @@ extern "C" nn_status nn_sim_deliver_spikes(nn_sim* s, const int* d_list, int cou
         NN_CHECK_LAUNCH(ctx, "k_list_bitmap");
     }
     return launch_pull(s, pull_args(s, 0, false), cs);
+}
+
+extern "C" nn_status nn_sim_pull_gather(nn_sim* s)
+{
+    if (!s) return NN_ERR_INVALID_ARG;
+    if (!s->bitmap || !s->col_ptr)
+        return nn_fail(s->ctx, NN_ERR_INVALID_ARG, "nn_sim_pull_gather: needs a simulation with pull delivery");
+    return launch_pull(s, pull_args(s, 0, false), s->ctx->stream);
 }
 
 extern "C" nn_status nn_sim_run_host(nn_sim* s, const float* h_in, int nsteps, float* h_out, int64_t* h_spikes)
