@@ -184,10 +184,12 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
             for (int st = consumed; st < issued; ++st) nn_mbar_wait(&full[st % S], (st / S) & 1, CONV_WAIT_LIMIT);
         }
     }
-    // lanes 1-31 of warp 0 wait here for lane 0's issue loop: spinning on
-    // the mbarrier beside it would stall that loop at every wait
+    // lanes 1-31 of warp 0 wait here for lane 0's issue loop (spinning on
+    // the mbarrier beside it would stall that loop at every wait); one thread
+    // then waits for the accumulator and the block barrier releases the rest,
+    // whose polls would otherwise take issue slots from the other CTAs
     __syncwarp();
-    if (!nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
+    if (tid == 0 && !nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
     __syncthreads();
     nn_tc_fence_after();
     if (abort_flag) {  // block-uniform: the TMEM loads below are warp-collective
@@ -359,10 +361,12 @@ __global__ void __launch_bounds__(WG_THREADS) k_conv3_wgrad(const uint4* __restr
                 nn_mbar_wait(&full[j % S], (uint32_t)((j / S) & 1), CONV_WAIT_LIMIT);
         }
     }
-    // lanes 1-31 of warp 0 wait here for lane 0's issue loop: spinning on
-    // the mbarrier beside it would stall that loop at every wait
+    // lanes 1-31 of warp 0 wait here for lane 0's issue loop (spinning on
+    // the mbarrier beside it would stall that loop at every wait); one thread
+    // then waits for the accumulator and the block barrier releases the rest,
+    // whose polls would otherwise take issue slots from the other CTAs
     __syncwarp();
-    if (!nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
+    if (tid == 0 && !nn_mbar_wait(&acc_bar, 0, CONV_WAIT_LIMIT)) abort_flag = 1;
     __syncthreads();
     nn_tc_fence_after();
     if (abort_flag) {  // block-uniform: the TMEM loads below are warp-collective
