@@ -301,12 +301,15 @@ NN_API nn_status nn_sim_set_instances(nn_sim* s, int n_inst, const int* h_offset
  * neurons per thread 1/2/4) candidate on the simulation's own network and
  * state, keeps the fastest and restores the state the trials touched. */
 NN_API nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, int* best_npt, float* best_ms);
-/* Autotuner of the field solver's block shape, on scratch vectors (the
- * simulation's state is not touched): for a single grid the z-depth of the
- * 32 x 16 tiles of the one-kernel PCG iteration (4 .. 32; NN_ERR_UNSUPPORTED
- * when the grid runs the two-kernel PCG), for a batch the batched PCG's cells
- * per block.  *shape: the chosen depth or cells per block; *ms_per_iter: its
- * iteration time. */
+/* Autotuner of the field solver's block shape: for a single grid the z-depth
+ * of the 32 x 16 tiles of the one-kernel PCG iteration (4 .. 32;
+ * NN_ERR_UNSUPPORTED when the grid runs the two-kernel PCG), for a batch the
+ * batched PCG's cells per block.  When the solve overlaps the neuron updates
+ * (par_overlap, no field feedback) each depth is timed over six whole periods
+ * from a snapshot of the simulation, which is restored afterwards;
+ * *ms_per_iter then holds the time per timestep.  Otherwise the solver is
+ * timed alone on scratch vectors and *ms_per_iter is its iteration time.
+ * *shape: the chosen depth or cells per block. */
 NN_API nn_status nn_sim_autotune_solver(nn_sim* s, int trial_iters, int* shape, float* ms_per_iter);
 /* Per-instance solver iteration counts of the last paracrine solve (n_inst entries). */
 NN_API nn_status nn_sim_instance_iterations(nn_sim* s, int* h_iters);

@@ -887,3 +887,11 @@ nn_status nn_cg_plan_autotune(nn_cg_plan* pl, const float* d_b, float* d_x, int 
 }
 
 int nn_cg_plan_tile_depth(const nn_cg_plan* pl) { return pl->zc; }
+
+// Set the tile depth (4 .. 32).
+void nn_cg_plan_set_tile_depth(nn_cg_plan* pl, int zc)
+{
+    const int64_t cols = (int64_t)((pl->nx + TX - 1) / TX) * ((pl->ny + TY - 1) / TY);
+    pl->zc = zc;
+    pl->tiles = (int)(cols * ((pl->nz + zc - 1) / zc));
+}

@@ -250,8 +250,11 @@ bool nn_pcg_async_supported(const nn_pcg* pc);
 void nn_cg_last_timing(const nn_cg_plan* pl, float* ms, int* iters);
 nn_status nn_cg_plan_autotune(nn_cg_plan* pl, const float* d_b, float* d_x, int iters, int* zc_out, float* ms_out);
 int nn_cg_plan_tile_depth(const nn_cg_plan* pl);
+void nn_cg_plan_set_tile_depth(nn_cg_plan* pl, int zc);
 struct nn_pcg;
 nn_status nn_pcg_autotune_tiles(nn_pcg* pc, int iters, int* tile_z, float* ms_per_iter);
+int nn_pcg_tile_depth(const nn_pcg* pc);
+void nn_pcg_set_tile_depth(nn_pcg* pc, int zc);
 double nn_host_inv_phi(double p);
 void nn_host_gauss_table(double sigma_sites, int16_t* table4096);
 

@@ -545,6 +545,13 @@ __global__ void k_pcg_trial_rhs(float* b, int64_t G)
         b[i] = 0.5f + (float)(((uint32_t)i * 2654435761u) >> 22) * (1.0f / 1024.0f);
 }
 
+// Tile depth of the single-kernel iteration (0: the grid runs the two-kernel PCG).
+int nn_pcg_tile_depth(const nn_pcg* pc) { return pc->fast ? nn_cg_plan_tile_depth(pc->fast) : 0; }
+void nn_pcg_set_tile_depth(nn_pcg* pc, int zc)
+{
+    if (pc->fast && zc >= 4) nn_cg_plan_set_tile_depth(pc->fast, zc);
+}
+
 // Tile autotuner of the single-kernel iteration (nn_cg_plan_autotune) on
 // scratch vectors; NN_ERR_UNSUPPORTED when the grid runs the two-kernel PCG.
 nn_status nn_pcg_autotune_tiles(nn_pcg* pc, int iters, int* tile_z, float* ms_per_iter)

@@ -2241,21 +2241,25 @@ static nn_status ensure_graph(nn_sim* s)
 // network and state, keep the fastest, and restore the state the trials
 // changed (neuron fields, delay ring, spike counters and lists, bitmap,
 // deposits).  The step counter is restored too, so the trials leave no trace.
-extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, int* best_npt, float* best_ms)
+// Copy of every device buffer that steps of the simulation write (neuron
+// fields, delay ring, bitmap and row flags, spike lists and counters, step
+// counter, deposits, the field and its right-hand side, electrode samples),
+// for trials that must leave no trace.
+struct SimSnapshot {
+    struct Buf { void* dst; const void* src; size_t bytes; };
+    std::vector<Buf> keep;
+};
+
+static nn_status snapshot_take(nn_sim* s, SimSnapshot& snap)
 {
-    if (!s || trial_steps < 1) return NN_ERR_INVALID_ARG;
-    if (!s->row_ptr) return nn_fail(s->ctx, NN_ERR_INVALID_ARG, "nn_sim_autotune: no network set");
     nn_ctx* ctx = s->ctx;
     cudaStream_t cs = ctx->stream;
     const size_t NP = (size_t)s->n_pad;
-    // snapshot
-    struct Buf { void* dst; const void* src; size_t bytes; };
-    std::vector<Buf> keep;
     auto save = [&](const void* p, size_t bytes) -> nn_status {
         if (!p || !bytes) return NN_OK;
         unsigned char* d = nullptr;
         NN_TRY(nn_alloc(ctx, &d, bytes));
-        keep.push_back({d, p, bytes});
+        snap.keep.push_back({d, p, bytes});
         NN_CUDA(ctx, cudaMemcpyAsync(d, p, bytes, cudaMemcpyDeviceToDevice, cs));
         return NN_OK;
     };
@@ -2270,8 +2274,38 @@ extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, 
     if (st == NN_OK) st = save(s->total, sizeof(unsigned long long));
     if (st == NN_OK) st = save(s->rcount, sizeof(unsigned long long));
     if (st == NN_OK) st = save(s->src, has_field(s) ? (size_t)s->G * sizeof(float) : 0);
+    if (st == NN_OK) st = save(s->u, s->u ? (size_t)s->G * sizeof(float) : 0);
+    if (st == NN_OK) st = save(s->u_prev, s->u_prev ? (size_t)s->G * sizeof(float) : 0);
+    if (st == NN_OK) st = save(s->b, s->b ? (size_t)s->G * sizeof(float) : 0);
     if (st == NN_OK) st = save(s->el_val, (size_t)s->el_cap * s->el_members * sizeof(float));
     if (st == NN_OK) st = save(s->el_spk, (size_t)s->el_cap * s->el_members);
+    return st;
+}
+
+static nn_status snapshot_restore(nn_sim* s, const SimSnapshot& snap)
+{
+    for (const auto& b : snap.keep)
+        NN_CUDA(s->ctx, cudaMemcpyAsync((void*)b.src, b.dst, b.bytes, cudaMemcpyDeviceToDevice, s->ctx->stream));
+    return NN_OK;
+}
+
+static void snapshot_free(SimSnapshot& snap)
+{
+    for (const auto& b : snap.keep) cudaFree(b.dst);
+    snap.keep.clear();
+}
+
+extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, int* best_npt, float* best_ms)
+{
+    if (!s || trial_steps < 1) return NN_ERR_INVALID_ARG;
+    if (!s->row_ptr) return nn_fail(s->ctx, NN_ERR_INVALID_ARG, "nn_sim_autotune: no network set");
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    // a pending overlapped solve writes the field the snapshot holds
+    NN_TRY(finish_solve(s));
+    if (s->ev_solved) NN_CUDA(ctx, cudaStreamWaitEvent(cs, s->ev_solved, 0));
+    SimSnapshot snap;
+    nn_status st = snapshot_take(s, snap);
     const int old_tpb = s->tpb, old_npt = s->npt;
     const bool old_timing = s->timing;
     s->timing = false;
@@ -2286,10 +2320,7 @@ extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, 
             s->tpb = tpb;
             s->npt = npt;
             // restore, warm once, then time
-            for (const Buf& b : keep)
-                if (st == NN_OK)
-                    st = nn_cuda_check(ctx, cudaMemcpyAsync((void*)b.src, b.dst, b.bytes, cudaMemcpyDeviceToDevice, cs),
-                                       "restore");
+            if (st == NN_OK) st = snapshot_restore(s, snap);
             if (st == NN_OK) st = enqueue_step(s, 0, -1);
             if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e0, cs), "event");
             for (int q = 0; q < trial_steps && st == NN_OK; ++q) st = enqueue_step(s, 0, -1);
@@ -2305,12 +2336,9 @@ extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, 
             }
         }
     }
-    for (const Buf& b : keep) {
-        if (st == NN_OK)
-            st = nn_cuda_check(ctx, cudaMemcpyAsync((void*)b.src, b.dst, b.bytes, cudaMemcpyDeviceToDevice, cs), "restore");
-    }
+    if (st == NN_OK) st = snapshot_restore(s, snap);
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(cs), "nn_sim_autotune");
-    for (const Buf& b : keep) cudaFree(b.dst);
+    snapshot_free(snap);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     s->timing = old_timing;
@@ -2395,6 +2423,102 @@ extern "C" nn_status nn_sim_delivery_log(nn_sim* s, int8_t* h_modes, float* h_ra
     return NN_OK;
 }
 
+// Tile depth of the overlapped field solve, chosen by the time of whole
+// periods: the solve shares the GPU with the next period's neuron updates, so
+// the depth fastest alone (fewer, deeper tiles make more blocks) need not be
+// fastest beside them.  Each candidate runs six periods from the same
+// snapshot of the simulation (restored after each, and at the end, with the
+// step counters and the delivery bookkeeping).
+static nn_status autotune_overlapped_tiles(nn_sim* s, int* shape, float* ms_per_step)
+{
+    nn_ctx* ctx = s->ctx;
+    cudaStream_t cs = ctx->stream;
+    // fold the pending spike totals, so the automatic delivery's state is all on the host
+    NN_CUDA(ctx, cudaStreamSynchronize(cs));
+    while (s->tot_pending > 0) {
+        const int k = s->tot_head;
+        const unsigned long long tot = s->h_tot[k];
+        if (s->base_step >= 0 && s->tot_step[k] > s->base_step)
+            s->last_rate = (float)((double)(tot - s->base_tot) / ((double)(s->tot_step[k] - s->base_step) * s->n));
+        s->base_tot = tot;
+        s->base_step = s->tot_step[k];
+        s->tot_head = (k + 1) % nn_sim::TOT_Q;
+        --s->tot_pending;
+    }
+    SimSnapshot snap;
+    nn_status st = snapshot_take(s, snap);
+    const int64_t host_step = s->host_step;
+    const int cur_mode = s->cur_mode, tot_head = s->tot_head, iter_estimate = s->iter_estimate;
+    const float last_rate = s->last_rate;
+    const unsigned long long base_tot = s->base_tot;
+    const int64_t base_step = s->base_step;
+    const size_t nlog = s->mode_log.size();
+    const nn_solve_stats stats = s->stats;
+    const bool have_prev = s->have_prev;
+    auto restore_host = [&]() {
+        s->host_step = host_step;
+        s->cur_mode = cur_mode;
+        s->tot_head = tot_head;
+        s->tot_pending = 0;
+        s->last_rate = last_rate;
+        s->base_tot = base_tot;
+        s->base_step = base_step;
+        s->mode_log.resize(nlog);
+        s->rate_log.resize(nlog);
+        s->stats = stats;
+        s->iter_estimate = iter_estimate;
+        s->have_prev = have_prev;
+    };
+    const int P = period_steps(s);
+    const int zc0 = nn_pcg_tile_depth(s->pcg);
+    int best_zc = zc0;
+    float best = 1e30f;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&e0), "event");
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&e1), "event");
+    int nz = 0, d0 = 0, d1 = 0;
+    nn_ctx* c_ = nullptr;
+    const float* i_ = nullptr;
+    const float* D_ = nullptr;
+    float ic_ = 0.0f;
+    nn_pcg_info(s->pcg, &c_, &d0, &d1, &nz, &i_, &ic_, &D_);
+    int prev = 0;
+    for (int zc : {4, 6, 8, 12, 16, 24, 32}) {
+        if (st != NN_OK || prev >= nz) break;
+        prev = zc;
+        nn_pcg_set_tile_depth(s->pcg, zc);
+        if (st == NN_OK) st = snapshot_restore(s, snap);
+        restore_host();
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e0, cs), "event");
+        if (st == NN_OK) st = nn_sim_step(s, 6 * P);  // returns with its last solve finished
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e1, cs), "event");
+        float ms = 0.0f;
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventSynchronize(e1), "event");
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventElapsedTime(&ms, e0, e1), "event");
+        if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(cs), "sync");
+        // fold the trial's spike totals away before the next restore
+        while (s->tot_pending > 0) {
+            s->tot_head = (s->tot_head + 1) % nn_sim::TOT_Q;
+            --s->tot_pending;
+        }
+        if (st == NN_OK && ms < best) {
+            best = ms;
+            best_zc = zc;
+        }
+    }
+    nn_pcg_set_tile_depth(s->pcg, st == NN_OK ? best_zc : zc0);
+    const nn_status st2 = snapshot_restore(s, snap);
+    restore_host();
+    if (st == NN_OK) st = st2;
+    if (st == NN_OK) st = nn_cuda_check(ctx, cudaStreamSynchronize(cs), "autotune_overlapped_tiles");
+    snapshot_free(snap);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (shape) *shape = nn_pcg_tile_depth(s->pcg);
+    if (ms_per_step) *ms_per_step = best < 1e30f ? best / (6.0f * P) : 0.0f;
+    return st;
+}
+
 extern "C" nn_status nn_sim_autotune_solver(nn_sim* s, int trial_iters, int* shape, float* ms_per_iter)
 {
     if (!s || trial_iters < 1) return NN_ERR_INVALID_ARG;
@@ -2403,7 +2527,11 @@ extern "C" nn_status nn_sim_autotune_solver(nn_sim* s, int trial_iters, int* sha
     // a pending overlapped solve owns the solver's work vectors
     NN_TRY(finish_solve(s));
     if (s->ev_solved) NN_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, s->ev_solved, 0));
-    if (s->pcg) return nn_pcg_autotune_tiles(s->pcg, trial_iters, shape, ms_per_iter);
+    if (s->pcg) {
+        if (!s->row_ptr || !overlap_solve(s) || nn_pcg_tile_depth(s->pcg) == 0)
+            return nn_pcg_autotune_tiles(s->pcg, trial_iters, shape, ms_per_iter);
+        return autotune_overlapped_tiles(s, shape, ms_per_iter);
+    }
     float *b = nullptr, *x = nullptr;
     const int64_t G = s->G;
     NN_TRY(nn_alloc(ctx, &b, (size_t)G));
