@@ -739,7 +739,9 @@ def run_batch(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
                    "timesteps_per_step": P, "grid_cells": int(sim.field_cells()),
                    "weights": "U[0, w_b], w_b = 2 * 2.5 nS / (p_b * size_b) per instance",
                    "autotuned": {"threads_per_block": tpb, "neurons_per_thread": npt, "trial_ms_per_step": tune_ms,
-                                 "pcg_cells_per_block": cpb, "pcg_trial_ms_per_iteration": pcg_iter_ms},
+                                 "pcg_cells_per_block": cpb, "pcg_trial_ms_per_timestep": pcg_iter_ms,
+                                 "pcg_how": "each block size timed over six periods with the batched solve "
+                                            "overlapping the neuron updates, from a snapshot restored afterwards"},
                    "network_generation_s": t_gen, "l2": "inputs larger than L2"},
         "spikes_in_timed_region": spikes_b - spikes_a,
         "cg": {"instances": int(wl["n_inst"]), "iterations_last_solve_max": int(iters.max()),

@@ -305,7 +305,7 @@ NN_API nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, int*
  * of the 32 x 16 tiles of the one-kernel PCG iteration (4 .. 32;
  * NN_ERR_UNSUPPORTED when the grid runs the two-kernel PCG), for a batch the
  * batched PCG's cells per block.  When the solve overlaps the neuron updates
- * (par_overlap, no field feedback) each depth is timed over six whole periods
+ * (par_overlap, no field feedback) each shape is timed over six whole periods
  * from a snapshot of the simulation, which is restored afterwards;
  * *ms_per_iter then holds the time per timestep.  Otherwise the solver is
  * timed alone on scratch vectors and *ms_per_iter is its iteration time.

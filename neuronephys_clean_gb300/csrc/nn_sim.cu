@@ -2423,14 +2423,15 @@ extern "C" nn_status nn_sim_delivery_log(nn_sim* s, int8_t* h_modes, float* h_ra
     return NN_OK;
 }
 
-// Tile depth of the overlapped field solve, chosen by the time of whole
-// periods: the solve shares the GPU with the next period's neuron updates, so
-// the depth fastest alone (fewer, deeper tiles make more blocks) need not be
-// fastest beside them.  Each candidate runs six periods from the same
-// snapshot of the simulation (restored after each, and at the end, with the
-// step counters and the delivery bookkeeping).
+// Block shape of the overlapped field solve (a single grid's tile depth, a
+// batch's cells per block), chosen by the time of whole periods: the solve
+// shares the GPU with the next period's neuron updates, so the shape fastest
+// alone need not be fastest beside them.  Each candidate runs six periods
+// from the same snapshot of the simulation (restored after each, and at the
+// end, with the step counters and the delivery bookkeeping).
 static nn_status autotune_overlapped_tiles(nn_sim* s, int* shape, float* ms_per_step)
 {
+    const bool batch = s->bpcg != nullptr;
     nn_ctx* ctx = s->ctx;
     cudaStream_t cs = ctx->stream;
     // fold the pending spike totals, so the automatic delivery's state is all on the host
@@ -2470,23 +2471,37 @@ static nn_status autotune_overlapped_tiles(nn_sim* s, int* shape, float* ms_per_
         s->have_prev = have_prev;
     };
     const int P = period_steps(s);
-    const int zc0 = nn_pcg_tile_depth(s->pcg);
+    const int zc0 = batch ? nn_bpcg_cells_per_block(s->bpcg) : nn_pcg_tile_depth(s->pcg);
+    auto set_shape = [&](int v) -> nn_status {
+        if (batch) return nn_bpcg_set_cells_per_block(s->bpcg, v);
+        nn_pcg_set_tile_depth(s->pcg, v);
+        return NN_OK;
+    };
     int best_zc = zc0;
     float best = 1e30f;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&e0), "event");
     if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventCreate(&e1), "event");
-    int nz = 0, d0 = 0, d1 = 0;
-    nn_ctx* c_ = nullptr;
-    const float* i_ = nullptr;
-    const float* D_ = nullptr;
-    float ic_ = 0.0f;
-    nn_pcg_info(s->pcg, &c_, &d0, &d1, &nz, &i_, &ic_, &D_);
-    int prev = 0;
-    for (int zc : {4, 6, 8, 12, 16, 24, 32}) {
-        if (st != NN_OK || prev >= nz) break;
-        prev = zc;
-        nn_pcg_set_tile_depth(s->pcg, zc);
+    std::vector<int> cands;
+    if (batch) {
+        cands = {512, 1024, 2048, 4096};
+    } else {
+        int nz = 0, d0 = 0, d1 = 0;
+        nn_ctx* c_ = nullptr;
+        const float* i_ = nullptr;
+        const float* D_ = nullptr;
+        float ic_ = 0.0f;
+        nn_pcg_info(s->pcg, &c_, &d0, &d1, &nz, &i_, &ic_, &D_);
+        int prev = 0;
+        for (int zc : {4, 6, 8, 12, 16, 24, 32}) {
+            if (prev >= nz) break;  // deeper tiles than the grid change nothing
+            prev = zc;
+            cands.push_back(zc);
+        }
+    }
+    for (int zc : cands) {
+        if (st != NN_OK) break;
+        st = set_shape(zc);
         if (st == NN_OK) st = snapshot_restore(s, snap);
         restore_host();
         if (st == NN_OK) st = nn_cuda_check(ctx, cudaEventRecord(e0, cs), "event");
@@ -2506,7 +2521,8 @@ static nn_status autotune_overlapped_tiles(nn_sim* s, int* shape, float* ms_per_
             best_zc = zc;
         }
     }
-    nn_pcg_set_tile_depth(s->pcg, st == NN_OK ? best_zc : zc0);
+    const nn_status st3 = set_shape(st == NN_OK ? best_zc : zc0);
+    if (st == NN_OK) st = st3;
     const nn_status st2 = snapshot_restore(s, snap);
     restore_host();
     if (st == NN_OK) st = st2;
@@ -2514,7 +2530,7 @@ static nn_status autotune_overlapped_tiles(nn_sim* s, int* shape, float* ms_per_
     snapshot_free(snap);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    if (shape) *shape = nn_pcg_tile_depth(s->pcg);
+    if (shape) *shape = batch ? nn_bpcg_cells_per_block(s->bpcg) : nn_pcg_tile_depth(s->pcg);
     if (ms_per_step) *ms_per_step = best < 1e30f ? best / (6.0f * P) : 0.0f;
     return st;
 }
@@ -2532,6 +2548,7 @@ extern "C" nn_status nn_sim_autotune_solver(nn_sim* s, int trial_iters, int* sha
             return nn_pcg_autotune_tiles(s->pcg, trial_iters, shape, ms_per_iter);
         return autotune_overlapped_tiles(s, shape, ms_per_iter);
     }
+    if (s->row_ptr && overlap_solve(s)) return autotune_overlapped_tiles(s, shape, ms_per_iter);
     float *b = nullptr, *x = nullptr;
     const int64_t G = s->G;
     NN_TRY(nn_alloc(ctx, &b, (size_t)G));
