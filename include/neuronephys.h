@@ -572,7 +572,7 @@ NN_API nn_status nn_lmg_train(nn_lmg* lm, int steps, float lr, float* mean_loss)
 NN_API nn_status nn_lmg_use_network(nn_lmg* lm, int enable);
 /* Jacobi sweeps on the network's level after its correction (default 2). */
 NN_API nn_status nn_lmg_set_post_sweeps(nn_lmg* lm, int sweeps);
-/* Choose that number (2, 4, 8, 12 or 16) by timing, for each, solves of the
+/* Choose that number (2, 4, 8, 12, 16, 20 or 24) by timing, for each, solves of the
  * nb right-hand sides d_bs[k] (host array of device pointers) from zero to
  * rtol (d_x: scratch); the smallest total is kept, *best_ms. */
 NN_API nn_status nn_lmg_autotune_post_sweeps(nn_lmg* lm, const float* const* d_bs, int nb, float* d_x, double rtol,

@@ -810,7 +810,7 @@ class LearnedMultigrid:
         _check(lib().nn_lmg_set_post_sweeps(self.handle, sweeps), self.ctx, "nn_lmg_set_post_sweeps")
 
     def autotune_post_sweeps(self, rhs, rtol: float = 1e-6) -> tuple[int, float]:
-        """Pick the post-network sweeps (2 .. 16) by timing solves of the device
+        """Pick the post-network sweeps (2 .. 24) by timing solves of the device
         right-hand sides `rhs` (a list); returns (sweeps, total ms of its solves)."""
         x = self.ctx.empty((int(np.prod(rhs[0].shape)),), np.float32)
         ptrs = (C.c_void_p * len(rhs))(*[r.ptr for r in rhs])

@@ -1246,7 +1246,7 @@ extern "C" nn_status nn_lmg_autotune_post_sweeps(nn_lmg* lm, const float* const*
     int bsw = 2;
     float bms = 1e30f;
     nn_status st = NN_OK;
-    for (int sw : {2, 4, 8, 12, 16}) {
+    for (int sw : {2, 4, 8, 12, 16, 20, 24}) {
         if (st != NN_OK) break;
         st = nn_mg_set_level_sweeps(lm->mg, sw);
         int it = 0;

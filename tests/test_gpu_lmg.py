@@ -69,7 +69,7 @@ def test_learned_coarse_solver(ctx, orc):
     # Jacobi sweeps after the network's correction, chosen by time: the
     # solve keeps its tolerance and its FP64 agreement
     sw, ms = lm.autotune_post_sweeps([ctx.to_device(sources(shape, np.random.default_rng(100 + j))) for j in range(2)])
-    assert sw in (2, 4, 8, 12, 16) and ms > 0
+    assert sw in (2, 4, 8, 12, 16, 20, 24) and ms > 0
     dx.zero()
     it_tuned, rel = lm.solve(db, dx)
     assert rel <= 1e-6 and it_tuned <= it_trained + 1

@@ -381,6 +381,14 @@ def test_deliver_spike_list(ctx):
     sp.generate_network(spec)
     sp.deliver_spikes(ctx.to_device(lst), len(lst), 1)
     ctx.synchronize()
+    # the pull wrote the complete input of the next step into ring slot 1:
+    # the same sums; the gather alone, rerun from the same bitmap, rewrites it
+    # bit for bit (fixed-point sums)
+    ring = sp.get_ring()
+    np.testing.assert_allclose(ring[1, :, 0], ge, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(ring[1, :, 1], gi, rtol=1e-5, atol=1e-6)
+    sp.pull_gather()
+    assert np.array_equal(sp.get_ring(), ring)
 
 
 def test_overlapped_field_solve_matches_serial(ctx):
