@@ -68,6 +68,8 @@ struct ConvArgs {
     int* err;
     int stages;  // (dz, dy) stages in flight, 2 .. ConvCfg::STAGES_BIG
     const double* y32_scale;
+    uint4* up;        // (nullable) the result also written, nearest-upsampled, into this finer activation
+    nn_act_geom gu;   // its geometry (twice the sides)
 };
 
 __device__ __forceinline__ unsigned char* align128(unsigned char* p)
@@ -212,7 +214,17 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3(ConvArgs a)
                 if (a.mask && !(mk[i] > 0.0f)) q = 0.0f;
                 t[i] = in ? q : 0.0f;
             }
-            a.y[gb * a.g.S + a.g.GD + o] = pack_bf16x8(t);
+            const uint4 pk = pack_bf16x8(t);
+            a.y[gb * a.g.S + a.g.GD + o] = pk;
+            if (a.up && in) {
+                // the eight children of interior voxel (z, y, x) (1-based) in the finer grid
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const int64_t fz = 2 * (z - 1) + (c >> 2) + 1, fy = 2 * (y - 1) + ((c >> 1) & 1) + 1,
+                                  fx = 2 * (x - 1) + (c & 1) + 1;
+                    a.up[gb * a.gu.S + a.gu.GD + fz * a.gu.P + fy * a.gu.R + fx] = pk;
+                }
+            }
             if (gb == 0 && a.y32 && in)
                 a.y32[((int64_t)(z - 1) * a.g.ny + (y - 1)) * a.g.nx + (x - 1)] =
                     a.y32_scale ? t[0] * (float)a.y32_scale[0] : t[0];
@@ -534,10 +546,12 @@ size_t nn_conv_packed_weight_bytes(int cin, int cout) { return (size_t)27 * cin 
 
 nn_status nn_conv_forward(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, const void* x, const void* wpacked,
                           const float* bias, int relu, const void* mask, void* y, float* y32, int* err,
-                          const double* y32_scale)
+                          const double* y32_scale, void* up, const nn_act_geom* gup)
 {
     ConvArgs a;
     a.y32_scale = y32_scale;
+    a.up = (uint4*)up;
+    if (up && gup) a.gu = *gup;
     a.x = (const uint4*)x;
     a.w = (const unsigned char*)wpacked;
     a.bias = bias;

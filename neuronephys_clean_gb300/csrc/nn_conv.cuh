@@ -45,11 +45,14 @@ size_t nn_conv_packed_weight_bytes(int cin, int cout);
 
 // y = act(conv(x) + bias) [* (mask > 0)], BF16 in and out, on ctx's stream.
 // y32 (nullable): channel 0 of the result also written as a dense FP32 grid,
-// times (float)*y32_scale when y32_scale (device) is given.  Launched as a
-// programmatic dependent of the kernel before it (nn_launch_pdl).
+// times (float)*y32_scale when y32_scale (device) is given.  up (nullable):
+// the result also written, nearest-upsampled (each voxel to its eight
+// children), into the first COUT/8 channel blocks of the activation up of
+// geometry *gup (twice the sides).  Launched as a programmatic dependent of
+// the kernel before it (nn_launch_pdl).
 nn_status nn_conv_forward(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, const void* x, const void* wpacked,
                           const float* bias, int relu, const void* mask, void* y, float* y32, int* err,
-                          const double* y32_scale = nullptr);
+                          const double* y32_scale = nullptr, void* up = nullptr, const nn_act_geom* gup = nullptr);
 // dw[27][cin][cout] += sum over voxels of x(o + tap) gy(o); db[cout] += sum gy.
 // err (device int) is set when a pipeline wait gives up.
 nn_status nn_conv_wgrad(nn_ctx* ctx, const nn_act_geom& g, int cin, int cout, const void* x, const void* gy,

@@ -98,21 +98,7 @@ __global__ void k_pool(const uint4* src, nn_act_geom gf, const uint4* dummy, uin
     (void)dummy;
 }
 
-// fine(c) = coarse(parent)            (nearest upsampling)
-__global__ void k_up(const uint4* src, nn_act_geom gc, uint4* dst, nn_act_geom gf, int groups)
-{
-    nn_grid_dep_wait();
-    const int64_t G = (int64_t)gf.nz * gf.ny * gf.nx;
-    GRID_LOOP(e, G * groups)
-    {
-        const int gb = (int)(e / G);
-        const int64_t c = e - gb * G;
-        const int x = (int)(c % gf.nx), y = (int)((c / gf.nx) % gf.ny), z = (int)(c / ((int64_t)gf.nx * gf.ny));
-        dst[gb * gf.S + gf.GD + vox(gf, z, y, x)] = src[gb * gc.S + gc.GD + vox(gc, z >> 1, y >> 1, x >> 1)];
-    }
-}
-
-// coarse(c) = sum of its 8 children   (adjoint of k_up)
+// coarse(c) = sum of its 8 children   (adjoint of the nearest upsampling)
 __global__ void k_sumpool(const uint4* src, nn_act_geom gf, uint4* dst, nn_act_geom gc, int groups)
 {
     const int64_t G = (int64_t)gc.nz * gc.ny * gc.nx;
@@ -557,10 +543,12 @@ nn_status nn_unet_make(nn_ctx* ctx, int nz, int ny, int nx, uint64_t seed, nn_un
 }
 
 static nn_status conv(nn_unet* u, int l, const void* x, void* y, bool relu, const void* mask = nullptr,
-                      float* y32 = nullptr, const double* y32_scale = nullptr)
+                      float* y32 = nullptr, const double* y32_scale = nullptr, void* up = nullptr)
 {
+    // up: the output also upsampled into the next finer level's activation
+    const nn_act_geom* gup = up ? &u->g[LLEVEL[l] - 1] : nullptr;
     return nn_conv_forward(u->ctx, u->g[LLEVEL[l]], LCIN[l], LCOUT[l], x, u->L[l].wp, u->L[l].b, relu ? 1 : 0, mask,
-                           y, y32, u->err, y32_scale);
+                           y, y32, u->err, y32_scale, up, gup);
 }
 
 // input gradient of layer l (adjoint weights), masked by `mask` (> 0) if given
@@ -616,11 +604,9 @@ static nn_status unet_forward(nn_unet* u, const float* rc, const float* logd, co
     NN_TRY(conv(u, L_E1B, u->E1a, SK1, true));
     NN_TRY(launch_pdl(ctx, G2 * 4, "k_pool", k_pool, (const uint4*)SK1, g1, (const uint4*)nullptr, (uint4*)u->P2, g2, 4));
     NN_TRY(conv(u, L_B2A, u->P2, u->B2a, true));
-    NN_TRY(conv(u, L_B2B, u->B2a, u->B2b, true));
-    NN_TRY(launch_pdl(ctx, G1 * 8, "k_up", k_up, (const uint4*)u->B2b, g2, (uint4*)u->CAT1, g1, 8));
+    NN_TRY(conv(u, L_B2B, u->B2a, u->B2b, true, nullptr, nullptr, nullptr, u->CAT1));  // + upsampled into CAT1
     NN_TRY(conv(u, L_D1A, u->CAT1, u->D1a, true));
-    NN_TRY(conv(u, L_D1B, u->D1a, u->D1b, true));
-    NN_TRY(launch_pdl(ctx, u->G0 * 4, "k_up", k_up, (const uint4*)u->D1b, g1, (uint4*)u->CAT0, g0, 4));
+    NN_TRY(conv(u, L_D1B, u->D1a, u->D1b, true, nullptr, nullptr, nullptr, u->CAT0));  // + upsampled into CAT0
     NN_TRY(conv(u, L_D0A, u->CAT0, u->D0a, true));
     NN_TRY(conv(u, L_D0B, u->D0a, u->D0b, true));
     NN_TRY(conv(u, L_OUT, u->D0b, u->OUT, false, nullptr, out ? out : u->y32, out ? (const double*)u->scal : nullptr));
