@@ -404,7 +404,7 @@ def c5_leg(nn, ctx, args) -> dict:
     """The workload's third metric, CG time to a 1e-6 relative residual, on
     the configuration-5 system (256^3 cells, lognormal D with sigma 1 and an
     8-cell correlation length, uptake 0.1), in the default line:
-    * plain Jacobi-PCG (the judge), the classical multigrid FCG, and the
+    * plain Jacobi-PCG (the baseline), the classical multigrid FCG, and the
       multigrid whose 32^3 level is solved by the learned U-Net (trained here
       on the GPU, on the coarse problems of six training right-hand sides);
     * each timed on the bench right-hand side and on four held-out ones
