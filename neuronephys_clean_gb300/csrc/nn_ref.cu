@@ -283,6 +283,93 @@ __global__ void __launch_bounds__(CMP_THREADS) k_cmp_write(const float* out, int
         if (f[q]) list[pos++] = base + q;
 }
 
+// Threshold count of each tile, with the tile's inputs zeroed (the first of
+// the two launches of nn_coupling_run).
+__global__ void __launch_bounds__(CMP_THREADS) k_cmp_count_zero(const float* out, int n, int64_t* block_counts,
+                                                                float* inputs)
+{
+    const int base = blockIdx.x * CMP_TILE + threadIdx.x * CMP_ITEMS;
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < CMP_ITEMS; ++q)
+        if (base + q < n) {
+            c += fires(out[base + q]);
+            inputs[base + q] = 0.0f;
+        }
+    __shared__ int tot;
+    if (threadIdx.x == 0) tot = 0;
+    __syncthreads();
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&tot, c);
+    __syncthreads();
+    if (threadIdx.x == 0) block_counts[blockIdx.x] = tot;
+}
+
+// The second launch: each tile's offset in the ascending firing list (the sum
+// of the earlier tiles' counts), its entries written, the total stored by the
+// last tile, and the tile's firing neurons scattered (signal_spikes_kernel),
+// a warp per firing neuron with four targets per lane loaded before their
+// reductions.
+__global__ void __launch_bounds__(CMP_THREADS) k_cmp_write_push(const float* out, int n, const int64_t* block_counts,
+                                                                int nblocks, int* list, int* count,
+                                                                const int* indices, const int* offsets, float* inputs,
+                                                                int signal_mode)
+{
+    __shared__ int64_t red[CMP_THREADS / 32];
+    __shared__ int s_list[CMP_TILE];
+    __shared__ int s_n;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t acc = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += CMP_THREADS) acc += block_counts[b];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) red[w] = acc;
+    __syncthreads();
+    int64_t boff = 0;
+    for (int q = 0; q < CMP_THREADS / 32; ++q) boff += red[q];
+    if (blockIdx.x == nblocks - 1 && threadIdx.x == 0) *count = (int)(boff + block_counts[blockIdx.x]);
+    const int base = blockIdx.x * CMP_TILE + threadIdx.x * CMP_ITEMS;
+    int f[CMP_ITEMS];
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < CMP_ITEMS; ++q) {
+        f[q] = base + q < n ? fires(out[base + q]) : 0;
+        c += f[q];
+    }
+    __shared__ int wt[CMP_THREADS / 32];
+    int inc = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wt[w] = inc;
+    __syncthreads();
+    int wbase = 0;
+    for (int q = 0; q < w; ++q) wbase += wt[q];
+    int pos = wbase + inc - c;
+#pragma unroll
+    for (int q = 0; q < CMP_ITEMS; ++q)
+        if (f[q]) {
+            list[boff + pos] = base + q;
+            s_list[pos++] = base + q;
+        }
+    if (threadIdx.x == CMP_THREADS - 1) s_n = wbase + inc;
+    __syncthreads();
+    const int nf = s_n;
+    for (int k = w; k < nf; k += CMP_THREADS / 32) {
+        const int pre = s_list[k];
+        const float sig = signal_mode ? out[pre] : 1.0f;
+        const int beg = offsets[pre], end = offsets[pre + 1];
+        for (int e0 = beg + lane; e0 < end; e0 += 128) {
+            int post[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) post[u] = e0 + 32 * u < end ? indices[e0 + 32 * u] : -1;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if ((unsigned)post[u] < (unsigned)n) atomicAdd(inputs + post[u], sig);
+        }
+    }
+}
+
 // signal_spikes_kernel (src/coupling.cu:34-48; src_wholebrain/coupling.cu:12-33),
 // a warp per firing presynaptic neuron with the lanes over its targets.
 __global__ void __launch_bounds__(256) k_push_ref(const int* list, const int* count, const int* indices,
@@ -370,10 +457,14 @@ extern "C" nn_status nn_coupling_run(nn_coupling* c, const int* d_indices, const
     if (!c || !d_offsets || !d_inputs || !d_outputs) return nn_fail(c ? c->ctx : nullptr, NN_ERR_INVALID_ARG, "nn_coupling_run: bad argument");
     if (c->n == 0) { if (num_firing) *num_firing = 0; return NN_OK; }
     nn_ctx* ctx = c->ctx;
-    NN_TRY(coupling_compact(c, d_inputs, d_outputs));
-    k_push_ref<<<nn_grid_for(ctx, (int64_t)c->n * 32, 256, 4), 256, 0, ctx->stream>>>(
-        c->firing, c->count, d_indices, d_offsets, d_inputs, d_outputs, signal_mode, c->n, 0);
-    NN_CHECK_LAUNCH(ctx, "k_push_ref");
+    // two launches: threshold counts with the inputs zeroed, then the ordered
+    // list, the count and the scatter
+    k_cmp_count_zero<<<c->nblocks, CMP_THREADS, 0, ctx->stream>>>(d_outputs, c->n, c->block_counts, d_inputs);
+    NN_CHECK_LAUNCH(ctx, "k_cmp_count_zero");
+    k_cmp_write_push<<<c->nblocks, CMP_THREADS, 0, ctx->stream>>>(d_outputs, c->n, c->block_counts, c->nblocks,
+                                                                  c->firing, c->count, d_indices, d_offsets, d_inputs,
+                                                                  signal_mode);
+    NN_CHECK_LAUNCH(ctx, "k_cmp_write_push");
     return coupling_readback(c, num_firing);
 }
 
