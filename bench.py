@@ -458,7 +458,8 @@ def c5_leg(nn, ctx, args) -> dict:
     # Jacobi sweeps after the network's correction, chosen by timing a solve
     # of one training right-hand side
     post_sweeps, _ = lm.autotune_post_sweeps(
-        [ctx.to_device(fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=2000 + j)) for j in range(4)])
+        [ctx.to_device(fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=2000 + j))
+         for j in range(wl["train_rhs"])])
     learned = lambda rb, x: lm.solve(rb, x, 1e-6)  # noqa: E731
     ms, it, rel = timed(learned, bench_rhs)
     sols["learned_multigrid"] = dx.numpy().astype(np.float64)
@@ -901,7 +902,7 @@ def learned_multigrid_cg(nn, ctx, pc, wl, shape, G, db, plain_ms, plain_iters, a
     t0 = time.perf_counter()
     loss = lm.train(wl["lmg_train_steps"], 1e-3)
     t_train = time.perf_counter() - t0
-    post_sweeps, _ = lm.autotune_post_sweeps([ctx.to_device(r) for r in rhs[:4]])
+    post_sweeps, _ = lm.autotune_post_sweeps([ctx.to_device(r) for r in rhs])
     dx = ctx.empty((G,), np.float32)
 
     def timed(solve):
