@@ -248,7 +248,6 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg_iter(const __grid_constant
     using L = Layout<HET>;
     constexpr int STAGE_BYTES = L::STAGE_BYTES;
     constexpr int PX_OFF = L::NARR * PLANE_STRIDE;  // p, x boxes after the halo planes
-    if (a.flags[0]) return;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
     unsigned char* stage_base = smem;
@@ -265,7 +264,6 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg_iter(const __grid_constant
     const int x0 = tx * TX, y0 = ty * TY, z0 = tz * a.zc;
     const int z1 = min(z0 + a.zc, a.nz);
     const int np = z1 - z0 + 2;  // planes z0-1 .. z1
-    const float alpha = (float)a.scal[C_ALPHA], beta = (float)a.scal[C_BETA];
     const int sy = a.nx, sz = a.nx * a.ny;  // grids below 2^31 cells (plan check)
 
     if (tid == 0) {
@@ -274,6 +272,11 @@ __global__ void __launch_bounds__(CG_THREADS, 4) k_cg_iter(const __grid_constant
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    // launched as a programmatic dependent of the previous iteration (in a
+    // synchronous solve): its scalars, flags and vectors are complete only now
+    nn_grid_dep_wait();
+    if (a.flags[0]) return;
+    const float alpha = (float)a.scal[C_ALPHA], beta = (float)a.scal[C_BETA];
     // plane j (z = z0 - 1 + j) into stage j % STAGES: r, w, s with halo, and
     // for owned planes p, x of the tile
     auto issue = [&](int j) {
@@ -682,13 +685,28 @@ static nn_status enqueue_init(nn_cg_plan* pl, const float* d_b, float* d_x, doub
 }
 
 // iterations it0 .. it0 + n - 1 (each a no-op once the device flag is set)
+// pdl: each iteration a programmatic dependent of the kernel before it
+// (synchronous solves; an overlapped solve's waiting blocks would hold SM
+// room the neuron updates use)
 static nn_status enqueue_iters(nn_cg_plan* pl, float* d_x, const CUtensorMap& map_x, double rtol, int max_iter, int it0,
-                               int n, cudaStream_t cs)
+                               int n, cudaStream_t cs, bool pdl = false)
 {
     nn_ctx* ctx = pl->ctx;
     for (int it = it0; it < it0 + n; ++it) {
         const int pin = it & 1, pout = pin ^ 1;
         CgArgs a = cg_args(pl, d_x, rtol, max_iter, pout);
+        if (pdl) {
+            if (pl->D)
+                NN_CUDA(ctx, nn_launch_pdl(k_cg_iter<true>, dim3(pl->tiles), dim3(CG_THREADS),
+                                           (size_t)Layout<true>::SMEM_BYTES, cs, pl->map_r[pin], pl->map_w[pin],
+                                           pl->map_s[pin], pl->map_d, pl->map_m, pl->map_p, map_x, a));
+            else
+                NN_CUDA(ctx, nn_launch_pdl(k_cg_iter<false>, dim3(pl->tiles), dim3(CG_THREADS),
+                                           (size_t)Layout<false>::SMEM_BYTES, cs, pl->map_r[pin], pl->map_w[pin],
+                                           pl->map_s[pin], pl->map_p, pl->map_p, pl->map_p, map_x, a));
+            ctx->launches++;
+            continue;
+        }
         if (pl->D)
             k_cg_iter<true><<<pl->tiles, CG_THREADS, Layout<true>::SMEM_BYTES, cs>>>(
                 pl->map_r[pin], pl->map_w[pin], pl->map_s[pin], pl->map_d, pl->map_m, pl->map_p, map_x, a);
@@ -803,7 +821,7 @@ nn_status nn_cg_run(nn_cg_plan* pl, const float* d_b, float* d_x, double rtol, i
             NN_CUDA(ctx, cudaEventRecord(pl->ev_a[nchunks], cs));
         }
         const int n = std::min(chunk, max_iter - it);
-        NN_TRY(enqueue_iters(pl, d_x, map_x, rtol, max_iter, it, n, cs));
+        NN_TRY(enqueue_iters(pl, d_x, map_x, rtol, max_iter, it, n, cs, true));
         it += n;
         if (pl->timing) NN_CUDA(ctx, cudaEventRecord(pl->ev_b[nchunks], cs));
         ++nchunks;
