@@ -2355,18 +2355,15 @@ extern "C" nn_status nn_sim_autotune(nn_sim* s, int trial_steps, int* best_tpb, 
 // pinned memory behind an event; the periods whose events have completed
 // give the measured rate (spikes per neuron and step), without waiting for
 // the device unless TOT_Q periods are outstanding.
-static nn_status record_total(nn_sim* s)
+// Fold the completed spike-total measurements into the measured rate, oldest
+// first (all of them once the stream is synchronised).
+static nn_status fold_totals(nn_sim* s)
 {
-    nn_ctx* ctx = s->ctx;
-    if (s->tot_pending == nn_sim::TOT_Q) {
-        NN_CUDA(ctx, cudaEventSynchronize(s->ev_tot[s->tot_head]));
-    }
-    // fold completed measurements
     while (s->tot_pending > 0) {
         const int k = s->tot_head;
         const cudaError_t q = cudaEventQuery(s->ev_tot[k]);
         if (q == cudaErrorNotReady) break;
-        NN_CUDA(ctx, q);
+        NN_CUDA(s->ctx, q);
         const unsigned long long tot = s->h_tot[k];
         if (s->base_step >= 0 && s->tot_step[k] > s->base_step)
             s->last_rate = (float)((double)(tot - s->base_tot) / ((double)(s->tot_step[k] - s->base_step) * s->n));
@@ -2375,6 +2372,16 @@ static nn_status record_total(nn_sim* s)
         s->tot_head = (k + 1) % nn_sim::TOT_Q;
         --s->tot_pending;
     }
+    return NN_OK;
+}
+
+static nn_status record_total(nn_sim* s)
+{
+    nn_ctx* ctx = s->ctx;
+    if (s->tot_pending == nn_sim::TOT_Q) {
+        NN_CUDA(ctx, cudaEventSynchronize(s->ev_tot[s->tot_head]));
+    }
+    NN_TRY(fold_totals(s));
     const int k = (s->tot_head + s->tot_pending) % nn_sim::TOT_Q;
     NN_CUDA(ctx, cudaMemcpyAsync(&s->h_tot[k], s->total, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                  ctx->stream));
@@ -2436,16 +2443,7 @@ static nn_status autotune_overlapped_tiles(nn_sim* s, int* shape, float* ms_per_
     cudaStream_t cs = ctx->stream;
     // fold the pending spike totals, so the automatic delivery's state is all on the host
     NN_CUDA(ctx, cudaStreamSynchronize(cs));
-    while (s->tot_pending > 0) {
-        const int k = s->tot_head;
-        const unsigned long long tot = s->h_tot[k];
-        if (s->base_step >= 0 && s->tot_step[k] > s->base_step)
-            s->last_rate = (float)((double)(tot - s->base_tot) / ((double)(s->tot_step[k] - s->base_step) * s->n));
-        s->base_tot = tot;
-        s->base_step = s->tot_step[k];
-        s->tot_head = (k + 1) % nn_sim::TOT_Q;
-        --s->tot_pending;
-    }
+    NN_TRY(fold_totals(s));
     SimSnapshot snap;
     nn_status st = snapshot_take(s, snap);
     const int64_t host_step = s->host_step;
