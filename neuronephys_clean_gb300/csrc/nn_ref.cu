@@ -40,19 +40,20 @@ struct LFVars { float* v[NN_HH_NUM_VARS]; };
 // (Float = float, src/defines.cuh:50-55).  The expressions keep the
 // reference's operand order, so each rounds as the reference's does.  The
 // removable singularities of alpha_m (V = -35) and alpha_n (V = -50), 0/0 in
-// the reference, take their limits (1 and 0.1) when the FP64 argument is
-// within 1e-9 of them, which no other input changes.
+// the reference, take their limits (1 and 0.1) there.  V = -35 and V = -50
+// are the only float inputs whose FP64 argument 3.5 + 0.1 V (or -5 - 0.1 V)
+// lies within 1e-9 of zero, fused or not (the neighbouring floats give
+// 3.8e-7), so the test is an FP32 compare, off the FP64 pipe that bounds
+// this kernel.
 __device__ __forceinline__ float lf_rate_am(float V)
 {
-    const double u = 3.5 + 0.1 * V;
-    if (fabs(u) < 1e-9) return 1.0f;
+    if (V == -35.0f) return 1.0f;
     return (float)((3.5 + 0.1 * V) / (1 - exp(-3.5 - 0.1 * V)));
 }
 
 __device__ __forceinline__ float lf_rate_an(float V)
 {
-    const double u = -5 - 0.1 * V;
-    if (fabs(u) < 1e-9) return 0.1f;
+    if (V == -50.0f) return 0.1f;
     return (float)((-0.5 - 0.01 * V) / (exp(-5 - 0.1 * V) - 1));
 }
 
