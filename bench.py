@@ -201,9 +201,10 @@ class ClockSampler:
 
 # --------------------------------------------------------------- our arm ---
 
-def build_sim(nn, ctx, wl: dict, seed: int = 1, delivery: int = 0, raster: int = 0):
+def build_sim(nn, ctx, wl: dict, seed: int = 1, delivery: int = 0, raster: int = 0, tpb: int = 0, npt: int = 0):
     c = nn.default_config(wl["n"])
     c.delivery = delivery
+    c.threads_per_block, c.neurons_per_thread = tpb, npt
     c.seed = seed
     c.max_delay = max(1, wl["dmax"])
     c.grid = wl["grid"]
@@ -646,6 +647,49 @@ def run_delivery_sweep(args, wl: dict, rank: int, local_rank: int) -> dict | Non
             if sliced else "k_deliver_pull (warp per column; bytes: the 9-byte CSC entry per synapse)",
             "sweep": rows,
             "push_pull_crossover_fraction": cross}
+
+
+def run_launch_shapes(args, wl: dict, rank: int, local_rank: int) -> dict | None:
+    """The neuron update's launch shapes on the workload: for every
+    (neurons per thread, threads per block) the autotuner considers, a
+    simulation from the same seed (the shapes give bit-identical neurons, so
+    every one follows the same trajectory) settles, warms up and times
+    args.steps bench steps with CUDA events, field solve included; one more
+    bench step with kernel timing gives the median neuron-update launch.
+    Four neurons per thread load the state as 128-bit float4 vectors, two as
+    float2, one as float."""
+    if rank != 0:
+        return None
+    import neuronephys_clean_gb300 as nn
+    ctx = nn.Context(local_rank)
+    P, n = wl["total_steps"], wl["n"]
+    rows = []
+    for npt in (1, 2, 4):
+        for tpb in (64, 128, 256):
+            sim = build_sim(nn, ctx, wl, delivery=DELIVERY_MODES[args.delivery], tpb=tpb, npt=npt)
+            sim.step(args.settle)
+            for _ in range(args.warmup):
+                sim.step(P)
+            ctx.time_begin()
+            for _ in range(args.steps):
+                sim.step(P)
+            ms = ctx.time_end()
+            sim.set_kernel_timing(True)
+            sim.step(P)
+            kt = sim.kernel_times()
+            sim.set_kernel_timing(False)
+            rows.append({"neurons_per_thread": npt, "threads_per_block": tpb,
+                         "load": {1: "float", 2: "float2", 4: "float4"}[npt],
+                         "ms_per_timestep": ms / (args.steps * P),
+                         "neuron_steps_per_s": n * P * args.steps / (ms * 1e-3),
+                         "k_hh_step_median_us": kt.hh_step_median_ms * 1e3})
+            sim.close()
+    ctx.close()
+    best = min(rows, key=lambda r: r["ms_per_timestep"])
+    return {"metric": "neuron-steps/s by neuron-update launch shape", "workload": wl["workload"], "neurons": n,
+            "steps": args.steps, "warmup": args.warmup, "timesteps_per_step": P, "shapes": rows,
+            "fastest": {"neurons_per_thread": best["neurons_per_thread"],
+                        "threads_per_block": best["threads_per_block"]}}
 
 
 def batch_layout(wl: dict, seed: int = 4):
@@ -1239,6 +1283,9 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--delivery-sweep", action="store_true",
                     help="time push / pull spike delivery alone over firing fractions (one JSON line)")
+    ap.add_argument("--launch-shapes", action="store_true",
+                    help="time the workload at every neuron-update launch shape (neurons per thread x threads "
+                         "per block; one JSON line)")
     ap.add_argument("--reference-kernels", action="store_true",
                     help="time the reference-semantics leapfrog and count coupling at 1M neurons: the reference's "
                          "own kernels with --impl reference, the library's drop-ins otherwise (one JSON line)")
@@ -1286,6 +1333,8 @@ def main() -> None:
         line = run_our_reference_kernels(args, rank, local_rank)
     elif args.delivery_sweep:
         line = run_delivery_sweep(args, wl, rank, local_rank)
+    elif args.launch_shapes:
+        line = run_launch_shapes(args, wl, rank, local_rank)
     else:
         runner = {"cg": run_cg, "batch": run_batch}.get(wl.get("kind"), run_ours)
         line = runner(args, wl, dist, rank, local_rank)
