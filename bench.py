@@ -962,20 +962,55 @@ def learned_multigrid_cg(nn, ctx, pc, wl, shape, G, db, plain_ms, plain_iters, a
             its.append(it)
         return statistics.mean(times), statistics.mean(its), rel
 
+    # held-out right-hand sides (seeds disjoint from the training ones)
+    test = [ctx.to_device(fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=5000 + j))
+            for j in range(args.c5_test_rhs)]
+
+    def test_set(solve) -> dict:
+        ms_t, its = [], []
+        for h in test:
+            dx.zero()
+            ctx.time_begin()
+            it_h, _ = solve(h, dx)
+            ms_t.append(ctx.time_end())
+            its.append(it_h)
+        return {"right_hand_sides": len(test), "iterations_mean": statistics.mean(its),
+                "iterations_max": max(its), "ms_mean": statistics.mean(ms_t)}
+
     ms, it, rel = timed(lambda b, x: lm.solve(b, x, 1e-6))
+    test_learned = test_set(lambda b, x: lm.solve(b, x, 1e-6)) if test else None
     lm.use_network(False)
     ms_c, it_c, _ = timed(lambda b, x: lm.solve(b, x, 1e-6))
+    test_classical = test_set(lambda b, x: lm.solve(b, x, 1e-6)) if test else None
     lm.close()
+    # the same training with four times the right-hand sides (pairs), judged
+    # on the same held-out set
+    more = None
+    if test and args.c5_more_training:
+        lm4 = nn.LearnedMultigrid(pc, level=level, seed=7)
+        rhs4 = [fields.spike_sources(shape, wl["neurons"], wl["rate"], seed=2000 + j)
+                for j in range(4 * wl["train_rhs"])]
+        pairs4 = lm4.add_solves(rhs4)
+        loss4 = lm4.train(wl["lmg_train_steps"], 1e-3)
+        sweeps4, _ = lm4.autotune_post_sweeps([ctx.to_device(r) for r in rhs4])
+        dx.zero()
+        lm4.solve(db, dx, 1e-6)  # warm (graph capture)
+        more = {"right_hand_sides": len(rhs4), "pairs": pairs4, "final_loss": loss4, "post_sweeps": sweeps4,
+                "held_out": test_set(lambda b, x: lm4.solve(b, x, 1e-6))}
+        lm4.close()
+    test.clear()
     cut = nn.MultigridPCG(pc, level + 1)
     ms_t, it_t, _ = timed(lambda b, x: cut.solve(b, x, 1e-6))
     cut.close()
     return {"ms_to_tol": ms, "iterations": it, "relres": rel, "vs_plain_time": ms / plain_ms,
             "vs_plain_iterations": it / plain_iters, "network_level_grid": shape[0] >> level,
             "post_sweeps": post_sweeps,
-            "classical_hierarchy": {"ms_to_tol": ms_c, "iterations": it_c},
+            "held_out": test_learned,
+            "classical_hierarchy": {"ms_to_tol": ms_c, "iterations": it_c, "held_out": test_classical},
             "cut_at_network_level": {"ms_to_tol": ms_t, "iterations": it_t},
-            "training": {"pairs": pairs, "pair_generation_s": t_pairs, "adam_steps": wl["lmg_train_steps"],
-                         "train_s": t_train, "final_loss": loss}}
+            "training": {"right_hand_sides": len(rhs), "pairs": pairs, "pair_generation_s": t_pairs,
+                         "adam_steps": wl["lmg_train_steps"], "train_s": t_train, "final_loss": loss},
+            "four_times_the_training_pairs": more}
 
 
 def learned_cg(nn, ctx, pc, wl, shape, db, plain_ms, plain_iters, args) -> dict:
@@ -1299,6 +1334,10 @@ def main() -> None:
                     help="default workload: skip the batched-networks leg")
     ap.add_argument("--no-c5", dest="c5", action="store_false",
                     help="default workload: skip the 256^3 CG time-to-tolerance leg")
+    ap.add_argument("--c5-test-rhs", type=int, default=64,
+                    help="CG workload: held-out right-hand sides the learned and classical multigrid solve")
+    ap.add_argument("--no-c5-more-training", dest="c5_more_training", action="store_false",
+                    help="CG workload: skip the learned multigrid trained on four times the pairs")
     ap.add_argument("--no-learned", dest="learned", action="store_false",
                     help="CG workload: skip the learned-preconditioner comparison")
     args = ap.parse_args()
