@@ -295,6 +295,14 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
     sim.step(P)
     kt = sim.kernel_times()
     sim.set_kernel_timing(False)
+    # the delivery slot between the second and third event of each step holds
+    # the pull gather in pull periods; in push periods it is empty (the
+    # scatter runs inside k_hh_step) and its time is the events' own interval
+    if args.delivery == "auto":
+        modes_t, _ = sim.delivery_log(reset=True)
+        any_pull = bool((modes_t == 1).any())
+    else:
+        any_pull = args.delivery == "pull"
     hbm_peak, peak_kind = measured_peaks()
     G = wl["grid"] ** 3
     hh_ms = kt.hh_step_median_ms if kt.hh_step_median_ms > 0 else kt.hh_step_ms
@@ -372,7 +380,12 @@ def run_ours(args, wl: dict, dist, rank: int, local_rank: int) -> dict | None:
                "time_to_tol_ms": kt.solve_ms, "grid": wl["grid"]},
         "roofline": dominant, "roofline_other": other, "roofline_fp32": hh_fp32,
         "kernel_ms": {"k_hh_step": kt.hh_step_ms, "k_hh_step_median": kt.hh_step_median_ms,
-                      "k_deliver_push": kt.deliver_ms, "pcg_solve": kt.solve_ms, "samples": kt.samples},
+                      ("k_deliver_pull" if any_pull else "empty_delivery_slot"): kt.deliver_ms,
+                      "delivery": ("pull gather after the neuron update (mean over the steps, push steps "
+                                   "included)" if any_pull else
+                                   "push scatter fused into k_hh_step; empty_delivery_slot is the interval "
+                                   "between two timing events with no kernel between them"),
+                      "pcg_solve": kt.solve_ms, "samples": kt.samples},
         "gpu_launches": int(launches),
         "clocks": clock_info,
         "e2e": e2e,
